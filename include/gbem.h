@@ -1,0 +1,154 @@
+/*
+ * gbem.h -- C ABI of the GB300-native BEM hot path (matrix assembly and dense
+ * complex LU factor/solve) that stands in for SCUFF-EM's
+ *   RWGGeometry::AssembleBEMMatrix / AssembleBEMMatrixBlock   (libs/libscuff)
+ *   HMatrix::LUFactorize / HMatrix::LUSolve                  (libs/libhmat)
+ *
+ * Plain C types only; every call returns a gbem_status; no call aborts the
+ * process.  Matrices are column-major (entry (r,c) at r + c*ld), complex
+ * entries interleaved (re, im), as in HMatrix's ZM array
+ * (libs/libhmat/HMatrix.cc:333).  Pivots are LAPACK-style, 1-based.
+ *
+ * Threading: distinct handles may be used from distinct host threads; a
+ * handle is not re-entrant.  Each handle owns one CUDA stream.
+ */
+#ifndef GBEM_H
+#define GBEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GBEM_OK = 0,
+  GBEM_EINVAL = 1,    /* bad argument (the analogue of LAPACK info < 0) */
+  GBEM_ENOMEM = 2,    /* device or host allocation failed */
+  GBEM_ECUDA = 3,     /* a CUDA runtime error; see gbem_last_error() */
+  GBEM_ENOTSUP = 4,   /* valid request outside what this build implements */
+  GBEM_ESINGULAR = 5, /* zero pivot met (info > 0 is also returned) */
+  GBEM_ENOCONV = 6,   /* iterative refinement did not reach its tolerance */
+  GBEM_EMESH = 7,     /* non-manifold mesh topology */
+  GBEM_ETIMEOUT = 8   /* a bounded device-side wait gave up */
+} gbem_status;
+
+/* arithmetic of a matrix / of an assembly */
+typedef enum {
+  GBEM_C128 = 0,      /* complex double (the reference's ZM) */
+  GBEM_C64 = 1,       /* complex float */
+  GBEM_F64 = 2        /* real double (imaginary frequency; the reference's DM) */
+} gbem_dtype;
+
+/* precision of the far-field panel-pair cubature in an assembly */
+typedef enum {
+  GBEM_PREC_FP64 = 0, /* plain: everything in FP64 */
+  GBEM_PREC_MIXED = 1 /* far field in FP32, near/singular pairs in FP64 */
+} gbem_precision;
+
+typedef struct gbem_geometry gbem_geometry;
+typedef struct gbem_matrix gbem_matrix;
+
+/* A closed or open triangulated surface (one OBJECT of a .scuffgeo file). */
+typedef struct {
+  int num_vertices;
+  const double *vertices;      /* 3*num_vertices, already displaced/rotated */
+  int num_panels;
+  const int *panel_vertices;   /* 3*num_panels, 0-based vertex indices */
+  int exterior_region;         /* index of the region the normals point into */
+  int interior_region;         /* region inside; -1 for a PEC body */
+  int is_pec;
+} gbem_surface_desc;
+
+/* last error message of the calling thread (never NULL) */
+const char *gbem_last_error(void);
+/* library version string */
+const char *gbem_version(void);
+
+/* ---- geometry ---------------------------------------------------------- */
+/* Replaces RWGGeometry(const char *GeoFile) (libs/libscuff/RWGGeometry.cc:353)
+ * for the parts the hot path needs: panels (RWGSurface.cc:55-100), RWG edges
+ * (InitEdgeList.cc:47-371), basis-function offsets (RWGGeometry.cc:708-724),
+ * and the frequency-independent near-pair classification
+ * (AssessPanelPair.cc:52-172).  device: CUDA ordinal. */
+gbem_status gbem_geometry_create(int num_surfaces, const gbem_surface_desc *surfaces,
+                                 int num_regions, int device, gbem_geometry **out);
+gbem_status gbem_geometry_destroy(gbem_geometry *g);
+/* Total basis functions (RWGGeometry::TotalBFs, libscuff.h:555). */
+gbem_status gbem_geometry_num_bfs(const gbem_geometry *g, int *N);
+/* Per-surface edge table: 8 ints per edge (iV1 iV2 iQP iQM iPPanel iMPanel
+ * PIndex MIndex, libscuff.h:124-146) and edge lengths. */
+gbem_status gbem_geometry_edges(const gbem_geometry *g, int surface, int *num_edges,
+                                int *edge_table, double *lengths);
+/* Counts of near panel pairs by common-vertex number (0..3), for logging. */
+gbem_status gbem_geometry_near_counts(const gbem_geometry *g, long long counts[4]);
+
+/* ---- matrices ------------------------------------------------------------ */
+/* A device-resident N x N matrix (replaces AllocateBEMMatrix,
+ * AssembleBEMMatrix.cc:778-783). */
+gbem_status gbem_matrix_create(const gbem_geometry *g, int dtype, gbem_matrix **out);
+gbem_status gbem_matrix_destroy(gbem_matrix *m);
+gbem_status gbem_matrix_device_ptr(gbem_matrix *m, void **dptr, int *ld);
+gbem_status gbem_matrix_download(gbem_matrix *m, void *host, int ldh);
+gbem_status gbem_matrix_upload(gbem_matrix *m, const void *host, int ldh);
+
+/* Replaces RWGGeometry::AssembleBEMMatrix(cdouble Omega, HMatrix *M)
+ * (AssembleBEMMatrix.cc:684-765, compact geometries, kBloch = NULL).
+ * eps/mu: 2*num_regions doubles each (re, im) at this frequency (the values
+ * RWGGeometry::UpdateCachedEpsMuValues caches, RWGGeometry.cc:1093-1113).
+ * precision: gbem_precision.  The matrix dtype must be C128 for FP64 and
+ * C64 for MIXED (F64 is accepted for FP64 at purely imaginary Omega). */
+gbem_status gbem_assemble(gbem_geometry *g, double omega_re, double omega_im,
+                          const double *eps, const double *mu, int precision,
+                          gbem_matrix *M);
+
+/* Host-buffer variant with the reference's drop-in semantics: fills a host
+ * column-major complex128 N x N array (HMatrix::ZM) with leading dimension ld. */
+gbem_status gbem_assemble_host(gbem_geometry *g, double omega_re, double omega_im,
+                               const double *eps, const double *mu, double *ZM, int ld);
+
+/* ---- dense LU ------------------------------------------------------------ */
+/* Replaces HMatrix::LUFactorize (libs/libhmat/LBWrappers.cc:151-171):
+ * in-place LU with partial pivoting of a C128 (zgetrf semantics) or C64
+ * matrix.  ipiv (optional, host, N ints) receives 1-based pivots; info is 0,
+ * or k > 0 if U(k,k) is exactly zero. */
+gbem_status gbem_lu_factor(gbem_matrix *M, int *ipiv, int *info);
+
+/* Replaces HMatrix::LUSolve(HMatrix *X, char Trans, int nrhs)
+ * (LBWrappers.cc:208-236): solves op(M) X = B in place on a host
+ * column-major C128 (or C64 for a C64 factor) array B (N x nrhs, ldb);
+ * trans is 'N' or 'T'. */
+gbem_status gbem_lu_solve(gbem_matrix *M, char trans, int nrhs, void *B, int ldb);
+
+/* Host-buffer drop-in for LUFactorize on a whole HMatrix: factors the host
+ * column-major C128 array ZM (N x N, ld) in place and writes 1-based ipiv. */
+gbem_status gbem_lu_factor_host(double *ZM, int N, int ld, int *ipiv, int *info);
+/* Drop-in for LUSolve with host factors from gbem_lu_factor_host. */
+gbem_status gbem_lu_solve_host(const double *ZM, int N, int ld, const int *ipiv,
+                               char trans, int nrhs, double *B, int ldb);
+
+/* ---- mixed-precision solve ----------------------------------------------- */
+/* One BEM solve in the mixed form: assemble the matrix with an FP32 far
+ * field and FP64 near field into C64, factor it in complex FP32 with pivoting
+ * and tensor-core trailing updates, then refine x with FP64 residuals against
+ * the assembled matrix until ||b - M x|| <= tol ||b|| (or max_iter).
+ * B, X: host column-major C128 N x nrhs.  iters (optional) receives the
+ * refinement sweeps taken, resid the final relative residual. */
+gbem_status gbem_solve_mixed(gbem_geometry *g, double omega_re, double omega_im,
+                             const double *eps, const double *mu, int nrhs,
+                             const double *B, int ldb, double *X, int ldx,
+                             double tol, int max_iter, int *iters, double *resid);
+
+/* ---- right-hand sides ----------------------------------------------------- */
+/* Plane-wave right-hand side (AssembleRHSVector.cc:145-255 with a PlaneWave
+ * incident field, libs/libIncField/PlaneWave.cc): E0 (complex, 6 doubles),
+ * nhat (3 doubles); writes N complex128 entries to host rhs. */
+gbem_status gbem_rhs_planewave(gbem_geometry *g, double omega_re, double omega_im,
+                               const double *eps, const double *mu,
+                               const double *E0, const double *nhat, double *rhs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBEM_H */

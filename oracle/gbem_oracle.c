@@ -129,6 +129,11 @@ typedef struct {
   /* edges: iV1 iV2 iQP iQM iPPanel iMPanel PIndex MIndex */
   int *E;              /* 8*ne */
   double *elen;        /* ne */
+  /* memo of Q-independent FIPPI data per ordered same-surface panel pair
+     (the role of FIPPICache, FIPPICache.cc:135-187) */
+  long long *fkey;
+  void *fval;
+  int fcap;
 } ora_surface;
 
 /* Panel data (RWGSurface.cc:55-100). */
@@ -160,7 +165,7 @@ int ora_build_edges(int nv, int np, const int *PV, int *Eout, int maxe)
   long long *key = malloc(sizeof(long long) * cap);
   int *slot = malloc(sizeof(int) * cap);
   for (int i = 0; i < cap; i++) key[i] = -1;
-  int ntot = 6*np;
+  size_t ntot = 6 * (size_t)(np > 0 ? np : 1);
   int *tmp = malloc(sizeof(int) * 8 * ntot);
   int *tidx = malloc(sizeof(int) * ntot);
   int nt = 0, ne = 0, bad = 0;
@@ -645,7 +650,7 @@ static void qdfippi(const double *Va[3], const double *Qa, const double *Vb[3], 
 enum { ALG_LO = 0, ALG_HO = 1, ALG_TD = 2, ALG_HKTD = 3, ALG_DESING = 4 };
 
 /* quadrature orders used by the oracle (high: the oracle is the checker) */
-static int ORA_N_TD3 = 32, ORA_N_TD2 = 20, ORA_N_TD1 = 14, ORA_N_FIP0 = 24, ORA_N_FIP12 = 16;
+static int ORA_N_TD3 = 32, ORA_N_TD2 = 20, ORA_N_TD1 = 14, ORA_N_FIP0 = 16, ORA_N_FIP12 = 16;
 
 void ora_set_orders(int td3, int td2, int td1, int fip0, int fip12)
 { ORA_N_TD3 = td3; ORA_N_TD2 = td2; ORA_N_TD1 = td1; ORA_N_FIP0 = fip0; ORA_N_FIP12 = fip12; }
@@ -673,7 +678,28 @@ int ora_ppi(const ora_surface *Sa, int pa, int iQa, const ora_surface *Sb, int p
   /* desingularisation */
   ppi_cubature(k, 1, 0, Va, Qa, Vb, Qb, H);
   ora_qifippi Q;
-  ora_qifippi_compute(Va, Vb, ncv, ncv == 0 ? ORA_N_FIP0 : ORA_N_FIP12, &Q);
+  int cached = 0;
+  long long key = (long long)pa * Sa->np + pb;
+  ora_qifippi *tab = (ora_qifippi *)Sa->fval;
+  int slot = -1;
+  if (Sa == Sb && Sa->fcap) {
+    slot = (int)(((unsigned long long)key * 0x9E3779B97F4A7C15ULL) >> 33) & (Sa->fcap - 1);
+    #pragma omp critical(ora_fippi_cache)
+    {
+      while (Sa->fkey[slot] != -1 && Sa->fkey[slot] != key) slot = (slot + 1) & (Sa->fcap - 1);
+      if (Sa->fkey[slot] == key) { Q = tab[slot]; cached = 1; }
+    }
+  }
+  if (!cached) {
+    ora_qifippi_compute(Va, Vb, ncv, ncv == 0 ? ORA_N_FIP0 : ORA_N_FIP12, &Q);
+    if (slot >= 0) {
+      #pragma omp critical(ora_fippi_cache)
+      {
+        while (Sa->fkey[slot] != -1 && Sa->fkey[slot] != key) slot = (slot + 1) & (Sa->fcap - 1);
+        if (Sa->fkey[slot] == -1) { Sa->fkey[slot] = key; tab[slot] = Q; }
+      }
+    }
+  }
   ora_qdfippi D;
   qdfippi(Va, Qa, Vb, Qb, &Q, &D);
   cplx ik = I*k, ooik2 = 1.0/(ik*ik), PF[5];
@@ -704,6 +730,10 @@ ora_surface *ora_surface_new(int nv, const double *V, int np, const int *PV)
   if (S->ne < 0) S->ne = 0;
   S->elen = malloc(sizeof(double)*(S->ne > 0 ? S->ne : 1));
   for (int e = 0; e < S->ne; e++) S->elen[e] = vdist(S->V + 3*S->E[8*e], S->V + 3*S->E[8*e+1]);
+  S->fcap = 1; while (S->fcap < 256*np) S->fcap <<= 1;
+  S->fkey = malloc(sizeof(long long)*S->fcap);
+  for (int i = 0; i < S->fcap; i++) S->fkey[i] = -1;
+  S->fval = malloc(sizeof(ora_qifippi)*S->fcap);
   return S;
 }
 
@@ -711,7 +741,7 @@ void ora_surface_free(ora_surface *S)
 {
   if (!S) return;
   free((void*)S->V); free((void*)S->PV); free(S->centroid); free(S->radius); free(S->area);
-  free(S->E); free(S->elen); free(S);
+  free(S->E); free(S->elen); free(S->fkey); free(S->fval); free(S);
 }
 
 int ora_surface_num_edges(const ora_surface *S) { return S->ne; }

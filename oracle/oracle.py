@@ -1,0 +1,117 @@
+"""ctypes wrapper of the CPU oracle (oracle/gbem_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
+by bench.py's CPU-baseline leg as the checker.  The product never calls it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "gbem_oracle.c")
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+REFDUMP = os.path.join(HERE, "_ref", "refdump")
+
+ALG_NAMES = {0: "LO", 1: "HO", 2: "TD", 3: "HKTD", 4: "DESING"}
+
+
+def build():
+    """Compile the oracle (gcc, OpenMP)."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    tmp = LIB + ".tmp"
+    subprocess.run(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-w", "-ffp-contract=off", "-o", tmp, SRC, "-lm"],
+                   check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_reference(ref="/root/reference", jobs=8):
+    """Build the reference from its sources into oracle/_ref (only where the
+    reference tree exists; the GPU host uses the committed fixtures)."""
+    if not os.path.isdir(ref):
+        return None
+    subprocess.run(["make", "-C", os.path.join(HERE, "ref"), "REF=" + ref, "-j%d" % jobs], check=True,
+                   capture_output=True)
+    return REFDUMP
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        L.ora_surface_new.restype = P
+        L.ora_surface_new.argtypes = [I, P, I, P]
+        L.ora_surface_free.argtypes = [P]
+        L.ora_surface_num_edges.argtypes = [P]
+        L.ora_surface_edges.argtypes = [P, P, P]
+        L.ora_ppi_c.argtypes = [P, I, I, I, I, D, D, P, P]
+        L.ora_qifippi_c.argtypes = [P, I, I, I, P, P]
+        L.ora_set_orders.argtypes = [I, I, I, I, I]
+        L.ora_assemble.argtypes = [I, P, P, P, D, D, P, P, P, I]
+        _lib = L
+    return _lib
+
+
+class Surface:
+    def __init__(self, V, P):
+        self.V = np.ascontiguousarray(V, dtype=np.float64)
+        self.P = np.ascontiguousarray(P, dtype=np.int32)
+        self.h = lib().ora_surface_new(len(self.V), self.V.ctypes.data, len(self.P), self.P.ctypes.data)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ora_surface_free(self.h)
+            self.h = None
+
+    def edges(self):
+        n = lib().ora_surface_num_edges(self.h)
+        E = np.zeros((n, 8), dtype=np.int32)
+        L = np.zeros(n)
+        lib().ora_surface_edges(self.h, E.ctypes.data, L.ctypes.data)
+        return E, L
+
+    def ppi(self, pa, iqa, pb, iqb, k):
+        k = complex(k)
+        H = np.zeros(4)
+        ncv = ctypes.c_int()
+        alg = lib().ora_ppi_c(self.h, pa, iqa, pb, iqb, k.real, k.imag, H.ctypes.data, ctypes.byref(ncv))
+        return np.array([H[0] + 1j * H[1], H[2] + 1j * H[3]]), alg, ncv.value
+
+    def qifippi(self, pa, pb, n=24):
+        out = np.zeros(33)
+        order = np.zeros(6, dtype=np.int32)
+        ncv = lib().ora_qifippi_c(self.h, pa, pb, n, out.ctypes.data, order.ctypes.data)
+        return out, ncv, order
+
+
+def assemble(surfaces, regions, pec, omega, eps, mu):
+    """Full BEM matrix of a compact geometry (complex128, N x N).
+
+    surfaces: list of Surface; regions: list of (exterior, interior) region
+    indices; pec: list of bools; eps/mu: complex per region."""
+    N = sum(s.edges()[0].shape[0] * (1 if p else 2) for s, p in zip(surfaces, pec))
+    handles = (ctypes.c_void_p * len(surfaces))(*[s.h for s in surfaces])
+    reg = np.array([r for pair in regions for r in pair], dtype=np.int32)
+    pe = np.array([1 if p else 0 for p in pec], dtype=np.int32)
+    ep = np.array([[complex(e).real, complex(e).imag] for e in eps], dtype=np.float64).ravel()
+    mm = np.array([[complex(m).real, complex(m).imag] for m in mu], dtype=np.float64).ravel()
+    M = np.zeros((N, N), dtype=np.complex128, order="F")
+    omega = complex(omega)
+    lib().ora_assemble(len(surfaces), handles, reg.ctypes.data, pe.ctypes.data, omega.real, omega.imag,
+                       ep.ctypes.data, mm.ctypes.data, M.ctypes.data, N)
+    return M
+
+
+def set_orders(td3=32, td2=20, td1=14, fip0=24, fip12=16):
+    lib().ora_set_orders(td3, td2, td1, fip0, fip12)

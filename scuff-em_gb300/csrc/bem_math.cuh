@@ -1,0 +1,537 @@
+// bem_math.cuh -- panel-pair integration math shared by the assembly kernels.
+//
+// All functions are __host__ __device__ so the same code runs in the CUDA
+// kernels and (for debugging only) on the host.
+//
+// Conventions
+//  * A panel with vertices (V0, V1, V2) in mesh order is parametrised as
+//    x = V0 + u A + v B, A = V1 - V0, B = V2 - V0, u, v >= 0, u + v <= 1
+//    (the triangle-cubature convention of libs/libTriInt/TCR.cc); integrals
+//    are over parameter space (area 1/2 per panel), so the RWG normalisation
+//    leaves the factor La*Lb (EdgeEdgeInteractions.cc:183-188).
+//  * For a panel pair the library keeps 9+9 "bilinear moments"
+//       MG[m] = int int mono_m G(r),  MP[m] = int int mono_m Psi(r),
+//    mono_m over {1, u', v', u, uu', uv', v, vu', vv'} (primes: second panel),
+//    G = e^{ikr}/(4 pi r), Psi = G (ik - 1/r)/r.  The reference's per-edge
+//    integrands (PanelPanelInteractions.cc:108-201)
+//       H0 = int int ((x-Qa).(x'-Qb) - 4/k^2) G,
+//       H1 = int int ((x-Qa) x (x'-Qb)).(x-x') Psi
+//    are bilinear in (x-Qa, x'-Qb); since ((x-Qa)x(x'-Qb)).(x-x') equals
+//    ((x-Qa)x(x'-Qb)).(Qa-Qb) pointwise, both follow from the moments for all
+//    9 choices of (Qa, Qb) without re-integrating (the reference integrates
+//    each of the up-to-9 edge pairs sharing a panel pair separately).
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+#define GB_HD __host__ __device__ __forceinline__
+
+namespace gbem {
+
+template <typename T> struct cx { T re, im; };
+template <typename T> GB_HD cx<T> mk(T a, T b) { cx<T> z; z.re = a; z.im = b; return z; }
+template <typename T> GB_HD cx<T> operator+(cx<T> a, cx<T> b) { return mk(a.re + b.re, a.im + b.im); }
+template <typename T> GB_HD cx<T> operator-(cx<T> a, cx<T> b) { return mk(a.re - b.re, a.im - b.im); }
+template <typename T> GB_HD cx<T> operator*(cx<T> a, cx<T> b) { return mk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
+template <typename T> GB_HD cx<T> operator*(T s, cx<T> a) { return mk(s * a.re, s * a.im); }
+template <typename T> GB_HD cx<T> cdiv(cx<T> a, cx<T> b) {
+  T d = b.re * b.re + b.im * b.im;
+  return mk((a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d);
+}
+template <typename T> GB_HD T cnorm2(cx<T> a) { return a.re * a.re + a.im * a.im; }
+template <typename T> GB_HD cx<T> cexpo(cx<T> z) {
+  T e = exp(z.re), s, c;
+#ifdef __CUDA_ARCH__
+  sincos(z.im, &s, &c);
+#else
+  s = sin(z.im); c = cos(z.im);
+#endif
+  return mk(e * c, e * s);
+}
+
+GB_HD double vdot(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+GB_HD void vcross(const double* a, const double* b, double* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+GB_HD double vdet(const double* a, const double* b, const double* c) {
+  double t[3];
+  vcross(a, b, t);
+  return vdot(t, c);
+}
+
+// ExpRel(x, 4) = sum_{m>=4} x^m/m!, summed until a term falls below 1e-8 of
+// the running sum (PanelPanelInteractions.cc:86-103; same truncation so the
+// desingularised remainder matches the reference term for term).
+GB_HD cx<double> exprel4(cx<double> x) {
+  cx<double> term = mk(1.0, 0.0);
+  for (int m = 1; m < 4; m++) term = (1.0 / m) * (term * x);
+  cx<double> sum = mk(0.0, 0.0);
+  for (int m = 4; m < 100; m++) {
+    term = (1.0 / m) * (term * x);
+    sum = sum + term;
+    if (cnorm2(term) < 1.0e-16 * cnorm2(sum)) break;
+  }
+  return sum;
+}
+
+// ---------------------------------------------------------------------------
+// Bilinear moments by a fixed product rule (LO 6x6 far field, desingularised
+// remainder, HO).  Geometry is given relative to each panel's V0:
+//   D0 = V0a - V0b; (Aa, Ba), (Ab, Bb) edge vectors in TCR convention.
+// Kernel selector: 0 = full Helmholtz, 1 = desingularised (ExpRel(ikr,4)).
+// ---------------------------------------------------------------------------
+template <typename T> struct PairGeom {
+  T D0[3], Aa[3], Ba[3], Ab[3], Bb[3];
+};
+
+GB_HD void sincos_t(float x, float* s, float* c) {
+#ifdef __CUDA_ARCH__
+  sincosf(x, s, c);
+#else
+  *s = sinf(x); *c = cosf(x);
+#endif
+}
+GB_HD void sincos_t(double x, double* s, double* c) {
+#ifdef __CUDA_ARCH__
+  sincos(x, s, c);
+#else
+  *s = sin(x); *c = cos(x);
+#endif
+}
+GB_HD float exp_t(float x) { return expf(x); }
+GB_HD double exp_t(double x) { return exp(x); }
+GB_HD float rsqrt_t(float x) {
+#ifdef __CUDA_ARCH__
+  return rsqrtf(x);
+#else
+  return 1.0f / sqrtf(x);
+#endif
+}
+GB_HD double rsqrt_t(double x) { return 1.0 / sqrt(x); }
+
+// Phi = e^{ikr}/(4 pi r), Psi = Phi (ik - 1/r)/r, both times the weight w.
+template <typename T>
+GB_HD void helmholtz_pp(T r2, cx<T> k, T w, cx<T>* phi, cx<T>* psi) {
+  const T inv4pi = (T)0.079577471545947667884;  // 1/(4 pi)
+  T rinv = rsqrt_t(r2);
+  T r = r2 * rinv;
+  T s, c;
+  sincos_t(k.re * r, &s, &c);
+  T amp = w * inv4pi * rinv;
+  if (k.im != (T)0) amp *= exp_t(-k.im * r);
+  cx<T> p = mk(amp * c, amp * s);
+  // (ik - 1/r)/r = (-k.im - 1/r + i k.re)/r
+  cx<T> f = mk((-k.im - rinv) * rinv, k.re * rinv);
+  *phi = p;
+  *psi = p * f;
+}
+
+GB_HD void desing_pp(double r2, cx<double> k, double w, cx<double>* phi, cx<double>* psi) {
+  const double inv4pi = 0.079577471545947667884;
+  double r = sqrt(r2), rinv = 1.0 / r;
+  cx<double> ikr = mk(-k.im * r, k.re * r);
+  cx<double> p = (w * inv4pi * rinv) * exprel4(ikr);
+  cx<double> f = mk((-k.im - rinv) * rinv, k.re * rinv);
+  *phi = p;
+  *psi = p * f;
+}
+
+// rule: npts triples (u, v, w)
+template <typename T, int DESING>
+GB_HD void pair_moments(const PairGeom<T>& g, cx<T> k, const T* rule, int npts, cx<T>* MG, cx<T>* MP) {
+  for (int m = 0; m < 9; m++) { MG[m] = mk((T)0, (T)0); MP[m] = mk((T)0, (T)0); }
+  for (int i = 0; i < npts; i++) {
+    T u = rule[3 * i], v = rule[3 * i + 1], wi = rule[3 * i + 2];
+    T pa[3];
+    for (int c = 0; c < 3; c++) pa[c] = g.D0[c] + u * g.Aa[c] + v * g.Ba[c];
+    cx<T> SG[3], SP[3];
+    for (int b = 0; b < 3; b++) { SG[b] = mk((T)0, (T)0); SP[b] = mk((T)0, (T)0); }
+    for (int j = 0; j < npts; j++) {
+      T up = rule[3 * j], vp = rule[3 * j + 1], wj = rule[3 * j + 2];
+      T R0 = pa[0] - up * g.Ab[0] - vp * g.Bb[0];
+      T R1 = pa[1] - up * g.Ab[1] - vp * g.Bb[1];
+      T R2 = pa[2] - up * g.Ab[2] - vp * g.Bb[2];
+      T r2 = R0 * R0 + R1 * R1 + R2 * R2;
+      cx<T> phi, psi;
+      if constexpr (DESING) desing_pp(r2, k, wj, &phi, &psi);
+      else helmholtz_pp(r2, k, wj, &phi, &psi);
+      SG[0] = SG[0] + phi; SP[0] = SP[0] + psi;
+      SG[1] = SG[1] + up * phi; SP[1] = SP[1] + up * psi;
+      SG[2] = SG[2] + vp * phi; SP[2] = SP[2] + vp * psi;
+    }
+    T a[3] = {wi, wi * u, wi * v};
+    for (int al = 0; al < 3; al++)
+      for (int b = 0; b < 3; b++) {
+        MG[3 * al + b] = MG[3 * al + b] + a[al] * SG[b];
+        MP[3 * al + b] = MP[3 * al + b] + a[al] * SP[b];
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Combination coefficients for one (Qa, Qb) choice.  ja, jb = local vertex
+// index of Q in each panel (mesh order).  Computed in double from the
+// panels' double geometry.
+//   c[m] = a_al . b_be,   d[m] = (a_al x b_be) . (Qa - Qb)
+// with a_1 = V0a - Qa, a_u = Aa, a_v = Ba (likewise b), m = 3 al + be.
+// ---------------------------------------------------------------------------
+GB_HD void combo_coeffs(const double* Va, const double* Vb, int ja, int jb, double* c, double* d) {
+  double A[3], B[3], Ap[3], Bp[3], a0[3], b0[3], QmQ[3];
+  for (int i = 0; i < 3; i++) {
+    A[i] = Va[3 + i] - Va[i]; B[i] = Va[6 + i] - Va[i];
+    Ap[i] = Vb[3 + i] - Vb[i]; Bp[i] = Vb[6 + i] - Vb[i];
+    a0[i] = Va[i] - Va[3 * ja + i];
+    b0[i] = Vb[i] - Vb[3 * jb + i];
+    QmQ[i] = Va[3 * ja + i] - Vb[3 * jb + i];
+  }
+  const double* av[3] = {a0, A, B};
+  const double* bv[3] = {b0, Ap, Bp};
+  for (int al = 0; al < 3; al++)
+    for (int be = 0; be < 3; be++) {
+      c[3 * al + be] = vdot(av[al], bv[be]);
+      d[3 * al + be] = vdet(av[al], bv[be], QmQ);
+    }
+}
+
+// H0 = sum c MG - (4/k^2) MG[0];  H1 = sum d MP.
+template <typename T>
+GB_HD void combine(const cx<T>* MG, const cx<T>* MP, const T* c, const T* d, cx<T> m4ok2, cx<T>* H0, cx<T>* H1) {
+  cx<T> h0 = m4ok2 * MG[0], h1 = mk((T)0, (T)0);
+  for (int m = 0; m < 9; m++) {
+    h0 = h0 + c[m] * MG[m];
+    h1 = h1 + d[m] * MP[m];
+  }
+  *H0 = h0;
+  *H1 = h1;
+}
+
+// ---------------------------------------------------------------------------
+// Radial moments E_n(z) = int_0^1 w^n e^{zw} dw, n = 0..NMAX.
+// ---------------------------------------------------------------------------
+template <int NMAX>
+GB_HD void expint_moments(cx<double> z, cx<double>* E) {
+  double az2 = cnorm2(z);
+  if (az2 < 4.0) {
+    for (int n = 0; n <= NMAX; n++) {
+      cx<double> term = mk(1.0, 0.0), sum = mk(1.0 / (n + 1.0), 0.0);
+      for (int m = 1; m < 60; m++) {
+        term = (1.0 / m) * (term * z);
+        cx<double> t = (1.0 / (n + m + 1.0)) * term;
+        sum = sum + t;
+        if (cnorm2(t) < 1e-36 * cnorm2(sum)) break;
+      }
+      E[n] = sum;
+    }
+  } else {
+    cx<double> ez = cexpo(z);
+    E[0] = cdiv(ez - mk(1.0, 0.0), z);
+    for (int n = 1; n <= NMAX; n++) E[n] = cdiv(ez - (double)n * E[n - 1], z);
+  }
+}
+
+// small real polynomials in the radial variable w (degree < 8)
+struct rpoly {
+  double c[8];
+};
+GB_HD rpoly rp_aff(double a0, double a1) {
+  rpoly p;
+  for (int i = 0; i < 8; i++) p.c[i] = 0.0;
+  p.c[0] = a0; p.c[1] = a1;
+  return p;
+}
+GB_HD rpoly rp_mul(const rpoly& a, const rpoly& b) {
+  rpoly p;
+  for (int i = 0; i < 8; i++) p.c[i] = 0.0;
+  for (int i = 0; i < 8; i++)
+    for (int j = 0; i + j < 8; j++) p.c[i + j] += a.c[i] * b.c[j];
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// Self-panel (common-triangle) Helmholtz moments MG[9] (H1 vanishes for a
+// flat panel).  The 4-D integral over the pair is split as s = s' + z:
+// z runs over the 6 sectors of the hexagon T - T in polar form z = w zh(t),
+// s' over T ∩ (T - z), a copy of T scaled by lambda(w) = 1 - w sig(zh)
+// (integrated exactly by a degree-2 rule), and w analytically against
+// e^{ikwX}: the generalized Taylor-Duffy reduction of a common-triangle
+// integral to a 1-D smooth integral (TaylorDuffy.cc:152-258 does the same
+// reduction with symbolic polynomial tables).  Panel parameters here are the
+// edge-ordered ones, s = (s1, s2), x = V0 + s1 (V1-V0) + s2 (V2-V1),
+// 0 <= s2 <= s1 <= 1, i.e. TCR (u, v) = (s1 - s2, s2).
+//   gx, gw: Gauss-Legendre rule on [0,1] with nt points.
+// ---------------------------------------------------------------------------
+GB_HD void self_moments(const double* V, cx<double> k, const double* gx, const double* gw, int nt, cx<double>* MG) {
+  const double inv4pi = 0.079577471545947667884;
+  double E1[3], E2[3];
+  for (int i = 0; i < 3; i++) { E1[i] = V[3 + i] - V[i]; E2[i] = V[6 + i] - V[3 + i]; }
+  const double H[7][2] = {{1, 0}, {1, 1}, {0, 1}, {-1, 0}, {-1, -1}, {0, -1}, {1, 0}};
+  const double TP[3][2] = {{0.5, 0.0}, {1.0, 0.5}, {0.5, 0.5}};
+  for (int m = 0; m < 9; m++) MG[m] = mk(0.0, 0.0);
+  for (int sct = 0; sct < 6; sct++)
+    for (int it = 0; it < nt; it++) {
+      double t = gx[it];
+      double z0 = H[sct][0] + t * (H[sct + 1][0] - H[sct][0]);
+      double z1 = H[sct][1] + t * (H[sct + 1][1] - H[sct][1]);
+      double am = z1 < 0 ? -z1 : 0.0, bm = z0 > 0 ? z0 : 0.0, cm = (z0 - z1) < 0 ? (z0 - z1) : 0.0;
+      double sig = bm + am - cm;
+      double D[3];
+      for (int i = 0; i < 3; i++) D[i] = z0 * E1[i] + z1 * E2[i];
+      double X = sqrt(vdot(D, D));
+      cx<double> E[7];
+      expint_moments<6>(mk(-k.im * X, k.re * X), E);
+      rpoly lam = rp_aff(1.0, -sig);
+      rpoly om = rp_mul(lam, lam);  // w lambda^2 / w  (the 1/w of G is taken here)
+      double W = gw[it] * (1.0 / 6.0) * inv4pi / X;
+      for (int ip = 0; ip < 3; ip++) {
+        double p1 = TP[ip][0], p2 = TP[ip][1];
+        // s' = (p1, p2) + w ((am - cm) - sig p1, am - sig p2);  s = s' + w z
+        double sb0 = p1, sb1 = (am - cm) - sig * p1, tb0 = p2, tb1 = am - sig * p2;
+        double sa0 = sb0, sa1 = sb1 + z0, ta0 = tb0, ta1 = tb1 + z1;
+        // TCR coordinates u = s1 - s2, v = s2
+        rpoly ua = rp_aff(sa0 - ta0, sa1 - ta1), va = rp_aff(ta0, ta1);
+        rpoly ub = rp_aff(sb0 - tb0, sb1 - tb1), vb = rp_aff(tb0, tb1);
+        rpoly one = rp_aff(1.0, 0.0);
+        const rpoly ma[3] = {one, ua, va}, mb[3] = {one, ub, vb};
+        for (int al = 0; al < 3; al++)
+          for (int be = 0; be < 3; be++) {
+            rpoly q = rp_mul(om, rp_mul(ma[al], mb[be]));
+            cx<double> s = mk(0.0, 0.0);
+            for (int n = 0; n < 7; n++) s = s + q.c[n] * E[n];
+            MG[3 * al + be] = MG[3 * al + be] + W * s;
+          }
+      }
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Frequency-independent near-pair table (the data the reference caches as
+// QIFIPPIData, libscuffInternals.h:282-292), in the TCR mesh-order basis:
+//   RM1[9], R1[9], R2[9] = int int mono_m r^p  (p = -1, 1, 2)
+//   XM[3] = int int (x - x')/r^3,  XX[3] = int int (xi x xi')/r^3,
+// xi = x - V0a (panel a's first mesh vertex).  33 doubles per pair.
+// ---------------------------------------------------------------------------
+struct Fippi {
+  double RM1[9], R1[9], R2[9], XM[3], XX[3];
+};
+
+// Segment integrals along the second panel's v' direction (closed forms of
+// int (t^2+b2)^{p/2} t^j dt), p = -3, -1, 1, 2; j = 0, 1
+// (QIFIPPICubature.cc:240-300 evaluates the same integrals).
+GB_HD void seg_integrals(double a2, double v0, double b2, double up, double J[4][2]) {
+  double a = sqrt(a2);
+  double t1 = -v0, t2 = up - v0;
+  double S1 = sqrt(t1 * t1 + b2), S2 = sqrt(t2 * t2 + b2);
+  double L;
+  if (t1 >= 0) L = log((t2 + S2) / (t1 + S1));
+  else if (t2 <= 0) L = log((S1 - t1) / (S2 - t2));
+  else L = log((t2 + S2) * (S1 - t1) / b2);
+  double Im3_0;
+  if (t1 * t2 > 0) Im3_0 = (t2 * t2 - t1 * t1) / (S1 * S2 * (t2 * S1 + t1 * S2));
+  else Im3_0 = (t2 / S2 - t1 / S1) / b2;
+  double Im3_1 = 1.0 / S1 - 1.0 / S2;
+  double Im1_0 = L, Im1_1 = S2 - S1;
+  double I1_0 = 0.5 * (t2 * S2 - t1 * S1 + b2 * L), I1_1 = (S2 * S2 * S2 - S1 * S1 * S1) / 3.0;
+  double I2_0 = (t2 * t2 * t2 - t1 * t1 * t1) / 3.0 + b2 * (t2 - t1);
+  double q1 = t1 * t1 + b2, q2 = t2 * t2 + b2;
+  double I2_1 = (q2 * q2 - q1 * q1) / 4.0;
+  J[0][0] = Im3_0 / (a2 * a); J[0][1] = (Im3_1 + v0 * Im3_0) / (a2 * a);
+  J[1][0] = Im1_0 / a;        J[1][1] = (Im1_1 + v0 * Im1_0) / a;
+  J[2][0] = I1_0 * a;         J[2][1] = (I1_1 + v0 * I1_0) * a;
+  J[3][0] = I2_0 * a2;        J[3][1] = (I2_1 + v0 * I2_0) * a2;
+}
+
+GB_HD void fippi_zero(Fippi* F) {
+  for (int m = 0; m < 9; m++) { F->RM1[m] = 0; F->R1[m] = 0; F->R2[m] = 0; }
+  for (int i = 0; i < 3; i++) { F->XM[i] = 0; F->XX[i] = 0; }
+}
+
+// Non-touching near pair: v' integrated in closed form, (u, v/u, u') by a
+// tensor Gauss-Legendre rule (the 3-D scheme of QIFIPPICubature.cc:187-325).
+// Va, Vb: 9 doubles each, mesh vertex order.
+GB_HD void fippi_far(const double* Va, const double* Vb, const double* gx, const double* gw, int n, Fippi* F) {
+  double A[3], B[3], Ap[3], Bp[3];
+  for (int i = 0; i < 3; i++) {
+    A[i] = Va[3 + i] - Va[i]; B[i] = Va[6 + i] - Va[3 + i];
+    Ap[i] = Vb[3 + i] - Vb[i]; Bp[i] = Vb[6 + i] - Vb[3 + i];
+  }
+  double a2 = vdot(Bp, Bp);
+  fippi_zero(F);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      for (int l = 0; l < n; l++) {
+        double u = gx[i], v = u * gx[j], up = gx[l];
+        double W = gw[i] * gw[j] * gw[l] * u;
+        double X[3], Z[3], Y[3], Xo[3], Zo[3];
+        for (int m = 0; m < 3; m++) {
+          Xo[m] = u * A[m] + v * B[m];                 // x - V0a
+          Zo[m] = (Vb[m] - Va[m]) + up * Ap[m];        // z - V0a
+          X[m] = Xo[m]; Z[m] = Zo[m];
+          Y[m] = X[m] - Z[m];
+        }
+        double v0 = vdot(Bp, Y) / a2;
+        double b2 = vdot(Y, Y) / a2 - v0 * v0;
+        if (b2 < 0) b2 = 0;
+        double J[4][2];
+        seg_integrals(a2, v0, b2, up, J);
+        for (int m = 0; m < 3; m++) F->XM[m] += W * (Y[m] * J[0][0] - Bp[m] * J[0][1]);
+        double XZ[3], XB[3];
+        vcross(Xo, Zo, XZ); vcross(Xo, Bp, XB);
+        for (int m = 0; m < 3; m++) F->XX[m] += W * (XZ[m] * J[0][0] + XB[m] * J[0][1]);
+        // TCR a-side monomials {1, u - v, v}; b-side {1, u' - v', v'}
+        double ma[3] = {1.0, u - v, v};
+        for (int al = 0; al < 3; al++) {
+          double f = W * ma[al];
+          F->RM1[3 * al + 0] += f * J[1][0]; F->RM1[3 * al + 1] += f * (up * J[1][0] - J[1][1]); F->RM1[3 * al + 2] += f * J[1][1];
+          F->R1[3 * al + 0] += f * J[2][0];  F->R1[3 * al + 1] += f * (up * J[2][0] - J[2][1]);  F->R1[3 * al + 2] += f * J[2][1];
+          F->R2[3 * al + 0] += f * J[3][0];  F->R2[3 * al + 1] += f * (up * J[3][0] - J[3][1]);  F->R2[3 * al + 2] += f * J[3][1];
+        }
+      }
+}
+
+// Touching pair (ncv = 1 common vertex, 2 common edge).  pa/pb map the
+// common-vertices-first order to mesh order (E_i = V[p[i]]).  Duffy splits:
+//  ncv=1: s1 = w, s2 = w al, s1' = w be, s2' = w be ga (and mirror), w^3 be;
+//  ncv=2: (u-u', v, v') = w zhat over 4 polyhedral pieces, u' on its
+//         interval of length 1-w (exact 2-point rule), w^2 (1-w).
+// Edge-ordered parameters s: x = E0 + s1 (E1-E0) + s2 (E2-E1).
+struct DuffyPt {
+  double W;       // constant weight
+  rpoly om;       // Jacobian polynomial in w
+  double sa0[2], sa1[2], sb0[2], sb1[2];
+};
+
+GB_HD void tcr_from_edge(const int* perm, const double* s0, const double* s1, rpoly* u, rpoly* v) {
+  // barycentrics on (E0,E1,E2): (1 - s1, s1 - s2, s2), affine in w
+  double m0[3] = {1.0 - s0[0], s0[0] - s0[1], s0[1]};
+  double m1[3] = {-s1[0], s1[0] - s1[1], s1[1]};
+  int inv[3];
+  for (int i = 0; i < 3; i++) inv[perm[i]] = i;
+  *u = rp_aff(m0[inv[1]], m1[inv[1]]);
+  *v = rp_aff(m0[inv[2]], m1[inv[2]]);
+}
+
+GB_HD void fippi_touch_point(const double* Ea, const double* Eb, const int* pa, const int* pb, const double* V0a,
+                             const DuffyPt& pt, Fippi* F) {
+  double A[3], B[3], Ap[3], Bp[3], D[3];
+  for (int i = 0; i < 3; i++) {
+    A[i] = Ea[3 + i] - Ea[i]; B[i] = Ea[6 + i] - Ea[3 + i];
+    Ap[i] = Eb[3 + i] - Eb[i]; Bp[i] = Eb[6 + i] - Eb[3 + i];
+    D[i] = pt.sa1[0] * A[i] + pt.sa1[1] * B[i] - pt.sb1[0] * Ap[i] - pt.sb1[1] * Bp[i];
+  }
+  double X = sqrt(vdot(D, D));
+  rpoly ua, va, ub, vb;
+  tcr_from_edge(pa, pt.sa0, pt.sa1, &ua, &va);
+  tcr_from_edge(pb, pt.sb0, pt.sb1, &ub, &vb);
+  rpoly one = rp_aff(1.0, 0.0);
+  const rpoly ma[3] = {one, ua, va}, mb[3] = {one, ub, vb};
+  for (int al = 0; al < 3; al++)
+    for (int be = 0; be < 3; be++) {
+      rpoly q = rp_mul(pt.om, rp_mul(ma[al], mb[be]));
+      double sm1 = 0, s1 = 0, s2 = 0;
+      for (int n = 1; n < 8; n++) {
+        sm1 += q.c[n] / n;
+        s1 += q.c[n] / (n + 2.0);
+        s2 += q.c[n] / (n + 3.0);
+      }
+      F->RM1[3 * al + be] += pt.W * sm1 / X;
+      F->R1[3 * al + be] += pt.W * s1 * X;
+      F->R2[3 * al + be] += pt.W * s2 * X * X;
+    }
+  double om2 = 0;
+  for (int n = 2; n < 8; n++) om2 += pt.om.c[n] / (n - 1.0);
+  double X3 = X * X * X;
+  for (int m = 0; m < 3; m++) F->XM[m] += pt.W * om2 * D[m] / X3;
+  // xi(w) = x(w) - V0a; (xi x xi')/r^3 -> -(xi(w) x D) w / (w^3 X^3)
+  rpoly xi[3];
+  for (int m = 0; m < 3; m++)
+    xi[m] = rp_aff(Ea[m] - V0a[m] + pt.sa0[0] * A[m] + pt.sa0[1] * B[m], pt.sa1[0] * A[m] + pt.sa1[1] * B[m]);
+  for (int m = 0; m < 3; m++) {
+    int m1 = (m + 1) % 3, m2 = (m + 2) % 3;
+    rpoly cxm;
+    for (int i = 0; i < 8; i++) cxm.c[i] = xi[m1].c[i] * D[m2] - xi[m2].c[i] * D[m1];
+    rpoly q = rp_mul(pt.om, cxm);
+    double s = 0;
+    for (int n = 2; n < 8; n++) s += q.c[n] / (n - 1.0);
+    F->XX[m] += -pt.W * s / X3;
+  }
+}
+
+GB_HD void fippi_touch(int ncv, const double* Va, const double* Vb, const int* pa, const int* pb, const double* gx,
+                       const double* gw, int n, Fippi* F) {
+  double Ea[9], Eb[9];
+  for (int i = 0; i < 3; i++)
+    for (int c = 0; c < 3; c++) { Ea[3 * i + c] = Va[3 * pa[i] + c]; Eb[3 * i + c] = Vb[3 * pb[i] + c]; }
+  fippi_zero(F);
+  DuffyPt pt;
+  if (ncv == 1) {
+    for (int reg = 0; reg < 2; reg++)
+      for (int i1 = 0; i1 < n; i1++)
+        for (int i2 = 0; i2 < n; i2++)
+          for (int i3 = 0; i3 < n; i3++) {
+            double al = gx[i1], be = gx[i2], ga = gx[i3];
+            pt.sa0[0] = pt.sa0[1] = pt.sb0[0] = pt.sb0[1] = 0.0;
+            double* s0 = reg == 0 ? pt.sa1 : pt.sb1;
+            double* s1 = reg == 0 ? pt.sb1 : pt.sa1;
+            s0[0] = 1.0; s0[1] = al; s1[0] = be; s1[1] = be * ga;
+            pt.om = rp_aff(0.0, 0.0); pt.om.c[3] = be;
+            pt.W = gw[i1] * gw[i2] * gw[i3];
+            fippi_touch_point(Ea, Eb, pa, pb, Va, pt, F);
+          }
+  } else {
+    const double tx[2] = {0.21132486540518711775, 0.78867513459481288225};
+    for (int reg = 0; reg < 4; reg++)
+      for (int ia = 0; ia < n; ia++)
+        for (int ib = 0; ib < n; ib++) {
+          double al = gx[ia], be = gx[ib], z[3], J, lo;
+          if (reg == 0) { z[0] = 1.0 - al; z[1] = be; z[2] = al; J = 1.0; lo = al; }
+          else if (reg == 1) { z[0] = al; z[1] = 1.0; z[2] = (1.0 - al) * be; J = 1.0 - al; lo = 1.0 - al; }
+          else if (reg == 2) { z[0] = -al; z[1] = (1.0 - al) * be; z[2] = 1.0; J = 1.0 - al; lo = 1.0; }
+          else { z[0] = -al; z[1] = 1.0 - al; z[2] = be; J = 1.0; lo = 1.0; }
+          for (int it = 0; it < 2; it++) {
+            double tau = tx[it];
+            pt.sb0[0] = tau; pt.sb1[0] = lo - tau;
+            pt.sb0[1] = 0.0; pt.sb1[1] = z[2];
+            pt.sa0[0] = tau; pt.sa1[0] = lo - tau + z[0];
+            pt.sa0[1] = 0.0; pt.sa1[1] = z[1];
+            pt.om = rp_aff(0.0, 0.0); pt.om.c[2] = 1.0; pt.om.c[3] = -1.0;
+            pt.W = gw[ia] * gw[ib] * 0.5 * J;
+            fippi_touch_point(Ea, Eb, pa, pb, Va, pt, F);
+          }
+        }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Desingularised near pair (PanelPanelInteractions.cc:504-559): the fixed-rule
+// moments of the ExpRel(ikr,4) remainder plus the Taylor terms rebuilt from
+// the static table.  Adds to MG/MP; returns the extra r^-3 term of H1 per
+// (Qa,Qb) through hTimesRM3 = (Qa-Qb).XX + (Qa x Qb).XM (origin V0a), which
+// enters H1 with the factor -1/(4 pi).
+//   PF[n] = (ik)^n/(4 pi):
+//   MG += PF0 RM1 + PF1 R0 + PF2/2 R1 + PF3/6 R2
+//   MP += PF2/2 RM1 + PF3/3 R0 + PF4/6 R1
+// ---------------------------------------------------------------------------
+GB_HD void add_taylor_terms(const Fippi& F, cx<double> k, cx<double>* MG, cx<double>* MP) {
+  const double R0[9] = {1.0 / 4, 1.0 / 12, 1.0 / 12, 1.0 / 12, 1.0 / 36, 1.0 / 36, 1.0 / 12, 1.0 / 36, 1.0 / 36};
+  const double inv4pi = 0.079577471545947667884;
+  cx<double> ik = mk(-k.im, k.re);
+  cx<double> PF[5];
+  PF[0] = mk(inv4pi, 0.0);
+  for (int i = 1; i < 5; i++) PF[i] = PF[i - 1] * ik;
+  for (int m = 0; m < 9; m++) {
+    MG[m] = MG[m] + F.RM1[m] * PF[0] + R0[m] * PF[1] + (0.5 * F.R1[m]) * PF[2] + (F.R2[m] / 6.0) * PF[3];
+    MP[m] = MP[m] + (0.5 * F.RM1[m]) * PF[2] + (R0[m] / 3.0) * PF[3] + (F.R1[m] / 6.0) * PF[4];
+  }
+}
+
+GB_HD double htimes_rm3(const Fippi& F, const double* Va, const double* Vb, int ja, int jb) {
+  double qa[3], qb[3], d[3], x[3];
+  for (int i = 0; i < 3; i++) { qa[i] = Va[3 * ja + i] - Va[i]; qb[i] = Vb[3 * jb + i] - Va[i]; d[i] = qa[i] - qb[i]; }
+  vcross(qa, qb, x);
+  return vdot(d, F.XX) + vdot(x, F.XM);
+}
+
+}  // namespace gbem

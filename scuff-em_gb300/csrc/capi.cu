@@ -1,0 +1,427 @@
+// capi.cu -- the extern "C" boundary declared in include/gbem.h.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <vector>
+#include "bem_math.cuh"
+#include "gbem_internal.h"
+
+namespace gbem {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+
+gbem_status cuda_status(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return GBEM_OK;
+  set_error("%s: %s", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? GBEM_ENOMEM : GBEM_ECUDA;
+}
+
+gbem_status rhs_planewave_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, const double* E0,
+                                 const double* nh, void* d_rhs, cudaStream_t s);
+
+static size_t esize(int dtype) { return dtype == GBEM_C128 ? 16 : (dtype == GBEM_C64 ? 8 : 8); }
+
+static void perm_from_ipiv(const std::vector<int>& ipiv0, std::vector<int>& perm) {
+  int N = (int)ipiv0.size();
+  perm.resize(N);
+  for (int i = 0; i < N; i++) perm[i] = i;
+  for (int i = 0; i < N; i++) std::swap(perm[i], perm[ipiv0[i]]);
+}
+
+}  // namespace gbem
+
+using namespace gbem;
+
+struct gbem_geometry : public Geometry {};
+struct gbem_matrix : public Matrix {
+  int* d_perm = nullptr;
+};
+
+#define CHECK_CUDA(call, what)                     \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_status(e_, what); \
+  } while (0)
+
+extern "C" {
+
+const char* gbem_last_error(void) { return g_err; }
+const char* gbem_version(void) { return "gbem 0.1 (sm_103a)"; }
+
+gbem_status gbem_geometry_create(int num_surfaces, const gbem_surface_desc* surfaces, int num_regions, int device,
+                                 gbem_geometry** out) {
+  if (!out) { set_error("gbem_geometry_create: out is NULL"); return GBEM_EINVAL; }
+  *out = nullptr;
+  gbem_geometry* g = new (std::nothrow) gbem_geometry();
+  if (!g) { set_error("out of host memory"); return GBEM_ENOMEM; }
+  g->device = device;
+  gbem_status st = build_geometry(num_surfaces, surfaces, num_regions, g);
+  if (st != GBEM_OK) { delete g; return st; }
+  // no CUDA call here: the device stream is created on first device use, so
+  // the mesh bookkeeping also works on a host without a GPU
+  *out = g;
+  return GBEM_OK;
+}
+
+static gbem_status ensure_stream(gbem_geometry* g) {
+  cudaError_t e = cudaSetDevice(g->device);
+  if (e == cudaSuccess && !g->stream) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+  return cuda_status(e, "device setup");
+}
+
+gbem_status gbem_geometry_destroy(gbem_geometry* g) {
+  if (!g) return GBEM_OK;
+  if (g->stream) {
+    cudaSetDevice(g->device);
+    cudaStreamSynchronize(g->stream);
+  }
+  if (g->d_pv) free_geometry_device(g);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+  return GBEM_OK;
+}
+
+gbem_status gbem_geometry_num_bfs(const gbem_geometry* g, int* N) {
+  if (!g || !N) { set_error("gbem_geometry_num_bfs: NULL argument"); return GBEM_EINVAL; }
+  *N = g->N;
+  return GBEM_OK;
+}
+
+gbem_status gbem_geometry_edges(const gbem_geometry* g, int surface, int* num_edges, int* edge_table, double* lengths) {
+  if (!g || surface < 0 || surface >= (int)g->S.size() || !num_edges) {
+    set_error("gbem_geometry_edges: bad arguments");
+    return GBEM_EINVAL;
+  }
+  const Surface& s = g->S[surface];
+  *num_edges = s.ne;
+  if (edge_table) memcpy(edge_table, s.E.data(), sizeof(int) * s.E.size());
+  if (lengths) memcpy(lengths, s.elen.data(), sizeof(double) * s.elen.size());
+  return GBEM_OK;
+}
+
+gbem_status gbem_geometry_near_counts(const gbem_geometry* g, long long counts[4]) {
+  if (!g || !counts) { set_error("gbem_geometry_near_counts: NULL argument"); return GBEM_EINVAL; }
+  for (int i = 0; i < 4; i++) counts[i] = g->near_counts[i];
+  return GBEM_OK;
+}
+
+gbem_status gbem_matrix_create(const gbem_geometry* g, int dtype, gbem_matrix** out) {
+  if (!g || !out || (dtype != GBEM_C128 && dtype != GBEM_C64)) {
+    set_error("gbem_matrix_create: bad arguments (dtype must be C128 or C64)");
+    return GBEM_EINVAL;
+  }
+  *out = nullptr;
+  gbem_status st0 = ensure_stream(const_cast<gbem_geometry*>(g));
+  if (st0 != GBEM_OK) return st0;
+  gbem_matrix* m = new gbem_matrix();
+  m->g = g; m->N = g->N; m->ld = g->N; m->dtype = dtype; m->stream = g->stream;
+  cudaError_t e = cudaMalloc(&m->d, (size_t)m->N * m->ld * esize(dtype));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->d_ipiv, sizeof(int) * m->N);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->d_perm, sizeof(int) * m->N);
+  if (e != cudaSuccess) {
+    cudaFree(m->d); cudaFree(m->d_ipiv); cudaFree(m->d_perm);
+    delete m;
+    return cuda_status(e, "gbem_matrix_create");
+  }
+  *out = m;
+  return GBEM_OK;
+}
+
+gbem_status gbem_matrix_destroy(gbem_matrix* m) {
+  if (!m) return GBEM_OK;
+  cudaStreamSynchronize(m->stream);
+  cudaFree(m->d); cudaFree(m->d_ipiv); cudaFree(m->d_perm); cudaFree(m->ws);
+  delete m;
+  return GBEM_OK;
+}
+
+gbem_status gbem_matrix_device_ptr(gbem_matrix* m, void** dptr, int* ld) {
+  if (!m || !dptr) { set_error("gbem_matrix_device_ptr: NULL argument"); return GBEM_EINVAL; }
+  *dptr = m->d;
+  if (ld) *ld = m->ld;
+  return GBEM_OK;
+}
+
+gbem_status gbem_matrix_download(gbem_matrix* m, void* host, int ldh) {
+  if (!m || !host || ldh < m->N) { set_error("gbem_matrix_download: bad arguments"); return GBEM_EINVAL; }
+  size_t es = esize(m->dtype);
+  CHECK_CUDA(cudaMemcpy2DAsync(host, (size_t)ldh * es, m->d, (size_t)m->ld * es, (size_t)m->N * es, m->N,
+                               cudaMemcpyDeviceToHost, m->stream), "download");
+  CHECK_CUDA(cudaStreamSynchronize(m->stream), "download");
+  return GBEM_OK;
+}
+
+gbem_status gbem_matrix_upload(gbem_matrix* m, const void* host, int ldh) {
+  if (!m || !host || ldh < m->N) { set_error("gbem_matrix_upload: bad arguments"); return GBEM_EINVAL; }
+  size_t es = esize(m->dtype);
+  CHECK_CUDA(cudaMemcpy2DAsync(m->d, (size_t)m->ld * es, host, (size_t)ldh * es, (size_t)m->N * es, m->N,
+                               cudaMemcpyHostToDevice, m->stream), "upload");
+  CHECK_CUDA(cudaStreamSynchronize(m->stream), "upload");
+  m->factored = false;
+  return GBEM_OK;
+}
+
+gbem_status gbem_assemble(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
+                          int precision, gbem_matrix* M) {
+  if (!g || !M || !eps || !mu || M->N != g->N) { set_error("gbem_assemble: bad arguments"); return GBEM_EINVAL; }
+  if (omega_re == 0.0 && omega_im == 0.0) { set_error("gbem_assemble: Omega = 0 is not supported"); return GBEM_EINVAL; }
+  gbem_status st0 = ensure_stream(g);
+  if (st0 != GBEM_OK) return st0;
+  M->factored = false;
+  return assemble_device(g, omega_re, omega_im, eps, mu, precision, M->d, M->ld, M->dtype, g->stream);
+}
+
+gbem_status gbem_assemble_host(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
+                               double* ZM, int ld) {
+  if (!g || !ZM || ld < g->N) { set_error("gbem_assemble_host: bad arguments"); return GBEM_EINVAL; }
+  gbem_matrix* M = nullptr;
+  gbem_status st = gbem_matrix_create(g, GBEM_C128, &M);
+  if (st != GBEM_OK) return st;
+  st = gbem_assemble(g, omega_re, omega_im, eps, mu, GBEM_PREC_FP64, M);
+  if (st == GBEM_OK) st = gbem_matrix_download(M, ZM, ld);
+  gbem_matrix_destroy(M);
+  return st;
+}
+
+gbem_status gbem_lu_factor(gbem_matrix* M, int* ipiv, int* info) {
+  if (!M) { set_error("gbem_lu_factor: NULL matrix"); return GBEM_EINVAL; }
+  CHECK_CUDA(cudaSetDevice(M->g->device), "cudaSetDevice");
+  int h_info = 0;
+  gbem_status st = lu_factor_device(M->d, M->N, M->ld, M->dtype, M->d_ipiv, &h_info, M->stream, &M->ws, &M->ws_bytes);
+  if (st != GBEM_OK) return st;
+  std::vector<int> piv(M->N), perm;
+  CHECK_CUDA(cudaMemcpy(piv.data(), M->d_ipiv, sizeof(int) * M->N, cudaMemcpyDeviceToHost), "ipiv");
+  perm_from_ipiv(piv, perm);
+  CHECK_CUDA(cudaMemcpy(M->d_perm, perm.data(), sizeof(int) * M->N, cudaMemcpyHostToDevice), "perm");
+  M->ipiv.resize(M->N);
+  for (int i = 0; i < M->N; i++) M->ipiv[i] = piv[i] + 1;
+  if (ipiv) memcpy(ipiv, M->ipiv.data(), sizeof(int) * M->N);
+  if (info) *info = h_info;
+  M->factored = true;
+  if (h_info > 0) { set_error("LU: U(%d,%d) is exactly zero", h_info, h_info); return GBEM_ESINGULAR; }
+  return GBEM_OK;
+}
+
+gbem_status gbem_lu_solve(gbem_matrix* M, char trans, int nrhs, void* B, int ldb) {
+  if (!M || !B || nrhs <= 0 || ldb < M->N) { set_error("gbem_lu_solve: bad arguments"); return GBEM_EINVAL; }
+  if (!M->factored) { set_error("gbem_lu_solve: matrix is not factored"); return GBEM_EINVAL; }
+  CHECK_CUDA(cudaSetDevice(M->g->device), "cudaSetDevice");
+  size_t es = esize(M->dtype);
+  void *dB = nullptr, *dY = nullptr;
+  CHECK_CUDA(cudaMallocAsync(&dB, (size_t)M->N * nrhs * es, M->stream), "solve alloc");
+  CHECK_CUDA(cudaMallocAsync(&dY, (size_t)M->N * 8 * es, M->stream), "solve alloc");
+  CHECK_CUDA(cudaMemcpy2DAsync(dB, (size_t)M->N * es, B, (size_t)ldb * es, (size_t)M->N * es, nrhs,
+                               cudaMemcpyHostToDevice, M->stream), "solve upload");
+  gbem_status st = lu_solve_device(M->d, M->N, M->ld, M->dtype, M->d_perm, trans, nrhs, dB, M->N, dY, M->stream);
+  if (st == GBEM_OK) {
+    cudaError_t e = cudaMemcpy2DAsync(B, (size_t)ldb * es, dB, (size_t)M->N * es, (size_t)M->N * es, nrhs,
+                                      cudaMemcpyDeviceToHost, M->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(M->stream);
+    if (e != cudaSuccess) st = cuda_status(e, "solve download");
+  }
+  cudaFreeAsync(dB, M->stream);
+  cudaFreeAsync(dY, M->stream);
+  cudaStreamSynchronize(M->stream);
+  return st;
+}
+
+gbem_status gbem_lu_factor_host(double* ZM, int N, int ld, int* ipiv, int* info) {
+  if (!ZM || N <= 0 || ld < N) { set_error("gbem_lu_factor_host: bad arguments"); return GBEM_EINVAL; }
+  cudaStream_t s;
+  CHECK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+  void* dA = nullptr;
+  int* dpiv = nullptr;
+  void* ws = nullptr;
+  size_t wsb = 0;
+  gbem_status st = GBEM_OK;
+  cudaError_t e = cudaMalloc(&dA, (size_t)N * N * 16);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&dpiv, sizeof(int) * N);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dA, (size_t)N * 16, ZM, (size_t)ld * 16, (size_t)N * 16, N, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) st = cuda_status(e, "gbem_lu_factor_host");
+  int h_info = 0;
+  if (st == GBEM_OK) st = lu_factor_device(dA, N, N, GBEM_C128, dpiv, &h_info, s, &ws, &wsb);
+  if (st == GBEM_OK) {
+    std::vector<int> piv(N);
+    e = cudaMemcpy2DAsync(ZM, (size_t)ld * 16, dA, (size_t)N * 16, (size_t)N * 16, N, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(piv.data(), dpiv, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "gbem_lu_factor_host");
+    else if (ipiv)
+      for (int i = 0; i < N; i++) ipiv[i] = piv[i] + 1;
+    if (info) *info = h_info;
+  }
+  cudaFree(dA); cudaFree(dpiv); cudaFree(ws);
+  cudaStreamDestroy(s);
+  if (st == GBEM_OK && h_info > 0) { set_error("LU: U(%d,%d) is exactly zero", h_info, h_info); return GBEM_ESINGULAR; }
+  return st;
+}
+
+gbem_status gbem_lu_solve_host(const double* ZM, int N, int ld, const int* ipiv, char trans, int nrhs, double* B,
+                               int ldb) {
+  if (!ZM || !ipiv || !B || N <= 0 || ld < N || ldb < N || nrhs <= 0) {
+    set_error("gbem_lu_solve_host: bad arguments");
+    return GBEM_EINVAL;
+  }
+  std::vector<int> piv(N), perm;
+  for (int i = 0; i < N; i++) {
+    piv[i] = ipiv[i] - 1;
+    if (piv[i] < i || piv[i] >= N) { set_error("gbem_lu_solve_host: invalid pivot %d at %d", ipiv[i], i + 1); return GBEM_EINVAL; }
+  }
+  perm_from_ipiv(piv, perm);
+  cudaStream_t s;
+  CHECK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+  void *dA = nullptr, *dB = nullptr, *dY = nullptr;
+  int* dperm = nullptr;
+  gbem_status st = GBEM_OK;
+  cudaError_t e = cudaMalloc(&dA, (size_t)N * N * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&dB, (size_t)N * nrhs * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&dY, (size_t)N * 8 * 16);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&dperm, sizeof(int) * N);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dA, (size_t)N * 16, ZM, (size_t)ld * 16, (size_t)N * 16, N, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dB, (size_t)N * 16, B, (size_t)ldb * 16, (size_t)N * 16, nrhs, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dperm, perm.data(), sizeof(int) * N, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) st = cuda_status(e, "gbem_lu_solve_host");
+  if (st == GBEM_OK) st = lu_solve_device(dA, N, N, GBEM_C128, dperm, trans, nrhs, dB, N, dY, s);
+  if (st == GBEM_OK) {
+    e = cudaMemcpy2DAsync(B, (size_t)ldb * 16, dB, (size_t)N * 16, (size_t)N * 16, nrhs, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "gbem_lu_solve_host");
+  }
+  cudaFree(dA); cudaFree(dB); cudaFree(dY); cudaFree(dperm);
+  cudaStreamDestroy(s);
+  return st;
+}
+
+// c64 <-> c128 conversions for the refinement loop
+__global__ void to_c64(const double2* a, float2* b, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+__global__ void add_c64(double2* x, const float2* d, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) { x[i].x += (double)d[i].x; x[i].y += (double)d[i].y; }
+}
+__global__ void colnorm2(const double2* a, int N, int nrhs, double* out) {
+  int r = blockIdx.x;
+  double s = 0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) { double2 z = a[(size_t)r * N + i]; s += z.x * z.x + z.y * z.y; }
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[r] = red[0];
+}
+
+gbem_status gbem_solve_mixed(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
+                             int nrhs, const double* B, int ldb, double* X, int ldx, double tol, int max_iter, int* iters,
+                             double* resid) {
+  if (!g || !B || !X || nrhs <= 0 || nrhs > 64 || ldb < g->N || ldx < g->N) {
+    set_error("gbem_solve_mixed: bad arguments");
+    return GBEM_EINVAL;
+  }
+  gbem_status st0 = ensure_stream(g);
+  if (st0 != GBEM_OK) return st0;
+  const int N = g->N;
+  cudaStream_t s = g->stream;
+  gbem_matrix *M = nullptr, *F = nullptr;
+  gbem_status st = gbem_matrix_create(g, GBEM_C64, &M);
+  if (st == GBEM_OK) st = gbem_matrix_create(g, GBEM_C64, &F);
+  void *dB = nullptr, *dX = nullptr, *dR = nullptr, *dD = nullptr, *dY = nullptr, *part = nullptr;
+  double* dn = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (st == GBEM_OK) {
+    e = cudaMalloc(&dB, (size_t)N * nrhs * 16);
+    if (e == cudaSuccess) e = cudaMalloc(&dX, (size_t)N * nrhs * 16);
+    if (e == cudaSuccess) e = cudaMalloc(&dR, (size_t)N * nrhs * 16);
+    if (e == cudaSuccess) e = cudaMalloc(&dD, (size_t)N * nrhs * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&dY, (size_t)N * 8 * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&part, (size_t)8 * 8 * N * 16);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dn, sizeof(double) * 2 * nrhs);
+    if (e != cudaSuccess) st = cuda_status(e, "gbem_solve_mixed alloc");
+  }
+  if (st == GBEM_OK) st = gbem_assemble(g, omega_re, omega_im, eps, mu, GBEM_PREC_MIXED, M);
+  if (st == GBEM_OK) {
+    e = cudaMemcpyAsync(F->d, M->d, (size_t)N * N * 8, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(dB, (size_t)N * 16, B, (size_t)ldb * 16, (size_t)N * 16, nrhs, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dX, 0, (size_t)N * nrhs * 16, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dR, dB, (size_t)N * nrhs * 16, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) st = cuda_status(e, "gbem_solve_mixed setup");
+  }
+  int info = 0;
+  if (st == GBEM_OK) st = gbem_lu_factor(F, nullptr, &info);
+  std::vector<double> bn(nrhs), rn(nrhs);
+  if (st == GBEM_OK) {
+    colnorm2<<<nrhs, 256, 0, s>>>((const double2*)dB, N, nrhs, dn);
+    e = cudaMemcpyAsync(bn.data(), dn, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "norm");
+  }
+  int it = 0;
+  double rel = 1.0;
+  size_t nel = (size_t)N * nrhs;
+  while (st == GBEM_OK && it < max_iter) {
+    to_c64<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>((const double2*)dR, (float2*)dD, nel);
+    st = lu_solve_device(F->d, N, N, GBEM_C64, F->d_perm, 'N', nrhs, dD, N, dY, s);
+    if (st != GBEM_OK) break;
+    add_c64<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>((double2*)dX, (const float2*)dD, nel);
+    st = residual_device(M->d, N, GBEM_C64, N, (const double*)dX, N, (const double*)dB, N, nrhs, (double*)dR, N, part, s);
+    if (st != GBEM_OK) break;
+    colnorm2<<<nrhs, 256, 0, s>>>((const double2*)dR, N, nrhs, dn);
+    e = cudaMemcpyAsync(rn.data(), dn, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { st = cuda_status(e, "refinement"); break; }
+    it++;
+    rel = 0;
+    for (int r = 0; r < nrhs; r++) rel = std::fmax(rel, std::sqrt(rn[r] / (bn[r] > 0 ? bn[r] : 1.0)));
+    if (rel <= tol) break;
+  }
+  if (st == GBEM_OK) {
+    e = cudaMemcpy2DAsync(X, (size_t)ldx * 16, dX, (size_t)N * 16, (size_t)N * 16, nrhs, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "gbem_solve_mixed download");
+  }
+  if (iters) *iters = it;
+  if (resid) *resid = rel;
+  cudaFree(dB); cudaFree(dX); cudaFree(dR); cudaFree(dD); cudaFree(dY); cudaFree(part); cudaFree(dn);
+  gbem_matrix_destroy(M);
+  gbem_matrix_destroy(F);
+  if (st == GBEM_OK && rel > tol) {
+    set_error("refinement stopped at relative residual %.3e after %d sweeps (tol %.1e)", rel, it, tol);
+    return GBEM_ENOCONV;
+  }
+  return st;
+}
+
+gbem_status gbem_rhs_planewave(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
+                               const double* E0, const double* nhat, double* rhs) {
+  if (!g || !eps || !mu || !E0 || !nhat || !rhs) { set_error("gbem_rhs_planewave: NULL argument"); return GBEM_EINVAL; }
+  gbem_status st0 = ensure_stream(g);
+  if (st0 != GBEM_OK) return st0;
+  void* d = nullptr;
+  CHECK_CUDA(cudaMalloc(&d, sizeof(double) * 2 * g->N), "rhs alloc");
+  gbem_status st = rhs_planewave_device(g, omega_re, omega_im, eps, mu, E0, nhat, d, g->stream);
+  if (st == GBEM_OK) {
+    cudaError_t e = cudaMemcpyAsync(rhs, d, sizeof(double) * 2 * g->N, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) st = cuda_status(e, "rhs download");
+  }
+  cudaFree(d);
+  return st;
+}
+
+}  // extern "C"

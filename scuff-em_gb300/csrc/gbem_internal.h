@@ -1,0 +1,112 @@
+// gbem_internal.h -- host-side data structures shared by the library's
+// translation units (never exposed through the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+#include <cstdint>
+#include "../../include/gbem.h"
+
+namespace gbem {
+
+// tile geometry of the far-field assembly: TE edges per side, at most
+// PMAX distinct panels per edge block
+constexpr int TE = 32;
+constexpr int PMAX = 48;
+
+struct Surface {
+  int nv = 0, np = 0, ne = 0;
+  std::vector<double> V;        // 3 nv
+  std::vector<int> PV;          // 3 np
+  std::vector<double> cen, rad; // 3 np, np
+  std::vector<int> E;           // 8 ne: iV1 iV2 iQP iQM iPPanel iMPanel PIndex MIndex
+  std::vector<double> elen;     // ne
+  int reg_ext = 0, reg_int = -1;
+  bool pec = false;
+  int bf_offset = 0;            // first basis-function index in the matrix
+  int panel_offset = 0;         // first global panel index
+  std::vector<int> he_edge;     // 3 np: edge of (panel, local vertex j) or -1
+  std::vector<int> he_side;     // 3 np: 0 = positive panel, 1 = negative panel
+};
+
+// a row (or column) block of consecutive edges of one surface
+struct EdgeBlock {
+  int e0 = 0, ne = 0;                 // edges [e0, e0+ne)
+  std::vector<int> panels;            // global panel indices (<= PMAX)
+  std::vector<int8_t> he_local;       // 3 per panel: local edge index in block or -1
+  std::vector<int8_t> he_side;        // 3 per panel
+};
+
+struct NearPair {
+  int pa, pb;      // global panel indices (pa <= pb inside a self block)
+  int ncv;         // common vertices 0..3
+  int8_t perm_a[3], perm_b[3];  // common-vertices-first order -> mesh order
+  double rmax;     // larger panel radius
+};
+
+struct Block {
+  int sa = 0, sb = 0;
+  bool sym = false;
+  int nreg = 0;
+  int reg[2] = {0, 0};
+  double sign[2] = {0, 0};
+  int bpe_a = 1, bpe_b = 1;            // basis functions per edge (1 PEC, 2 dielectric)
+  std::vector<EdgeBlock> rows, cols;
+  std::vector<int2> tiles;             // (row block, col block)
+  std::vector<NearPair> near;          // near pairs of this surface pair
+  std::vector<int> near_ptr, near_col, near_idx;  // CSR over local row panel: (pb, pair index, transpose flag in sign)
+};
+
+struct DevBlock;  // defined in assemble.cu
+
+struct Geometry {
+  int device = 0;
+  int nregions = 1;
+  int N = 0;
+  int np_total = 0;
+  std::vector<Surface> S;
+  std::vector<Block> blocks;
+  long long near_counts[4] = {0, 0, 0, 0};
+  // device data (owned)
+  cudaStream_t stream = nullptr;
+  double* d_pv = nullptr;    // 9 per global panel
+  double* d_pc = nullptr;    // 4 per global panel: centroid, radius
+  std::vector<DevBlock*> dblocks;
+  bool fippi_ready = false;
+  std::string err;
+};
+
+struct Matrix {
+  const Geometry* g = nullptr;
+  int N = 0, ld = 0, dtype = 0;
+  void* d = nullptr;            // device storage
+  int* d_ipiv = nullptr;        // device pivots (0-based) after factorisation
+  std::vector<int> ipiv;        // host copy (1-based)
+  bool factored = false;
+  cudaStream_t stream = nullptr;
+  void* ws = nullptr;           // LU workspace
+  size_t ws_bytes = 0;
+};
+
+// geometry.cpp
+gbem_status build_geometry(int ns, const gbem_surface_desc* d, int nreg, Geometry* g);
+
+// assemble.cu
+gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps, const double* mu,
+                            int precision, void* dM, int ld, int dtype, cudaStream_t s);
+gbem_status upload_geometry(Geometry* g);
+void free_geometry_device(Geometry* g);
+
+// lu.cu
+gbem_status lu_factor_device(void* dA, int N, int ld, int dtype, int* d_ipiv, int* h_info, cudaStream_t s,
+                             void** ws, size_t* ws_bytes);
+gbem_status lu_solve_device(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs,
+                            void* dB, int ldb, void* dY, cudaStream_t s);
+gbem_status residual_device(const void* dA, int lda, int dtype, int N, const double* dX, int ldx, const double* dB,
+                            int ldb, int nrhs, double* dR, int ldr, void* part, cudaStream_t s);
+
+// error helpers
+void set_error(const char* fmt, ...);
+gbem_status cuda_status(cudaError_t e, const char* what);
+
+}  // namespace gbem

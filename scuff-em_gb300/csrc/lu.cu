@@ -1,0 +1,544 @@
+// lu.cu -- dense complex LU factorisation with partial pivoting, triangular
+// solves, and the FP64 residual of iterative refinement (replaces
+// HMatrix::LUFactorize / LUSolve, libs/libhmat/LBWrappers.cc:151-236, which
+// call LAPACK zgetrf_/zgetrs_).
+//
+// Right-looking blocked LU, column-major, panel width w:
+//   panel_kernel  one cooperative launch per panel: the panel's rows are
+//                 spread over the CTAs' shared memory; each column needs one
+//                 grid-wide barrier (pivot candidates and the candidate rows
+//                 are exchanged through double-buffered global stashes, so
+//                 row swaps need no second barrier).  Pivots maximise
+//                 |Re|+|Im| in FP64 (LAPACK's IZAMAX); ties go to the lowest row.
+//   laswp_kernel  applies the panel's row interchanges outside the panel.
+//   trsm_kernel   U12 = L11^{-1} A12 (unit lower triangle).
+//   trailing update A22 -= L21 U12: gemm_simt<T> for FP64, the tensor-core
+//                 split-BF16 GEMM (gemm_tc.cu) for the complex-FP32 form.
+#include <cooperative_groups.h>
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+#include "bem_math.cuh"
+#include "gbem_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace gbem {
+
+// tensor-core trailing update (gemm_tc.cu); returns false if unavailable
+bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long lda, const cx<float>* B,
+                    long long ldb, int m, int n, int k, void* ws, size_t ws_bytes, cudaStream_t s, cudaError_t* err);
+size_t tc_gemm_ws_bytes(int m, int n, int k);
+
+template <typename T> struct Stash {
+  cx<T>* cand_rows;  // [2][G][w]
+  cx<T>* diag_row;   // [2][w]
+  double* cand_val;  // [2][G]
+  int* cand_idx;     // [2][G]
+};
+
+template <typename T> struct PanelArgs {
+  cx<T>* A;
+  long long ld;
+  int N, c0, w, R;
+  int* ipiv;   // 0-based global pivot rows for columns c0..c0+w-1
+  int* info;   // first zero pivot (1-based), 0 if none
+  Stash<T> st;
+};
+
+__device__ __forceinline__ void better(double v, int i, double& bv, int& bi) {
+  if (i < 0) return;
+  if (bi < 0 || v > bv || (v == bv && i < bi)) { bv = v; bi = i; }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int w = a.w, wp = a.w + 1;
+  cx<T>* rows = reinterpret_cast<cx<T>*>(smem_raw);  // [R][w+1]
+  cx<T>* u = rows + (size_t)a.R * wp;                 // pivot row [w]
+  __shared__ double red_v[32];
+  __shared__ int red_i[32];
+  __shared__ int s_best, s_win, s_p;
+  const int G = gridDim.x, c = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int m0 = a.c0 + c * a.R;
+  const int nr = max(0, min(a.R, a.N - m0));
+  for (int q = tid; q < nr * w; q += nt) {
+    int r = q % nr, k = q / nr;
+    rows[r * wp + k] = a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld];
+  }
+  __syncthreads();
+  for (int jj = 0; jj < w; jj++) {
+    const int d = a.c0 + jj, buf = jj & 1;
+    // local pivot candidate
+    double bv = -1.0;
+    int bi = -1;
+    for (int r = tid; r < nr; r += nt) {
+      int gi = m0 + r;
+      if (gi < d) continue;
+      cx<T> z = rows[r * wp + jj];
+      // LAPACK's IZAMAX measure |Re| + |Im| (dcabs1), evaluated in FP64
+      double v = fabs((double)z.re) + fabs((double)z.im);
+      better(v, gi, bv, bi);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ov = __shfl_down_sync(0xffffffff, bv, o);
+      int oi = __shfl_down_sync(0xffffffff, bi, o);
+      better(ov, oi, bv, bi);
+    }
+    if ((tid & 31) == 0) { red_v[tid >> 5] = bv; red_i[tid >> 5] = bi; }
+    __syncthreads();
+    if (tid < 32) {
+      bv = tid < (nt >> 5) ? red_v[tid] : -1.0;
+      bi = tid < (nt >> 5) ? red_i[tid] : -1;
+      for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_down_sync(0xffffffff, bv, o);
+        int oi = __shfl_down_sync(0xffffffff, bi, o);
+        better(ov, oi, bv, bi);
+      }
+      if (tid == 0) {
+        s_best = bi;
+        a.st.cand_val[buf * G + c] = bv;
+        a.st.cand_idx[buf * G + c] = bi;
+      }
+    }
+    __syncthreads();
+    const int cb = s_best;
+    if (cb >= 0)
+      for (int k = tid; k < w; k += nt) a.st.cand_rows[((size_t)buf * G + c) * w + k] = rows[(cb - m0) * wp + k];
+    if (d >= m0 && d < m0 + nr)
+      for (int k = tid; k < w; k += nt) a.st.diag_row[(size_t)buf * w + k] = rows[(d - m0) * wp + k];
+    __threadfence();
+    grid.sync();
+    // global pivot: best over all CTAs' candidates
+    bv = -1.0; bi = -1;
+    int bc = -1;
+    for (int q = tid; q < G; q += nt) {
+      int i = a.st.cand_idx[buf * G + q];
+      double v = a.st.cand_val[buf * G + q];
+      if (i >= 0 && (bi < 0 || v > bv || (v == bv && i < bi))) { bv = v; bi = i; bc = q; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ov = __shfl_down_sync(0xffffffff, bv, o);
+      int oi = __shfl_down_sync(0xffffffff, bi, o);
+      int oc = __shfl_down_sync(0xffffffff, bc, o);
+      if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; bc = oc; }
+    }
+    if ((tid & 31) == 0) { red_v[tid >> 5] = bv; red_i[tid >> 5] = bc; }
+    __syncthreads();
+    if (tid == 0) {
+      double b2 = -1.0;
+      int wc = -1;
+      for (int q = 0; q < (nt >> 5); q++) {
+        int cc = red_i[q];
+        if (cc < 0) continue;
+        int i = a.st.cand_idx[buf * G + cc];
+        double v = red_v[q];
+        if (wc < 0 || v > b2 || (v == b2 && i < a.st.cand_idx[buf * G + wc])) { b2 = v; wc = cc; }
+      }
+      s_win = wc;
+      s_p = a.st.cand_idx[buf * G + wc];
+      if (c == 0) {
+        a.ipiv[d] = s_p;
+        if (b2 == 0.0 && *a.info == 0) *a.info = d + 1;
+      }
+    }
+    __syncthreads();
+    const int p = s_p, wc = s_win;
+    for (int k = tid; k < w; k += nt) u[k] = a.st.cand_rows[((size_t)buf * G + wc) * w + k];
+    __syncthreads();
+    // row interchange d <-> p inside the panel
+    if (d >= m0 && d < m0 + nr)
+      for (int k = tid; k < w; k += nt) rows[(d - m0) * wp + k] = u[k];
+    if (p != d && p >= m0 && p < m0 + nr)
+      for (int k = tid; k < w; k += nt) rows[(p - m0) * wp + k] = a.st.diag_row[(size_t)buf * w + k];
+    __syncthreads();
+    // multipliers and rank-1 update of the rows below d
+    cx<T> piv = u[jj];
+    T pn = piv.re * piv.re + piv.im * piv.im;
+    if (pn != (T)0) {
+      cx<T> inv = mk(piv.re / pn, -piv.im / pn);
+      int rs = max(0, d + 1 - m0);
+      for (int r = rs + tid; r < nr; r += nt) rows[r * wp + jj] = rows[r * wp + jj] * inv;
+      __syncthreads();
+      int nk = w - jj - 1, nrr = nr - rs;
+      for (int q = tid; q < nrr * nk; q += nt) {
+        int r = rs + q % nrr, k = jj + 1 + q / nrr;
+        rows[r * wp + k] = rows[r * wp + k] - rows[r * wp + jj] * u[k];
+      }
+    }
+    __syncthreads();
+  }
+  for (int q = tid; q < nr * w; q += nt) {
+    int r = q % nr, k = q / nr;
+    a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld] = rows[r * wp + k];
+  }
+}
+
+// row interchanges of columns [cb, ce) for pivots of rows [r0, r1)
+template <typename T>
+__global__ void laswp_kernel(cx<T>* A, long long ld, const int* ipiv, int r0, int r1, int cb, int ce, int skip0, int skip1) {
+  int j = cb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ce || (j >= skip0 && j < skip1)) return;
+  cx<T>* col = A + (long long)j * ld;
+  for (int i = r0; i < r1; i++) {
+    int p = ipiv[i];
+    if (p != i) { cx<T> t = col[i]; col[i] = col[p]; col[p] = t; }
+  }
+}
+
+// U12 = L11^{-1} A12: rows [c0, c0+w), columns [cb, N); 16 columns per CTA
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int N) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][16]
+  const int j0 = cb + blockIdx.x * 16;
+  const int nc = min(16, N - j0);
+  for (int q = threadIdx.x; q < w * nc; q += blockDim.x) {
+    int i = q % w, j = q / w;
+    B[i * 16 + j] = A[(c0 + i) + (long long)(j0 + j) * ld];
+  }
+  __syncthreads();
+  for (int k = 0; k < w - 1; k++) {
+    int rem = w - k - 1;
+    for (int q = threadIdx.x; q < rem * nc; q += blockDim.x) {
+      int i = k + 1 + q % rem, j = q / rem;
+      cx<T> l = A[(c0 + i) + (long long)(c0 + k) * ld];
+      B[i * 16 + j] = B[i * 16 + j] - l * B[k * 16 + j];
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < w * nc; q += blockDim.x) {
+    int i = q % w, j = q / w;
+    A[(c0 + i) + (long long)(j0 + j) * ld] = B[i * 16 + j];
+  }
+}
+
+// C -= A B (complex, column-major), 64x64 tiles, 4x4 outputs per thread
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_simt(cx<T>* C, long long ldc, const cx<T>* A, long long lda,
+                                                 const cx<T>* B, long long ldb, int m, int n, int K) {
+  __shared__ cx<T> As[16][64 + 1];
+  __shared__ cx<T> Bs[16][64 + 1];
+  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  cx<T> acc[4][4];
+  for (int a = 0; a < 4; a++)
+    for (int b = 0; b < 4; b++) acc[a][b] = mk((T)0, (T)0);
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int q = threadIdx.x; q < 16 * 64; q += 256) {
+      int ii = q % 64, kk = q / 64;
+      int gi = i0 + ii, gk = k0 + kk;
+      As[kk][ii] = (gi < m && gk < K) ? A[gi + (long long)gk * lda] : mk((T)0, (T)0);
+      int jj = q / 16, kb = q % 16;
+      int gj = j0 + jj, gkb = k0 + kb;
+      Bs[kb][jj] = (gj < n && gkb < K) ? B[gkb + (long long)gj * ldb] : mk((T)0, (T)0);
+    }
+    __syncthreads();
+    for (int kk = 0; kk < 16; kk++) {
+      cx<T> av[4], bv[4];
+      for (int a = 0; a < 4; a++) av[a] = As[kk][tx + 16 * a];
+      for (int b = 0; b < 4; b++) bv[b] = Bs[kk][ty + 16 * b];
+      for (int a = 0; a < 4; a++)
+        for (int b = 0; b < 4; b++) acc[a][b] = acc[a][b] + av[a] * bv[b];
+    }
+    __syncthreads();
+  }
+  for (int a = 0; a < 4; a++)
+    for (int b = 0; b < 4; b++) {
+      int gi = i0 + tx + 16 * a, gj = j0 + ty + 16 * b;
+      if (gi < m && gj < n) {
+        cx<T>* p = C + gi + (long long)gj * ldc;
+        *p = *p - acc[a][b];
+      }
+    }
+}
+
+template <typename T>
+static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info, cudaStream_t s, void** ws,
+                               size_t* ws_bytes) {
+  int dev = 0, nsm = 0, smem_optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t esz = sizeof(cx<T>);
+  const size_t smem_cap = (size_t)smem_optin - 2048;
+  // panel width: largest w whose panel rows fit the CTAs' shared memory
+  int w = 256;
+  int R = 0;
+  for (;; w /= 2) {
+    R = (N + nsm - 1) / nsm;
+    if ((size_t)(R * (w + 1) + w) * esz <= smem_cap || w <= 8) break;
+  }
+  if (w > N) w = std::max(1, N);
+  R = std::max(R, 1);
+  size_t smem = (size_t)(R * (w + 1) + w) * esz;
+  cudaError_t e = cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_status(e, "panel smem");
+  int maxb = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, panel_kernel<T>, 512, smem);
+  if (e != cudaSuccess || maxb < 1) return cuda_status(e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "panel occupancy");
+  // workspace: stash + info + tensor-core scratch
+  const int Gmax = nsm * maxb;
+  size_t need = (size_t)2 * Gmax * w * esz + 2 * (size_t)w * esz + 2 * Gmax * (sizeof(double) + sizeof(int)) + 256;
+  size_t tcb = 0;
+  if (sizeof(T) == 4) tcb = tc_gemm_ws_bytes(N, N, w);
+  size_t total = need + tcb + 1024;
+  if (*ws_bytes < total) {
+    if (*ws) cudaFree(*ws);
+    *ws = nullptr;
+    *ws_bytes = 0;
+    e = cudaMalloc(ws, total);
+    if (e != cudaSuccess) return cuda_status(e, "LU workspace");
+    *ws_bytes = total;
+  }
+  unsigned char* wp = (unsigned char*)*ws;
+  Stash<T> st;
+  st.cand_rows = (cx<T>*)wp; wp += (size_t)2 * Gmax * w * esz;
+  st.diag_row = (cx<T>*)wp; wp += (size_t)2 * w * esz;
+  st.cand_val = (double*)wp; wp += 2 * Gmax * sizeof(double);
+  st.cand_idx = (int*)wp; wp += 2 * Gmax * sizeof(int);
+  int* d_info = (int*)(((uintptr_t)wp + 15) & ~(uintptr_t)15); wp = (unsigned char*)(d_info + 4);
+  void* tcws = (void*)(((uintptr_t)wp + 1023) & ~(uintptr_t)1023);
+  e = cudaMemsetAsync(d_info, 0, sizeof(int), s);
+  if (e != cudaSuccess) return cuda_status(e, "info");
+  for (int c0 = 0; c0 < N; c0 += w) {
+    const int wc = std::min(w, N - c0);
+    const int m = N - c0;
+    int G = std::min(Gmax, (m + R - 1) / R);
+    PanelArgs<T> pa;
+    pa.A = A; pa.ld = ld; pa.N = N; pa.c0 = c0; pa.w = wc; pa.R = (m + G - 1) / G;
+    pa.ipiv = d_ipiv; pa.info = d_info; pa.st = st;
+    size_t sm = (size_t)(pa.R * (wc + 1) + wc) * esz;
+    void* args[] = {&pa};
+    e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(512), args, sm, s);
+    if (e != cudaSuccess) return cuda_status(e, "panel_kernel");
+    // interchanges to the left and right of the panel
+    laswp_kernel<T><<<(N + 255) / 256, 256, 0, s>>>(A, ld, d_ipiv, c0, c0 + wc, 0, N, c0, c0 + wc);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "laswp");
+    const int cb = c0 + wc;
+    if (cb >= N) break;
+    const int nrest = N - cb;
+    size_t tsm = (size_t)wc * 16 * esz;
+    if (tsm > 48 * 1024) {
+      e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
+      if (e != cudaSuccess) return cuda_status(e, "trsm smem");
+    }
+    trsm_kernel<T><<<(nrest + 15) / 16, 256, tsm, s>>>(A, ld, c0, wc, cb, N);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
+    cx<T>* C = A + cb + (long long)cb * ld;
+    const cx<T>* L21 = A + cb + (long long)c0 * ld;
+    const cx<T>* U12 = A + c0 + (long long)cb * ld;
+    bool done = false;
+    if (sizeof(T) == 4) {
+      done = tc_gemm_update((cx<float>*)C, ld, (const cx<float>*)L21, ld, (const cx<float>*)U12, ld, nrest, nrest, wc,
+                            tcws, tcb, s, &e);
+      if (e != cudaSuccess) return cuda_status(e, "tensor-core update");
+    }
+    if (!done) {
+      dim3 grid((nrest + 63) / 64, (nrest + 63) / 64);
+      gemm_simt<T><<<grid, 256, 0, s>>>(C, ld, L21, ld, U12, ld, nrest, nrest, wc);
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "gemm");
+    }
+  }
+  e = cudaMemcpyAsync(h_info, d_info, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e, "LU");
+  return GBEM_OK;
+}
+
+gbem_status lu_factor_device(void* dA, int N, int ld, int dtype, int* d_ipiv, int* h_info, cudaStream_t s, void** ws,
+                             size_t* ws_bytes) {
+  if (N <= 0 || ld < N) { set_error("lu_factor: bad size"); return GBEM_EINVAL; }
+  if (dtype == GBEM_C128) return factor_impl<double>((cx<double>*)dA, N, ld, d_ipiv, h_info, s, ws, ws_bytes);
+  if (dtype == GBEM_C64) return factor_impl<float>((cx<float>*)dA, N, ld, d_ipiv, h_info, s, ws, ws_bytes);
+  set_error("lu_factor: dtype must be C128 or C64");
+  return GBEM_EINVAL;
+}
+
+// ---------------------------------------------------------------------------
+// triangular solves (forward with unit L, backward with U), blocked by 64
+// ---------------------------------------------------------------------------
+// B[perm[i]] -> Y[i]  (perm: final row order implied by ipiv)
+template <typename T>
+__global__ void gather_rows(const cx<T>* B, long long ldb, cx<T>* Y, long long ldy, const int* perm, int N, int nrhs) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  for (int r = 0; r < nrhs; r++) Y[i + r * ldy] = B[perm[i] + r * ldb];
+}
+template <typename T>
+__global__ void scatter_rows(const cx<T>* Y, long long ldy, cx<T>* B, long long ldb, const int* perm, int N, int nrhs) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  for (int r = 0; r < nrhs; r++) B[perm[i] + r * ldb] = Y[i + r * ldy];
+}
+
+// solve the diagonal block [i0, i0+bs) in place; lower: unit L, forward;
+// upper: U, backward; transposed variants use op(A) = A^T.
+template <typename T, bool LOWER, bool TRANS>
+__global__ void __launch_bounds__(256) diag_solve(const cx<T>* A, long long lda, cx<T>* X, long long ldx, int i0,
+                                                   int bs, int nrhs) {
+  __shared__ cx<T> x[64][8];
+  int r = blockIdx.x;  // one CTA per right-hand side... up to 8 per CTA
+  (void)r;
+  for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) x[q % bs][q / bs] = X[i0 + q % bs + (long long)(q / bs) * ldx];
+  __syncthreads();
+  for (int s = 0; s < bs; s++) {
+    int k = (LOWER != TRANS) ? s : bs - 1 - s;  // forward for L or U^T, backward for U or L^T
+    // finalize x[k]
+    if (!LOWER) {
+      if (threadIdx.x < nrhs) {
+        cx<T> d = A[(i0 + k) + (long long)(i0 + k) * lda];
+        x[k][threadIdx.x] = cdiv(x[k][threadIdx.x], d);
+      }
+      __syncthreads();
+    } else if (TRANS) {
+      // L^T is unit upper: nothing to divide
+    }
+    // eliminate x[k] from the remaining rows
+    int rem = (LOWER != TRANS) ? bs - k - 1 : k;
+    for (int q = threadIdx.x; q < rem * nrhs; q += blockDim.x) {
+      int ii = (LOWER != TRANS) ? k + 1 + q % rem : q % rem;
+      int rr = q / rem;
+      cx<T> a = TRANS ? A[(i0 + k) + (long long)(i0 + ii) * lda] : A[(i0 + ii) + (long long)(i0 + k) * lda];
+      x[ii][rr] = x[ii][rr] - a * x[k][rr];
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) X[i0 + q % bs + (long long)(q / bs) * ldx] = x[q % bs][q / bs];
+}
+
+// X[rows outside block] -= op(A)[rows, block] * X[block]
+template <typename T, bool TRANS>
+__global__ void __launch_bounds__(256) off_update(const cx<T>* A, long long lda, cx<T>* X, long long ldx, int i0, int bs,
+                                                   int r0, int r1, int nrhs) {
+  __shared__ cx<T> xb[64][8];
+  for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) xb[q % bs][q / bs] = X[i0 + q % bs + (long long)(q / bs) * ldx];
+  __syncthreads();
+  int i = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= r1) return;
+  cx<T> acc[8];
+  for (int r = 0; r < nrhs; r++) acc[r] = mk((T)0, (T)0);
+  for (int k = 0; k < bs; k++) {
+    cx<T> a = TRANS ? A[(i0 + k) + (long long)i * lda] : A[i + (long long)(i0 + k) * lda];
+    for (int r = 0; r < nrhs; r++) acc[r] = acc[r] + a * xb[k][r];
+  }
+  for (int r = 0; r < nrhs; r++) X[i + (long long)r * ldx] = X[i + (long long)r * ldx] - acc[r];
+}
+
+template <typename T>
+static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, char trans, int nrhs, cx<T>* B, int ldb,
+                              cx<T>* Y, cudaStream_t s) {
+  const int bs = 64;
+  cudaError_t e;
+  for (int r0 = 0; r0 < nrhs; r0 += 8) {
+    int nr = std::min(8, nrhs - r0);
+    cx<T>* Bc = B + (long long)r0 * ldb;
+    if (trans == 'N') {
+      gather_rows<T><<<(N + 255) / 256, 256, 0, s>>>(Bc, ldb, Y, N, d_perm, N, nr);
+      for (int i0 = 0; i0 < N; i0 += bs) {
+        int b = std::min(bs, N - i0);
+        diag_solve<T, true, false><<<1, 256, 0, s>>>(A, ld, Y, N, i0, b, nr);
+        if (i0 + b < N) off_update<T, false><<<(N - i0 - b + 255) / 256, 256, 0, s>>>(A, ld, Y, N, i0, b, i0 + b, N, nr);
+      }
+      for (int i0 = ((N - 1) / bs) * bs; i0 >= 0; i0 -= bs) {
+        int b = std::min(bs, N - i0);
+        diag_solve<T, false, false><<<1, 256, 0, s>>>(A, ld, Y, N, i0, b, nr);
+        if (i0 > 0) off_update<T, false><<<(i0 + 255) / 256, 256, 0, s>>>(A, ld, Y, N, i0, b, 0, i0, nr);
+      }
+      e = cudaMemcpy2DAsync(Bc, (size_t)ldb * sizeof(cx<T>), Y, (size_t)N * sizeof(cx<T>), (size_t)N * sizeof(cx<T>), nr,
+                            cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return cuda_status(e, "solve copy");
+    } else {
+      // A^T x = b with A = P^T L U: U^T z = b, L^T y = z, x = P^T y
+      e = cudaMemcpy2DAsync(Y, (size_t)N * sizeof(cx<T>), Bc, (size_t)ldb * sizeof(cx<T>), (size_t)N * sizeof(cx<T>), nr,
+                            cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return cuda_status(e, "solve copy");
+      for (int i0 = 0; i0 < N; i0 += bs) {
+        int b = std::min(bs, N - i0);
+        diag_solve<T, false, true><<<1, 256, 0, s>>>(A, ld, Y, N, i0, b, nr);
+        if (i0 + b < N) off_update<T, true><<<(N - i0 - b + 255) / 256, 256, 0, s>>>(A, ld, Y, N, i0, b, i0 + b, N, nr);
+      }
+      for (int i0 = ((N - 1) / bs) * bs; i0 >= 0; i0 -= bs) {
+        int b = std::min(bs, N - i0);
+        diag_solve<T, true, true><<<1, 256, 0, s>>>(A, ld, Y, N, i0, b, nr);
+        if (i0 > 0) off_update<T, true><<<(i0 + 255) / 256, 256, 0, s>>>(A, ld, Y, N, i0, b, 0, i0, nr);
+      }
+      scatter_rows<T><<<(N + 255) / 256, 256, 0, s>>>(Y, N, Bc, ldb, d_perm, N, nr);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "solve");
+  }
+  return GBEM_OK;
+}
+
+gbem_status lu_solve_device(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs, void* dB,
+                            int ldb, void* dY, cudaStream_t s) {
+  if (trans != 'N' && trans != 'T') { set_error("lu_solve: trans must be 'N' or 'T'"); return GBEM_EINVAL; }
+  if (dtype == GBEM_C128)
+    return solve_impl<double>((const cx<double>*)dA, N, ld, d_perm, trans, nrhs, (cx<double>*)dB, ldb, (cx<double>*)dY, s);
+  if (dtype == GBEM_C64)
+    return solve_impl<float>((const cx<float>*)dA, N, ld, d_perm, trans, nrhs, (cx<float>*)dB, ldb, (cx<float>*)dY, s);
+  set_error("lu_solve: dtype must be C128 or C64");
+  return GBEM_EINVAL;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 residual R = B - A X for a C64 or C128 matrix A and C128 X, B
+// ---------------------------------------------------------------------------
+template <typename TA>
+__global__ void __launch_bounds__(128) residual_partial(const cx<TA>* A, long long lda, const cx<double>* X, long long ldx,
+                                                        int N, int nrhs, int cchunk, cx<double>* part) {
+  __shared__ cx<double> xs[128][8];
+  const int i = blockIdx.x * 128 + threadIdx.x;
+  const int c0 = blockIdx.y * cchunk, c1 = min(N, c0 + cchunk);
+  cx<double> acc[8];
+  for (int r = 0; r < 8; r++) acc[r] = mk(0.0, 0.0);
+  for (int j0 = c0; j0 < c1; j0 += 128) {
+    int nj = min(128, c1 - j0);
+    __syncthreads();
+    for (int q = threadIdx.x; q < nj * nrhs; q += 128) xs[q % nj][q / nj] = X[(j0 + q % nj) + (long long)(q / nj) * ldx];
+    __syncthreads();
+    if (i < N)
+      for (int j = 0; j < nj; j++) {
+        cx<TA> a = A[i + (long long)(j0 + j) * lda];
+        cx<double> ad = mk((double)a.re, (double)a.im);
+        for (int r = 0; r < nrhs; r++) acc[r] = acc[r] + ad * xs[j][r];
+      }
+  }
+  if (i < N)
+    for (int r = 0; r < nrhs; r++) part[((size_t)blockIdx.y * nrhs + r) * N + i] = acc[r];
+}
+
+__global__ void residual_finish(const cx<double>* B, long long ldb, const cx<double>* part, int nsplit, int N, int nrhs,
+                                cx<double>* R, long long ldr) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  for (int r = 0; r < nrhs; r++) {
+    cx<double> s = B[i + (long long)r * ldb];
+    for (int p = 0; p < nsplit; p++) s = s - part[((size_t)p * nrhs + r) * N + i];
+    R[i + (long long)r * ldr] = s;
+  }
+}
+
+gbem_status residual_device(const void* dA, int lda, int dtype, int N, const double* dX, int ldx, const double* dB,
+                            int ldb, int nrhs, double* dR, int ldr, void* part, cudaStream_t s) {
+  const int nsplit = 8;
+  int cchunk = (N + nsplit - 1) / nsplit;
+  cudaError_t e;
+  for (int r0 = 0; r0 < nrhs; r0 += 8) {
+    int nr = std::min(8, nrhs - r0);
+    dim3 grid((N + 127) / 128, nsplit);
+    const cx<double>* X = (const cx<double>*)dX + (long long)r0 * ldx;
+    if (dtype == GBEM_C64)
+      residual_partial<float><<<grid, 128, 0, s>>>((const cx<float>*)dA, lda, X, ldx, N, nr, cchunk, (cx<double>*)part);
+    else
+      residual_partial<double><<<grid, 128, 0, s>>>((const cx<double>*)dA, lda, X, ldx, N, nr, cchunk, (cx<double>*)part);
+    residual_finish<<<(N + 255) / 256, 256, 0, s>>>((const cx<double>*)dB + (long long)r0 * ldb, ldb, (cx<double>*)part,
+                                                   nsplit, N, nr, (cx<double>*)dR + (long long)r0 * ldr, ldr);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "residual");
+  }
+  return GBEM_OK;
+}
+
+}  // namespace gbem

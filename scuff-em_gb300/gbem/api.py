@@ -1,0 +1,237 @@
+"""Python mirror of the reference's API for the BEM hot path.
+
+``RWGGeometry`` mirrors scuff::RWGGeometry (libs/libscuff/libscuff.h:340-634)
+for what the hot path needs -- ``TotalBFs``, ``AllocateBEMMatrix``,
+``AssembleBEMMatrix``, ``AssembleRHSVector`` -- and ``HMatrix`` mirrors
+libhmat's HMatrix for ``LUFactorize``/``LUSolve`` (LBWrappers.cc:151-236).
+Everything runs through the C ABI of libgbem.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from . import _lib
+from ._lib import C128, C64, PREC_FP64, PREC_MIXED, check, lib
+from .mesh import read_msh
+
+ZVAC = 376.73031346177
+
+
+class Material:
+    """Constant (frequency-independent) eps and mu, like the reference's
+    CONST_EPS_..._MU_... materials (libs/libMatProp/libMatProp.cc:205-299)."""
+
+    def __init__(self, eps=1.0, mu=1.0):
+        self.eps = complex(eps)
+        self.mu = complex(mu)
+
+    @classmethod
+    def parse(cls, name):
+        if name is None or name.upper() in ("PEC",):
+            return None
+        if name.upper() == "VACUUM":
+            return cls()
+        m = re.match(r"CONST_(.*)$", name, re.I)
+        if not m:
+            raise ValueError("only CONST_ materials are supported: %r" % name)
+        toks = m.group(1).split("_")
+        eps, mu = 1.0, 1.0
+        for i in range(0, len(toks) - 1, 2):
+            val = _parse_cval(toks[i + 1])
+            if toks[i].upper() == "EPS":
+                eps = val
+            elif toks[i].upper() == "MU":
+                mu = val
+        return cls(eps, mu)
+
+
+def _parse_cval(s):
+    m = re.match(r"^([-+0-9.eE]+?)([-+])([0-9.eE]+)[iI]$", s)
+    if m:
+        re_, sg, im = m.groups()
+        return complex(float(re_), (1 if sg == "+" else -1) * float(im))
+    return complex(float(s), 0.0)
+
+
+class HMatrix:
+    """A device-resident N x N BEM matrix (complex128 or complex64)."""
+
+    def __init__(self, geometry, dtype=C128):
+        self.geometry = geometry
+        self.dtype = dtype
+        self.N = geometry.TotalBFs
+        h = ctypes.c_void_p()
+        check(lib().gbem_matrix_create(geometry._h, dtype, ctypes.byref(h)))
+        self._h = h
+        self.ipiv = None
+        self.info = None
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().gbem_matrix_destroy(self._h)
+            self._h = None
+
+    @property
+    def np_dtype(self):
+        return np.complex128 if self.dtype == C128 else np.complex64
+
+    def device_ptr(self):
+        p, ld = ctypes.c_void_p(), ctypes.c_int()
+        check(lib().gbem_matrix_device_ptr(self._h, ctypes.byref(p), ctypes.byref(ld)))
+        return p.value, ld.value
+
+    def numpy(self):
+        """The matrix as a column-major numpy array (M[r, c])."""
+        a = np.empty((self.N, self.N), dtype=self.np_dtype, order="F")
+        check(lib().gbem_matrix_download(self._h, a.ctypes.data, self.N))
+        return a
+
+    def set(self, a):
+        a = np.asfortranarray(a, dtype=self.np_dtype)
+        check(lib().gbem_matrix_upload(self._h, a.ctypes.data, self.N))
+
+    def LUFactorize(self):
+        """In-place LU with partial pivoting; returns LAPACK's info (0 = ok)."""
+        ipiv = np.zeros(self.N, dtype=np.int32)
+        info = ctypes.c_int()
+        st = lib().gbem_lu_factor(self._h, ipiv.ctypes.data, ctypes.byref(info))
+        if st not in (_lib.GBEM_OK, _lib.GBEM_ESINGULAR):
+            check(st)
+        self.ipiv, self.info = ipiv, info.value
+        return info.value
+
+    def LUSolve(self, B, Trans="N"):
+        """Solve op(M) X = B for a vector or an N x nrhs array; returns X."""
+        B = np.asarray(B)
+        vec = B.ndim == 1
+        X = np.array(B.reshape(self.N, -1), dtype=self.np_dtype, order="F", copy=True)
+        check(lib().gbem_lu_solve(self._h, Trans.encode()[:1], X.shape[1], X.ctypes.data, self.N))
+        return X[:, 0] if vec else X
+
+
+class RWGGeometry:
+    """Surfaces, regions and materials of a compact (non-periodic) geometry.
+
+    surfaces: list of dicts with keys V (nv x 3), P (np x 3, 0-based), and
+    material (None for PEC, a Material, or a CONST_ material name).  Region 0
+    is the exterior medium (``exterior`` material, vacuum by default); each
+    dielectric surface encloses its own region."""
+
+    def __init__(self, surfaces, exterior=None, device=0):
+        self.surfaces = []
+        self.materials = [exterior if isinstance(exterior, Material) else (Material.parse(exterior) or Material())]
+        descs = (_lib.SurfaceDesc * len(surfaces))()
+        self._keep = []
+        for i, s in enumerate(surfaces):
+            V = np.ascontiguousarray(s["V"], dtype=np.float64)
+            P = np.ascontiguousarray(s["P"], dtype=np.int32)
+            mat = s.get("material")
+            if isinstance(mat, str):
+                mat = Material.parse(mat)
+            pec = mat is None
+            if not pec:
+                self.materials.append(mat)
+                interior = len(self.materials) - 1
+            else:
+                interior = -1
+            self._keep += [V, P]
+            descs[i] = _lib.SurfaceDesc(len(V), V.ctypes.data, len(P), P.ctypes.data, 0, interior, 1 if pec else 0)
+            self.surfaces.append({"V": V, "P": P, "pec": pec, "interior": interior})
+        h = ctypes.c_void_p()
+        check(lib().gbem_geometry_create(len(surfaces), descs, len(self.materials), device, ctypes.byref(h)))
+        self._h = h
+        n = ctypes.c_int()
+        check(lib().gbem_geometry_num_bfs(h, ctypes.byref(n)))
+        self.TotalBFs = n.value
+
+    @classmethod
+    def from_scuffgeo(cls, path, device=0):
+        """Read a .scuffgeo file with OBJECT/MESHFILE/MATERIAL/DISPLACED lines
+        (RWGGeometry.cc:433-571) and CONST_ materials."""
+        base = os.path.dirname(os.path.abspath(path))
+        surfaces, cur = [], None
+        for line in open(path):
+            t = line.split("#")[0].split()
+            if not t:
+                continue
+            kw = t[0].upper()
+            if kw == "OBJECT":
+                cur = {"material": None, "disp": np.zeros(3)}
+            elif kw == "MESHFILE" and cur is not None:
+                cur["mesh"] = os.path.join(base, t[1])
+            elif kw == "MATERIAL" and cur is not None:
+                cur["material"] = t[1]
+            elif kw == "DISPLACED" and cur is not None:
+                cur["disp"] = np.array([float(x) for x in t[1:4]])
+            elif kw == "ENDOBJECT" and cur is not None:
+                V, P = read_msh(cur["mesh"])
+                surfaces.append({"V": V + cur["disp"], "P": P, "material": cur["material"]})
+                cur = None
+        return cls(surfaces, device=device)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().gbem_geometry_destroy(self._h)
+            self._h = None
+
+    def eps_mu(self, Omega):
+        eps = np.array([[m.eps.real, m.eps.imag] for m in self.materials], dtype=np.float64).ravel()
+        mu = np.array([[m.mu.real, m.mu.imag] for m in self.materials], dtype=np.float64).ravel()
+        return eps, mu
+
+    def edges(self, surface=0):
+        n = ctypes.c_int()
+        check(lib().gbem_geometry_edges(self._h, surface, ctypes.byref(n), None, None))
+        E = np.zeros((n.value, 8), dtype=np.int32)
+        L = np.zeros(n.value)
+        check(lib().gbem_geometry_edges(self._h, surface, ctypes.byref(n), E.ctypes.data, L.ctypes.data))
+        return E, L
+
+    def near_counts(self):
+        c = (ctypes.c_longlong * 4)()
+        check(lib().gbem_geometry_near_counts(self._h, c))
+        return list(c)
+
+    def AllocateBEMMatrix(self, dtype=C128):
+        return HMatrix(self, dtype)
+
+    def AssembleBEMMatrix(self, Omega, M=None, precision="fp64"):
+        """Assemble the BEM matrix at angular frequency Omega (units of
+        3e14 rad/s; lengths in microns, so the vacuum wavenumber is Omega)."""
+        prec = PREC_MIXED if precision == "mixed" else PREC_FP64
+        if M is None:
+            M = HMatrix(self, C64 if prec == PREC_MIXED else C128)
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        check(lib().gbem_assemble(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data, prec, M._h))
+        return M
+
+    def AssembleRHSVector(self, Omega, E0, nHat):
+        """Plane wave E0 exp(i k nHat.x) incident from the exterior region."""
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        e0 = np.array([[complex(e).real, complex(e).imag] for e in E0], dtype=np.float64).ravel()
+        nh = np.asarray(nHat, dtype=np.float64)
+        out = np.zeros(self.TotalBFs, dtype=np.complex128)
+        check(lib().gbem_rhs_planewave(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data,
+                                       e0.ctypes.data, nh.ctypes.data, out.ctypes.data))
+        return out
+
+    def solve_mixed(self, Omega, B, tol=1e-10, max_iter=10):
+        """Mixed-precision solve (FP32 far field, complex-FP32 LU, FP64
+        refinement).  Returns (X, iterations, relative residual)."""
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        B = np.asfortranarray(np.asarray(B, dtype=np.complex128).reshape(self.TotalBFs, -1))
+        X = np.zeros_like(B, order="F")
+        it, res = ctypes.c_int(), ctypes.c_double()
+        st = lib().gbem_solve_mixed(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data, B.shape[1],
+                                    B.ctypes.data, self.TotalBFs, X.ctypes.data, self.TotalBFs, tol, max_iter,
+                                    ctypes.byref(it), ctypes.byref(res))
+        if st not in (_lib.GBEM_OK, _lib.GBEM_ENOCONV):
+            check(st)
+        return X, it.value, res.value

@@ -1,0 +1,75 @@
+"""Dense LU factor/solve on the GPU against LAPACK (numpy/scipy)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _lu_host(A):
+    from gbem._lib import check, lib
+    import ctypes
+    N = A.shape[0]
+    LU = np.asfortranarray(A.astype(np.complex128))
+    ipiv = np.zeros(N, dtype=np.int32)
+    info = ctypes.c_int()
+    st = lib().gbem_lu_factor_host(LU.ctypes.data, N, N, ipiv.ctypes.data, ctypes.byref(info))
+    return st, LU, ipiv, info.value
+
+
+def _solve_host(LU, ipiv, B, trans="N"):
+    from gbem._lib import check, lib
+    N = LU.shape[0]
+    X = np.asfortranarray(B.astype(np.complex128).reshape(N, -1))
+    check(lib().gbem_lu_solve_host(LU.ctypes.data, N, N, ipiv.ctypes.data, trans.encode(), X.shape[1],
+                                   X.ctypes.data, N))
+    return X
+
+
+@pytest.mark.parametrize("N", [1, 7, 64, 257, 1000, 2049])
+def test_lu_matches_lapack(N):
+    import scipy.linalg as sl
+    rng = np.random.default_rng(N)
+    A = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))
+    st, LU, ipiv, info = _lu_host(A)
+    assert st == 0 and info == 0
+    lu_ref, piv_ref = sl.lu_factor(A)
+    # same pivoting rule as zgetrf (|Re|+|Im|, first maximum): identical pivots
+    assert np.array_equal(ipiv - 1, piv_ref)
+    assert np.abs(LU - lu_ref).max() / np.abs(lu_ref).max() < 1e-11
+    B = rng.standard_normal((N, 3)) + 1j * rng.standard_normal((N, 3))
+    X = _solve_host(LU, ipiv, B)
+    assert np.abs(A @ X - B).max() / np.abs(B).max() < 1e-9
+    XT = _solve_host(LU, ipiv, B, "T")
+    assert np.abs(A.T @ XT - B).max() / np.abs(B).max() < 1e-9
+
+
+def test_singular_info():
+    N = 50
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((N, N)) + 0j
+    A[:, 10] = 0.0
+    st, LU, ipiv, info = _lu_host(A)
+    from gbem._lib import GBEM_ESINGULAR
+    assert st == GBEM_ESINGULAR and info == 11
+
+
+def test_bem_matrix_c64_and_c128(golden):
+    import scipy.linalg as sl
+    from gbem import C64, RWGGeometry
+    from helpers import fixture_surfaces, omega_of
+    d = golden("ref_diel_s1_w2.npz")
+    gs, _ = fixture_surfaces(d)
+    G = RWGGeometry(gs)
+    M = G.AssembleBEMMatrix(omega_of(d))
+    A = M.numpy()
+    assert M.LUFactorize() == 0
+    b = d["rhs0"]
+    x = M.LUSolve(b)
+    xr = sl.solve(A, b)
+    assert np.abs(x - xr).max() / np.abs(xr).max() < 1e-10
+    # the reference's own solution of its own matrix (same mesh, frequency)
+    assert np.abs(x - d["kn0"]).max() / np.abs(d["kn0"]).max() < 1e-5
+    M32 = G.AssembleBEMMatrix(omega_of(d), precision="mixed")
+    assert M32.LUFactorize() == 0
+    x32 = M32.LUSolve(b.astype(np.complex64))
+    assert np.abs(x32 - xr).max() / np.abs(xr).max() < 1e-3

@@ -1,0 +1,40 @@
+"""Right-hand sides and the mixed-precision solve."""
+import numpy as np
+import pytest
+
+from helpers import fixture_surfaces, omega_of
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case,j", [("pec_s2_w1", 0), ("diel_s1_w2", 0), ("diel_s1_w2", 1)])
+def test_planewave_rhs_matches_reference(golden, case, j):
+    from gbem import RWGGeometry
+    d = golden("ref_%s.npz" % case)
+    gs, _ = fixture_surfaces(d)
+    G = RWGGeometry(gs)
+    pw = d["pw%d" % j]
+    b = G.AssembleRHSVector(omega_of(d), pw[:3], pw[3:])
+    ref = d["rhs%d" % j]
+    assert np.abs(b - ref).max() / np.abs(ref).max() < 1e-12
+
+
+def test_mixed_solve_refines_to_fp64(golden):
+    import scipy.linalg as sl
+    from gbem import RWGGeometry, mesh
+    from gbem.api import Material
+    V, P = mesh.icosphere(2)
+    G = RWGGeometry([{"V": V, "P": P, "material": Material(2.25 + 0.01j)}])
+    w = 2.0
+    B = np.stack([G.AssembleRHSVector(w, e, n) for e, n in
+                  [((1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1)), ((1, 0, 0), (0, 0, -1)), ((0, 1, 0), (0, 0, -1))]],
+                 axis=1)
+    X, it, res = G.solve_mixed(w, B, tol=1e-10, max_iter=12)
+    assert res <= 1e-10 and 1 <= it <= 12
+    # the refined solution solves the mixed-assembled (complex64) matrix to FP64 accuracy
+    M32 = G.AssembleBEMMatrix(w, precision="mixed").numpy().astype(np.complex128)
+    assert np.abs(M32 @ X - B).max() / np.abs(B).max() < 1e-9
+    # and differs from the FP64 path only by the FP32 far-field cubature
+    M64 = G.AssembleBEMMatrix(w).numpy()
+    X64 = sl.solve(M64, B)
+    assert np.abs(X - X64).max() / np.abs(X64).max() < 1e-5

@@ -1,0 +1,107 @@
+"""The CPU oracle against the reference: its own unit-test goldens
+(unitTests/unit-test-PPIs.cc:70-107) and outputs of the reference built from
+its sources (fixtures made by tests/golden/make_golden.py)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as ora
+
+# per-branch tolerances (relative to the larger of |H0|, |H1| scale), set by the
+# reference's own quadrature: LO/HO are fixed rules (bitwise formula), TD uses
+# adaptive cubature to 1e-10 (ncv=3) or at most 1000 evaluations (ncv=1,2),
+# desingularised pairs use FIPPIs from adaptive cubature at rel 1e-6 / 1e-5.
+# the 3-D common-vertex Taylor-Duffy cubature is capped at 1000 evaluations
+# (PanelPanelInteractions.cc via InitTaylorDuffyArgs, TaylorDuffy.cc:268-272);
+# at |k r| ~ 10 it stops near 3e-4, while this oracle converges to 1e-12
+# (checked by raising its order from 14 to 40 points per dimension).
+TOL = {("LO", 0): 1e-12, ("HO", 0): 5e-7, ("TD", 3): 1e-9, ("TD", 2): 1e-6, ("TD", 1): 5e-4,
+       ("DESING", 0): 1e-6, ("DESING", 1): 1e-6, ("DESING", 2): 1e-7}
+
+
+def test_unit_ppi_goldens(golden):
+    d = golden("ppi_unit.npz")
+    S = ora.Surface(d["V"], d["P"])
+    for c, exact, ref in zip(d["cases"], d["exact"], d["ref"]):
+        pa, qa, pb, qb, kr, ki = c
+        H, alg, ncv = S.ppi(int(pa), int(qa), int(pb), int(qb), kr + 1j * ki)
+        scale = max(abs(exact[0]), 1e-300)
+        # the unit test compares after rounding to float; the goldens carry 10 digits
+        assert np.abs(H[0] - exact[0]) <= 2e-6 * scale + 1e-30
+        if abs(exact[1]) > 0:
+            assert abs(H[1] - exact[1]) <= 2e-6 * abs(exact[1]) + 1e-7 * scale
+        # and against the built reference at its own branch tolerance
+        tol = TOL[(ora.ALG_NAMES[alg], ncv)]
+        assert np.abs(H - ref).max() <= tol * np.abs(ref).max() + 1e-300
+
+
+def test_ppi_all_branches(golden):
+    d = golden("ref_ppi_s2.npz")
+    S = ora.Surface(d["V"], d["P"])
+    worst = {}
+    for c, Href, alg_ref, ncv_ref in zip(d["cases"], d["H"], d["alg"], d["ncv"]):
+        pa, qa, pb, qb, kr, ki = c
+        H, alg, ncv = S.ppi(int(pa), int(qa), int(pb), int(qb), kr + 1j * ki)
+        assert (alg, ncv) == (alg_ref, ncv_ref)
+        key = (ora.ALG_NAMES[alg], ncv)
+        err = np.abs(H - Href).max() / np.abs(Href).max()
+        worst[key] = max(worst.get(key, 0.0), err)
+    for key, err in worst.items():
+        assert err <= TOL[key], (key, err)
+    assert {k[0] for k in worst} == {"LO", "HO", "TD", "DESING"}
+
+
+def test_fippi_against_reference(golden):
+    d = golden("ref_fippi_s2.npz")
+    S = ora.Surface(d["V"], d["P"])
+    for (pa, pb), ncv_ref, data in zip(d["pairs"], d["ncv"], d["data"]):
+        if ncv_ref == 3:
+            continue  # common-triangle pairs never use FIPPIs (Taylor-Duffy instead)
+        out, ncv, order = S.qifippi(int(pa), int(pb))
+        assert ncv == ncv_ref
+        scale = np.abs(data).max()
+        # reference: hcubature rel 1e-6 (ncv=0), Taylor-Duffy V2P0 rel 1e-5
+        assert np.abs(out - data).max() <= (2e-6 if ncv == 0 else 2e-5) * scale
+
+
+def test_edges_match_reference(golden):
+    d = golden("ref_pec_s2_w1.npz")
+    S = ora.Surface(d["V0"], d["P0"])
+    E, L = S.edges()
+    assert E.shape == (480, 8)
+    # Euler characteristic of a closed sphere: V - E + F = 2
+    assert len(d["V0"]) - len(E) + len(d["P0"]) == 2
+    assert np.all(E[:, 0] < E[:, 1]) and np.all(E[:, 5] >= 0)
+
+
+def _geometry(d):
+    n = int(d["objects"])
+    surfs, regs, pec, eps, mu = [], [], [], [1.0], [1.0]
+    for i in range(n):
+        V = d["V%d" % i] + d["disp%d" % i]
+        surfs.append(ora.Surface(V, d["P%d" % i]))
+        mat = str(d["mat%d" % i])
+        if mat == "PEC":
+            regs.append((0, -1)); pec.append(True)
+        else:
+            from gbem.api import Material
+            m = Material.parse(mat)
+            eps.append(m.eps); mu.append(m.mu)
+            regs.append((0, len(eps) - 1)); pec.append(False)
+    return surfs, regs, pec, eps, mu
+
+
+@pytest.mark.parametrize("case", ["diel_s1_w2", "pec2_s1_xi", "pec_s2_w1"])
+def test_matrix_against_reference(golden, case):
+    d = golden("ref_%s.npz" % case)
+    surfs, regs, pec, eps, mu = _geometry(d)
+    w = d["omega"][0] + 1j * d["omega"][1]
+    M = ora.assemble(surfs, regs, pec, w, eps, mu)
+    Mref = d["M"] if "M" in d.files else None
+    if Mref is None:
+        cols = d["cols"]
+        err = np.abs(M[:, cols] - d["Mcols"]).max() / np.abs(d["Mcols"]).max()
+    else:
+        err = np.abs(M - Mref).max() / np.abs(Mref).max()
+    # entries carry the reference's near-field quadrature error (<= ~1e-7 of
+    # the largest entry); far-field entries agree to rounding
+    assert err < 2e-7, err
