@@ -104,7 +104,7 @@ struct DevEdgeBlock {
 struct DevNear {
   int pa, pb;
   int ncv;
-  int perm;  // perm_a[i] in bits 2i..2i+1, perm_b[i] in bits 6+2i..
+  int perm_a[3], perm_b[3];  // common-vertices-first order -> mesh order
   double rmax;
 };
 
@@ -180,8 +180,8 @@ gbem_status upload_geometry(Geometry* g) {
     for (size_t i = 0; i < b.near.size(); i++) {
       const NearPair& n = b.near[i];
       DevNear d;
-      d.pa = n.pa; d.pb = n.pb; d.ncv = n.ncv; d.rmax = n.rmax; d.perm = 0;
-      for (int j = 0; j < 3; j++) d.perm |= (n.perm_a[j] << (2 * j)) | (n.perm_b[j] << (6 + 2 * j));
+      d.pa = n.pa; d.pb = n.pb; d.ncv = n.ncv; d.rmax = n.rmax;
+      for (int j = 0; j < 3; j++) { d.perm_a[j] = n.perm_a[j]; d.perm_b[j] = n.perm_b[j]; }
       dn.push_back(d);
       if (n.ncv == 3) self_l.push_back((int)i); else other_l[n.ncv].push_back((int)i);
     }
@@ -221,9 +221,6 @@ struct RegionArgs {
   cx<double> pf3[2];   // -+i eps omega
 };
 
-__device__ __forceinline__ void unpack_perm(int perm, int* pa, int* pb) {
-  for (int j = 0; j < 3; j++) { pa[j] = (perm >> (2 * j)) & 3; pb[j] = (perm >> (6 + 2 * j)) & 3; }
-}
 
 // ---------------------------------------------------------------------------
 // static near-pair table (once per geometry)
@@ -239,9 +236,7 @@ __global__ void fippi_kernel(const DevNear* near, const int* list, int n, const 
   if (d.ncv == 0) {
     fippi_far(Va, Vb, c_gx12, c_gw12, N_FIP, &F);
   } else {
-    int pa[3], pb[3];
-    unpack_perm(d.perm, pa, pb);
-    fippi_touch(d.ncv, Va, Vb, pa, pb, c_gx12, c_gw12, N_FIP, &F);
+    fippi_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, c_gx12, c_gw12, N_FIP, &F);
   }
   out[i] = F;
 }

@@ -25,6 +25,7 @@
 #include <math.h>
 
 #define GB_HD __host__ __device__ __forceinline__
+#define GB_HD_NOINLINE static __host__ __device__ __noinline__
 
 namespace gbem {
 
@@ -404,17 +405,23 @@ struct DuffyPt {
 };
 
 GB_HD void tcr_from_edge(const int* perm, const double* s0, const double* s1, rpoly* u, rpoly* v) {
-  // barycentrics on (E0,E1,E2): (1 - s1, s1 - s2, s2), affine in w
+  // barycentrics on (E0,E1,E2): (1 - s1, s1 - s2, s2), affine in w; mesh
+  // vertex perm[i] carries barycentric i (selected without data-dependent
+  // array indexing)
   double m0[3] = {1.0 - s0[0], s0[0] - s0[1], s0[1]};
   double m1[3] = {-s1[0], s1[0] - s1[1], s1[1]};
-  int inv[3];
-  for (int i = 0; i < 3; i++) inv[perm[i]] = i;
-  *u = rp_aff(m0[inv[1]], m1[inv[1]]);
-  *v = rp_aff(m0[inv[2]], m1[inv[2]]);
+  int i1 = perm[0] == 1 ? 0 : (perm[1] == 1 ? 1 : 2);
+  int i2 = perm[0] == 2 ? 0 : (perm[1] == 2 ? 1 : 2);
+  double u0 = i1 == 0 ? m0[0] : (i1 == 1 ? m0[1] : m0[2]);
+  double u1 = i1 == 0 ? m1[0] : (i1 == 1 ? m1[1] : m1[2]);
+  double v0 = i2 == 0 ? m0[0] : (i2 == 1 ? m0[1] : m0[2]);
+  double v1 = i2 == 0 ? m1[0] : (i2 == 1 ? m1[1] : m1[2]);
+  *u = rp_aff(u0, u1);
+  *v = rp_aff(v0, v1);
 }
 
-GB_HD void fippi_touch_point(const double* Ea, const double* Eb, const int* pa, const int* pb, const double* V0a,
-                             const DuffyPt& pt, Fippi* F) {
+GB_HD_NOINLINE void fippi_touch_point(const double* Ea, const double* Eb, const int* pa, const int* pb,
+                                      const double* V0a, const DuffyPt& pt, Fippi* F) {
   double A[3], B[3], Ap[3], Bp[3], D[3];
   for (int i = 0; i < 3; i++) {
     A[i] = Ea[3 + i] - Ea[i]; B[i] = Ea[6 + i] - Ea[3 + i];
@@ -463,7 +470,10 @@ GB_HD void fippi_touch(int ncv, const double* Va, const double* Vb, const int* p
                        const double* gw, int n, Fippi* F) {
   double Ea[9], Eb[9];
   for (int i = 0; i < 3; i++)
-    for (int c = 0; c < 3; c++) { Ea[3 * i + c] = Va[3 * pa[i] + c]; Eb[3 * i + c] = Vb[3 * pb[i] + c]; }
+    for (int c = 0; c < 3; c++) {
+      Ea[3 * i + c] = pa[i] == 0 ? Va[c] : (pa[i] == 1 ? Va[3 + c] : Va[6 + c]);
+      Eb[3 * i + c] = pb[i] == 0 ? Vb[c] : (pb[i] == 1 ? Vb[3 + c] : Vb[6 + c]);
+    }
   fippi_zero(F);
   DuffyPt pt;
   if (ncv == 1) {
@@ -473,9 +483,8 @@ GB_HD void fippi_touch(int ncv, const double* Va, const double* Vb, const int* p
           for (int i3 = 0; i3 < n; i3++) {
             double al = gx[i1], be = gx[i2], ga = gx[i3];
             pt.sa0[0] = pt.sa0[1] = pt.sb0[0] = pt.sb0[1] = 0.0;
-            double* s0 = reg == 0 ? pt.sa1 : pt.sb1;
-            double* s1 = reg == 0 ? pt.sb1 : pt.sa1;
-            s0[0] = 1.0; s0[1] = al; s1[0] = be; s1[1] = be * ga;
+            if (reg == 0) { pt.sa1[0] = 1.0; pt.sa1[1] = al; pt.sb1[0] = be; pt.sb1[1] = be * ga; }
+            else { pt.sb1[0] = 1.0; pt.sb1[1] = al; pt.sa1[0] = be; pt.sa1[1] = be * ga; }
             pt.om = rp_aff(0.0, 0.0); pt.om.c[3] = be;
             pt.W = gw[i1] * gw[i2] * gw[i3];
             fippi_touch_point(Ea, Eb, pa, pb, Va, pt, F);

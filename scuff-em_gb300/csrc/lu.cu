@@ -29,6 +29,7 @@ namespace gbem {
 bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long lda, const cx<float>* B,
                     long long ldb, int m, int n, int k, void* ws, size_t ws_bytes, cudaStream_t s, cudaError_t* err);
 size_t tc_gemm_ws_bytes(int m, int n, int k);
+int tc_gemm_error(bool reset);
 
 template <typename T> struct Stash {
   cx<T>* cand_rows;  // [2][G][w]
@@ -345,6 +346,10 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   e = cudaMemcpyAsync(h_info, d_info, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_status(e, "LU");
+  if (sizeof(T) == 4 && tc_gemm_error(true)) {
+    set_error("LU: a bounded wait in the tensor-core update gave up");
+    return GBEM_ETIMEOUT;
+  }
   return GBEM_OK;
 }
 
