@@ -81,6 +81,11 @@ gbem_status gbem_geometry_num_bfs(const gbem_geometry *g, int *N);
  * PIndex MIndex, libscuff.h:124-146) and edge lengths. */
 gbem_status gbem_geometry_edges(const gbem_geometry *g, int surface, int *num_edges,
                                 int *edge_table, double *lengths);
+/* Run this geometry's device work on a caller-owned CUDA stream (a
+ * cudaStream_t passed as void*; NULL restores the library's own stream).
+ * No counterpart in the reference (host-only); lets a caller order the
+ * library's kernels with its own work and time them with its own events. */
+gbem_status gbem_geometry_set_stream(gbem_geometry *g, void *stream);
 /* Counts of near panel pairs by common-vertex number (0..3), for logging. */
 gbem_status gbem_geometry_near_counts(const gbem_geometry *g, long long counts[4]);
 
@@ -139,6 +144,26 @@ gbem_status gbem_solve_mixed(gbem_geometry *g, double omega_re, double omega_im,
                              const double *eps, const double *mu, int nrhs,
                              const double *B, int ldb, double *X, int ldx,
                              double tol, int max_iter, int *iters, double *resid);
+
+/* Device-resident variant of gbem_solve_mixed: dB and dX are device
+ * pointers (N x nrhs complex128, column-major).  No counterpart in the
+ * reference, whose solves run on host arrays; it serves callers whose
+ * right-hand sides already live in GPU memory.  The C64 matrix, its factor
+ * and the refinement workspace are cached on the geometry between calls. */
+gbem_status gbem_solve_mixed_device(gbem_geometry *g, double omega_re, double omega_im,
+                                    const double *eps, const double *mu, int nrhs,
+                                    const void *dB, int ldb, void *dX, int ldx,
+                                    double tol, int max_iter, int *iters, double *resid);
+
+/* Process-wide stage statistics (no counterpart in the reference, whose
+ * stage timings are log lines, SurfaceSurfaceInteractions.cc:550-558):
+ * returns the device milliseconds (CUDA events on the launching stream) and
+ * kernel-launch counts accumulated since the previous call, per stage
+ * [0] far-field tiles, [1] near/singular pairs, [2] LU panels, [3] LU
+ * trailing updates, [4] triangular solves, [5] FP64 residuals, [6] other,
+ * [7] reserved; then resets them.  enable != 0 turns event timing on for
+ * subsequent calls (launch counts are always kept). */
+gbem_status gbem_stats(int enable, double ms[8], long long counts[8]);
 
 /* ---- right-hand sides ----------------------------------------------------- */
 /* Plane-wave right-hand side (AssembleRHSVector.cc:145-255 with a PlaneWave

@@ -22,6 +22,7 @@
 //                 sum is deterministic and needs no atomics.
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <vector>
 #include "bem_math.cuh"
 #include "gbem_internal.h"
@@ -472,11 +473,14 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
   // entries: sum of the four P/M contributions times La Lb
   cx<T>* out = reinterpret_cast<cx<T>*>(a.out);
   const long long ld = a.ld;
-  const int mirror = !(a.sym && tile.x == tile.y);
-  for (int pass = 0; pass < 1 + mirror; pass++) {
+  // A diagonal tile of a symmetric block writes its upper triangle and
+  // mirrors it, so the matrix is exactly symmetric (AssembleBEMMatrix.cc:753-758).
+  const bool diag = a.sym && tile.x == tile.y;
+  for (int pass = 0; pass < 2; pass++) {
     for (int q = threadIdx.x; q < NR * NCc; q += blockDim.x) {
       int i, j;
       if (pass == 0) { i = q % NR; j = q / NR; } else { j = q % NCc; i = q / NCc; }
+      if (diag && (pass == 0 ? i > j : i >= j)) continue;
       const cx<T>* s = slots + (size_t)(i * TE + j) * 4 * NC;
       cx<T> v[3];
       for (int c = 0; c < NC; c++) v[c] = (s[c] - s[NC + c]) - (s[2 * NC + c] - s[3 * NC + c]);
@@ -525,7 +529,9 @@ gbem_status compute_fippi(Geometry* g, cudaStream_t s) {
   for (size_t bi = 0; bi < g->blocks.size(); bi++) {
     DevBlock* db = g->dblocks[bi];
     if (db->nother == 0) continue;
+    StatTimer t(ST_NEAR, s);
     fippi_kernel<<<(db->nother + 63) / 64, 64, 0, s>>>(db->near, db->other_list, db->nother, g->d_pv, db->fippi);
+    stats_launch(ST_NEAR);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e, "fippi_kernel");
   }
@@ -582,14 +588,19 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
       ra.pfc[r] = (k.re == 0.0 && k.im == 0.0) ? cxd(0.0, 0.0) : cdiv(pf2, I * k);
       ra.pf3[r] = (-sg) * (I * ep * omega);
     }
-    if (db->nself) {
-      self_kernel<<<(db->nself + 63) / 64, 64, 0, s>>>(db->near, db->self_list, db->nself, g->d_pv, ra, db->nearval);
-      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "self_kernel");
-    }
-    if (db->nother) {
-      near_kernel<<<(db->nother + 63) / 64, 64, 0, s>>>(db->near, db->other_list, db->nother, g->d_pv, db->fippi, ra,
-                                                        db->nearval, d_status);
-      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "near_kernel");
+    {
+      StatTimer tn(ST_NEAR, s);
+      if (db->nself) {
+        stats_launch(ST_NEAR);
+        self_kernel<<<(db->nself + 63) / 64, 64, 0, s>>>(db->near, db->self_list, db->nself, g->d_pv, ra, db->nearval);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "self_kernel");
+      }
+      if (db->nother) {
+        stats_launch(ST_NEAR);
+        near_kernel<<<(db->nother + 63) / 64, 64, 0, s>>>(db->near, db->other_list, db->nother, g->d_pv, db->fippi,
+                                                          ra, db->nearval, d_status);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "near_kernel");
+      }
     }
     TileArgs ta;
     ta.rows = db->rows; ta.cols = db->cols; ta.tiles = db->tiles;
@@ -601,6 +612,8 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
     ta.sym = b.sym ? 1 : 0;
     ta.out = dM; ta.ld = ld;
     int nc = (b.bpe_a == 2 && b.bpe_b == 2) ? 3 : ((b.bpe_a == 1 && b.bpe_b == 1) ? 1 : 2);
+    StatTimer tf(ST_FAR, s);
+    stats_launch(ST_FAR);
     if (precision == GBEM_PREC_MIXED) {
       e = nc == 1 ? launch_tiles<float, 1>(ta, ra, db->ntiles, s)
                   : nc == 2 ? launch_tiles<float, 2>(ta, ra, db->ntiles, s) : launch_tiles<float, 3>(ta, ra, db->ntiles, s);

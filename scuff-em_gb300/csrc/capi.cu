@@ -1,5 +1,6 @@
 // capi.cu -- the extern "C" boundary declared in include/gbem.h.
 #include <cstdarg>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <cmath>
@@ -22,6 +23,43 @@ gbem_status cuda_status(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return GBEM_OK;
   set_error("%s: %s", what, cudaGetErrorString(e));
   return e == cudaErrorMemoryAllocation ? GBEM_ENOMEM : GBEM_ECUDA;
+}
+
+// ---- stage statistics ----
+static std::mutex g_stats_mu;
+static bool g_stats_on = false;
+static long long g_counts[ST_N] = {0};
+struct Pending { int stage; cudaEvent_t a, b; };
+static std::vector<Pending> g_pending;
+static double g_ms[ST_N] = {0};
+
+void stats_launch(int stage, int n) {
+  std::lock_guard<std::mutex> l(g_stats_mu);
+  g_counts[stage] += n;
+}
+
+StatTimer::StatTimer(int st, cudaStream_t str) : stage(st), s(str) {
+  if (!g_stats_on) return;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) { a = b = nullptr; return; }
+  cudaEventRecord(a, s);
+}
+StatTimer::~StatTimer() {
+  if (!a) return;
+  cudaEventRecord(b, s);
+  std::lock_guard<std::mutex> l(g_stats_mu);
+  g_pending.push_back({stage, a, b});
+}
+
+static void stats_collect() {
+  std::lock_guard<std::mutex> l(g_stats_mu);
+  for (auto& p : g_pending) {
+    float ms = 0;
+    cudaEventSynchronize(p.b);
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) g_ms[p.stage] += ms;
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  g_pending.clear();
 }
 
 gbem_status rhs_planewave_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, const double* E0,
@@ -83,9 +121,23 @@ gbem_status gbem_geometry_destroy(gbem_geometry* g) {
     cudaSetDevice(g->device);
     cudaStreamSynchronize(g->stream);
   }
+  if (g->mixedM) { gbem_matrix_destroy((gbem_matrix*)g->mixedM); gbem_matrix_destroy((gbem_matrix*)g->mixedF); }
+  cudaFree(g->mixed_ws);
   if (g->d_pv) free_geometry_device(g);
-  if (g->stream) cudaStreamDestroy(g->stream);
+  if (g->own_stream) cudaStreamDestroy(g->own_stream);
+  else if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
+  return GBEM_OK;
+}
+
+gbem_status gbem_geometry_set_stream(gbem_geometry* g, void* stream) {
+  if (!g) { set_error("gbem_geometry_set_stream: NULL geometry"); return GBEM_EINVAL; }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  if (!g->own_stream) g->own_stream = g->stream;
+  cudaStreamSynchronize(g->stream);
+  g->stream = stream ? (cudaStream_t)stream : g->own_stream;
+  if (g->mixedM) { ((gbem_matrix*)g->mixedM)->stream = g->stream; ((gbem_matrix*)g->mixedF)->stream = g->stream; }
   return GBEM_OK;
 }
 
@@ -326,9 +378,9 @@ __global__ void colnorm2(const double2* a, int N, int nrhs, double* out) {
   if (threadIdx.x == 0) out[r] = red[0];
 }
 
-gbem_status gbem_solve_mixed(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
-                             int nrhs, const double* B, int ldb, double* X, int ldx, double tol, int max_iter, int* iters,
-                             double* resid) {
+static gbem_status solve_mixed_impl(gbem_geometry* g, double omega_re, double omega_im, const double* eps,
+                                    const double* mu, int nrhs, const void* B, int ldb, bool b_host, void* X, int ldx,
+                                    bool x_host, double tol, int max_iter, int* iters, double* resid) {
   if (!g || !B || !X || nrhs <= 0 || nrhs > 64 || ldb < g->N || ldx < g->N) {
     set_error("gbem_solve_mixed: bad arguments");
     return GBEM_EINVAL;
@@ -337,27 +389,40 @@ gbem_status gbem_solve_mixed(gbem_geometry* g, double omega_re, double omega_im,
   if (st0 != GBEM_OK) return st0;
   const int N = g->N;
   cudaStream_t s = g->stream;
-  gbem_matrix *M = nullptr, *F = nullptr;
-  gbem_status st = gbem_matrix_create(g, GBEM_C64, &M);
-  if (st == GBEM_OK) st = gbem_matrix_create(g, GBEM_C64, &F);
-  void *dB = nullptr, *dX = nullptr, *dR = nullptr, *dD = nullptr, *dY = nullptr, *part = nullptr;
-  double* dn = nullptr;
-  cudaError_t e = cudaSuccess;
-  if (st == GBEM_OK) {
-    e = cudaMalloc(&dB, (size_t)N * nrhs * 16);
-    if (e == cudaSuccess) e = cudaMalloc(&dX, (size_t)N * nrhs * 16);
-    if (e == cudaSuccess) e = cudaMalloc(&dR, (size_t)N * nrhs * 16);
-    if (e == cudaSuccess) e = cudaMalloc(&dD, (size_t)N * nrhs * 8);
-    if (e == cudaSuccess) e = cudaMalloc(&dY, (size_t)N * 8 * 8);
-    if (e == cudaSuccess) e = cudaMalloc(&part, (size_t)8 * 8 * N * 16);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&dn, sizeof(double) * 2 * nrhs);
-    if (e != cudaSuccess) st = cuda_status(e, "gbem_solve_mixed alloc");
+  // matrices and workspaces are cached on the geometry between solves
+  gbem_status st = GBEM_OK;
+  if (!g->mixedM || g->mixed_nrhs < nrhs) {
+    if (g->mixedM) { gbem_matrix_destroy((gbem_matrix*)g->mixedM); gbem_matrix_destroy((gbem_matrix*)g->mixedF); }
+    cudaFree(g->mixed_ws);
+    g->mixedM = g->mixedF = nullptr;
+    g->mixed_ws = nullptr;
+    gbem_matrix *M = nullptr, *F = nullptr;
+    st = gbem_matrix_create(g, GBEM_C64, &M);
+    if (st == GBEM_OK) st = gbem_matrix_create(g, GBEM_C64, &F);
+    if (st != GBEM_OK) return st;
+    g->mixedM = M; g->mixedF = F;
+    size_t wsb = (size_t)N * nrhs * 16 * 4 + (size_t)N * nrhs * 8 + (size_t)N * 8 * 8 + (size_t)8 * 8 * N * 16 + 4096;
+    cudaError_t e = cudaMalloc(&g->mixed_ws, wsb);
+    if (e != cudaSuccess) return cuda_status(e, "gbem_solve_mixed alloc");
+    g->mixed_nrhs = nrhs;
   }
-  if (st == GBEM_OK) st = gbem_assemble(g, omega_re, omega_im, eps, mu, GBEM_PREC_MIXED, M);
+  gbem_matrix* M = (gbem_matrix*)g->mixedM;
+  gbem_matrix* F = (gbem_matrix*)g->mixedF;
+  unsigned char* w = (unsigned char*)g->mixed_ws;
+  void* dB = w; w += (size_t)N * nrhs * 16;
+  void* dX = w; w += (size_t)N * nrhs * 16;
+  void* dR = w; w += (size_t)N * nrhs * 16;
+  double* dn = (double*)w; w += (size_t)N * nrhs * 16;
+  void* dD = w; w += (size_t)N * nrhs * 8;
+  void* dY = w; w += (size_t)N * 8 * 8;
+  void* part = w;
+  cudaError_t e = cudaSuccess;
+  st = gbem_assemble(g, omega_re, omega_im, eps, mu, GBEM_PREC_MIXED, M);
   if (st == GBEM_OK) {
     e = cudaMemcpyAsync(F->d, M->d, (size_t)N * N * 8, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess)
-      e = cudaMemcpy2DAsync(dB, (size_t)N * 16, B, (size_t)ldb * 16, (size_t)N * 16, nrhs, cudaMemcpyHostToDevice, s);
+      e = cudaMemcpy2DAsync(dB, (size_t)N * 16, B, (size_t)ldb * 16, (size_t)N * 16, nrhs,
+                            b_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(dX, 0, (size_t)N * nrhs * 16, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dR, dB, (size_t)N * nrhs * 16, cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) st = cuda_status(e, "gbem_solve_mixed setup");
@@ -367,6 +432,7 @@ gbem_status gbem_solve_mixed(gbem_geometry* g, double omega_re, double omega_im,
   std::vector<double> bn(nrhs), rn(nrhs);
   if (st == GBEM_OK) {
     colnorm2<<<nrhs, 256, 0, s>>>((const double2*)dB, N, nrhs, dn);
+    stats_launch(ST_OTHER);
     e = cudaMemcpyAsync(bn.data(), dn, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) st = cuda_status(e, "norm");
@@ -376,12 +442,22 @@ gbem_status gbem_solve_mixed(gbem_geometry* g, double omega_re, double omega_im,
   size_t nel = (size_t)N * nrhs;
   while (st == GBEM_OK && it < max_iter) {
     to_c64<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>((const double2*)dR, (float2*)dD, nel);
-    st = lu_solve_device(F->d, N, N, GBEM_C64, F->d_perm, 'N', nrhs, dD, N, dY, s);
+    stats_launch(ST_OTHER);
+    {
+      StatTimer t(ST_SOLVE, s);
+      st = lu_solve_device(F->d, N, N, GBEM_C64, F->d_perm, 'N', nrhs, dD, N, dY, s);
+    }
     if (st != GBEM_OK) break;
     add_c64<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>((double2*)dX, (const float2*)dD, nel);
-    st = residual_device(M->d, N, GBEM_C64, N, (const double*)dX, N, (const double*)dB, N, nrhs, (double*)dR, N, part, s);
+    stats_launch(ST_OTHER);
+    {
+      StatTimer t(ST_RESID, s);
+      st = residual_device(M->d, N, GBEM_C64, N, (const double*)dX, N, (const double*)dB, N, nrhs, (double*)dR, N,
+                           part, s);
+    }
     if (st != GBEM_OK) break;
     colnorm2<<<nrhs, 256, 0, s>>>((const double2*)dR, N, nrhs, dn);
+    stats_launch(ST_OTHER);
     e = cudaMemcpyAsync(rn.data(), dn, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { st = cuda_status(e, "refinement"); break; }
@@ -391,20 +467,49 @@ gbem_status gbem_solve_mixed(gbem_geometry* g, double omega_re, double omega_im,
     if (rel <= tol) break;
   }
   if (st == GBEM_OK) {
-    e = cudaMemcpy2DAsync(X, (size_t)ldx * 16, dX, (size_t)N * 16, (size_t)N * 16, nrhs, cudaMemcpyDeviceToHost, s);
+    e = cudaMemcpy2DAsync(X, (size_t)ldx * 16, dX, (size_t)N * 16, (size_t)N * 16, nrhs,
+                          x_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) st = cuda_status(e, "gbem_solve_mixed download");
   }
   if (iters) *iters = it;
   if (resid) *resid = rel;
-  cudaFree(dB); cudaFree(dX); cudaFree(dR); cudaFree(dD); cudaFree(dY); cudaFree(part); cudaFree(dn);
-  gbem_matrix_destroy(M);
-  gbem_matrix_destroy(F);
   if (st == GBEM_OK && rel > tol) {
     set_error("refinement stopped at relative residual %.3e after %d sweeps (tol %.1e)", rel, it, tol);
     return GBEM_ENOCONV;
   }
   return st;
+}
+
+gbem_status gbem_solve_mixed(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
+                             int nrhs, const double* B, int ldb, double* X, int ldx, double tol, int max_iter, int* iters,
+                             double* resid) {
+  return solve_mixed_impl(g, omega_re, omega_im, eps, mu, nrhs, B, ldb, true, X, ldx, true, tol, max_iter, iters, resid);
+}
+
+gbem_status gbem_solve_mixed_device(gbem_geometry* g, double omega_re, double omega_im, const double* eps,
+                                    const double* mu, int nrhs, const void* dB, int ldb, void* dX, int ldx, double tol,
+                                    int max_iter, int* iters, double* resid) {
+  return solve_mixed_impl(g, omega_re, omega_im, eps, mu, nrhs, dB, ldb, false, dX, ldx, false, tol, max_iter, iters,
+                          resid);
+}
+
+gbem_status gbem_stats(int enable, double* ms, long long* counts) {
+  if (g_stats_on) {
+    for (int d = 0; d < 1; d++) cudaDeviceSynchronize();
+  }
+  stats_collect();
+  {
+    std::lock_guard<std::mutex> l(g_stats_mu);
+    for (int i = 0; i < ST_N; i++) {
+      if (ms) ms[i] = g_ms[i];
+      if (counts) counts[i] = g_counts[i];
+      g_ms[i] = 0;
+      g_counts[i] = 0;
+    }
+    g_stats_on = enable != 0;
+  }
+  return GBEM_OK;
 }
 
 gbem_status gbem_rhs_planewave(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,

@@ -69,11 +69,17 @@ struct Geometry {
   long long near_counts[4] = {0, 0, 0, 0};
   // device data (owned)
   cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;  // the library's stream while a caller's is in use
   double* d_pv = nullptr;    // 9 per global panel
   double* d_pc = nullptr;    // 4 per global panel: centroid, radius
   std::vector<DevBlock*> dblocks;
   bool fippi_ready = false;
   std::string err;
+  // cached buffers of the mixed-precision solve
+  void* mixedM = nullptr;
+  void* mixedF = nullptr;
+  void* mixed_ws = nullptr;
+  int mixed_nrhs = 0;
 };
 
 struct Matrix {
@@ -104,6 +110,17 @@ gbem_status lu_solve_device(const void* dA, int N, int ld, int dtype, const int*
                             void* dB, int ldb, void* dY, cudaStream_t s);
 gbem_status residual_device(const void* dA, int lda, int dtype, int N, const double* dX, int ldx, const double* dB,
                             int ldb, int nrhs, double* dR, int ldr, void* part, cudaStream_t s);
+
+// per-stage device timing and launch counts (process-wide; see gbem_stats)
+enum Stage { ST_FAR = 0, ST_NEAR = 1, ST_PANEL = 2, ST_GEMM = 3, ST_SOLVE = 4, ST_RESID = 5, ST_OTHER = 6, ST_N = 8 };
+void stats_launch(int stage, int n = 1);
+struct StatTimer {
+  int stage;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  StatTimer(int stage, cudaStream_t s);
+  ~StatTimer();
+};
 
 // error helpers
 void set_error(const char* fmt, ...);

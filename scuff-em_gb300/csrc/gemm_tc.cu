@@ -39,7 +39,7 @@ constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
 constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr uint32_t TMEM_COLS = 256;
-constexpr long long SPIN_LIMIT = 1ll << 28;  // bounded waits (~seconds)
+constexpr long long SPIN_LIMIT = 1ll << 20;  // bounded waits (about a second at most)
 }  // namespace tc
 
 __device__ int g_tc_error = 0;
@@ -177,6 +177,8 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_kernel(const __grid_constant__
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tm = blockIdx.x, tn = blockIdx.y;
+  // once any CTA has given up on a wait, the rest of the grid does no work
+  if (*(volatile int*)&g_tc_error) return;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < tc::STAGES; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }

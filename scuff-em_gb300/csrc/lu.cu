@@ -313,11 +313,15 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     pa.ipiv = d_ipiv; pa.info = d_info; pa.st = st;
     size_t sm = (size_t)(pa.R * (wc + 1) + wc) * esz;
     void* args[] = {&pa};
-    e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(512), args, sm, s);
-    if (e != cudaSuccess) return cuda_status(e, "panel_kernel");
-    // interchanges to the left and right of the panel
-    laswp_kernel<T><<<(N + 255) / 256, 256, 0, s>>>(A, ld, d_ipiv, c0, c0 + wc, 0, N, c0, c0 + wc);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "laswp");
+    {
+      StatTimer tp(ST_PANEL, s);
+      stats_launch(ST_PANEL, 2);
+      e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(512), args, sm, s);
+      if (e != cudaSuccess) return cuda_status(e, "panel_kernel");
+      // interchanges to the left and right of the panel
+      laswp_kernel<T><<<(N + 255) / 256, 256, 0, s>>>(A, ld, d_ipiv, c0, c0 + wc, 0, N, c0, c0 + wc);
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "laswp");
+    }
     const int cb = c0 + wc;
     if (cb >= N) break;
     const int nrest = N - cb;
@@ -326,8 +330,13 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
       e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
       if (e != cudaSuccess) return cuda_status(e, "trsm smem");
     }
-    trsm_kernel<T><<<(nrest + 15) / 16, 256, tsm, s>>>(A, ld, c0, wc, cb, N);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
+    {
+      StatTimer tt(ST_PANEL, s);
+      stats_launch(ST_PANEL);
+      trsm_kernel<T><<<(nrest + 15) / 16, 256, tsm, s>>>(A, ld, c0, wc, cb, N);
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
+    }
+    StatTimer tg(ST_GEMM, s);
     cx<T>* C = A + cb + (long long)cb * ld;
     const cx<T>* L21 = A + cb + (long long)c0 * ld;
     const cx<T>* U12 = A + c0 + (long long)cb * ld;
@@ -336,10 +345,12 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
       done = tc_gemm_update((cx<float>*)C, ld, (const cx<float>*)L21, ld, (const cx<float>*)U12, ld, nrest, nrest, wc,
                             tcws, tcb, s, &e);
       if (e != cudaSuccess) return cuda_status(e, "tensor-core update");
+      if (done) stats_launch(ST_GEMM, 3);
     }
     if (!done) {
       dim3 grid((nrest + 63) / 64, (nrest + 63) / 64);
       gemm_simt<T><<<grid, 256, 0, s>>>(C, ld, L21, ld, U12, ld, nrest, nrest, wc);
+      stats_launch(ST_GEMM);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "gemm");
     }
   }
@@ -442,6 +453,7 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
     cx<T>* Bc = B + (long long)r0 * ldb;
     if (trans == 'N') {
       gather_rows<T><<<(N + 255) / 256, 256, 0, s>>>(Bc, ldb, Y, N, d_perm, N, nr);
+      stats_launch(ST_SOLVE, 1 + 4 * ((N + bs - 1) / bs));
       for (int i0 = 0; i0 < N; i0 += bs) {
         int b = std::min(bs, N - i0);
         diag_solve<T, true, false><<<1, 256, 0, s>>>(A, ld, Y, N, i0, b, nr);
@@ -471,6 +483,7 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
         if (i0 > 0) off_update<T, true><<<(i0 + 255) / 256, 256, 0, s>>>(A, ld, Y, N, i0, b, 0, i0, nr);
       }
       scatter_rows<T><<<(N + 255) / 256, 256, 0, s>>>(Y, N, Bc, ldb, d_perm, N, nr);
+      stats_launch(ST_SOLVE, 1 + 4 * ((N + bs - 1) / bs));
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "solve");
   }
@@ -539,6 +552,7 @@ gbem_status residual_device(const void* dA, int lda, int dtype, int N, const dou
       residual_partial<float><<<grid, 128, 0, s>>>((const cx<float>*)dA, lda, X, ldx, N, nr, cchunk, (cx<double>*)part);
     else
       residual_partial<double><<<grid, 128, 0, s>>>((const cx<double>*)dA, lda, X, ldx, N, nr, cchunk, (cx<double>*)part);
+    stats_launch(ST_RESID, 2);
     residual_finish<<<(N + 255) / 256, 256, 0, s>>>((const cx<double>*)dB + (long long)r0 * ldb, ldb, (cx<double>*)part,
                                                    nsplit, N, nr, (cx<double>*)dR + (long long)r0 * ldr, ldr);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "residual");

@@ -73,3 +73,24 @@ def test_bem_matrix_c64_and_c128(golden):
     assert M32.LUFactorize() == 0
     x32 = M32.LUSolve(b.astype(np.complex64))
     assert np.abs(x32 - xr).max() / np.abs(xr).max() < 1e-3
+
+
+def test_complex64_lu_tensor_core_update():
+    """C64 LU (split-BF16 tensor-core trailing updates) on a matrix large
+    enough for several panels; compared with LAPACK in FP64."""
+    import scipy.linalg as sl
+    from gbem import C64, RWGGeometry, mesh
+    from gbem.api import Material
+    V, P = mesh.icosphere(2)
+    G = RWGGeometry([{"V": V, "P": P, "material": Material(2.25 + 0.01j)}])
+    M = G.AssembleBEMMatrix(2.0, precision="mixed")     # N = 960: 4 panels of 256
+    A = M.numpy().astype(np.complex128)
+    assert M.LUFactorize() == 0
+    lu_ref, piv_ref = sl.lu_factor(A)
+    # pivots agree with LAPACK except where FP32 rounding reorders near-ties
+    assert np.mean((M.ipiv - 1) == piv_ref) > 0.98
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(A.shape[0]) + 1j * rng.standard_normal(A.shape[0])
+    x = M.LUSolve(b.astype(np.complex64)).astype(np.complex128)
+    xr = sl.lu_solve((lu_ref, piv_ref), b)
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 2e-4
