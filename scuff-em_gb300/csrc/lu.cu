@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
   cx<T>* rows = reinterpret_cast<cx<T>*>(smem_raw);  // [R][w+1]
   cx<T>* u = rows + (size_t)a.R * wp;                 // pivot row [w]
   __shared__ double red_v[32];
-  __shared__ int red_i[32];
+  __shared__ int red_i[32], red_c[32];
   __shared__ int s_best, s_win, s_p;
   const int G = gridDim.x, c = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   const int m0 = a.c0 + c * a.R;
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
       for (int k = tid; k < w; k += nt) a.st.diag_row[(size_t)buf * w + k] = rows[(d - m0) * wp + k];
     __threadfence();
     grid.sync();
-    // global pivot: best over all CTAs' candidates
+    // global pivot: best over all CTAs' candidates (value, row, CTA carried together)
     bv = -1.0; bi = -1;
     int bc = -1;
     for (int q = tid; q < G; q += nt) {
@@ -126,23 +126,25 @@ __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
       int oc = __shfl_down_sync(0xffffffff, bc, o);
       if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; bc = oc; }
     }
-    if ((tid & 31) == 0) { red_v[tid >> 5] = bv; red_i[tid >> 5] = bc; }
+    if ((tid & 31) == 0) { red_v[tid >> 5] = bv; red_i[tid >> 5] = bi; red_c[tid >> 5] = bc; }
     __syncthreads();
-    if (tid == 0) {
-      double b2 = -1.0;
-      int wc = -1;
-      for (int q = 0; q < (nt >> 5); q++) {
-        int cc = red_i[q];
-        if (cc < 0) continue;
-        int i = a.st.cand_idx[buf * G + cc];
-        double v = red_v[q];
-        if (wc < 0 || v > b2 || (v == b2 && i < a.st.cand_idx[buf * G + wc])) { b2 = v; wc = cc; }
+    if (tid < 32) {
+      bv = tid < (nt >> 5) ? red_v[tid] : -1.0;
+      bi = tid < (nt >> 5) ? red_i[tid] : -1;
+      bc = tid < (nt >> 5) ? red_c[tid] : -1;
+      for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_down_sync(0xffffffff, bv, o);
+        int oi = __shfl_down_sync(0xffffffff, bi, o);
+        int oc = __shfl_down_sync(0xffffffff, bc, o);
+        if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; bc = oc; }
       }
-      s_win = wc;
-      s_p = a.st.cand_idx[buf * G + wc];
-      if (c == 0) {
-        a.ipiv[d] = s_p;
-        if (b2 == 0.0 && *a.info == 0) *a.info = d + 1;
+      if (tid == 0) {
+        s_win = bc;
+        s_p = bi;
+        if (c == 0) {
+          a.ipiv[d] = bi;
+          if (bv == 0.0 && *a.info == 0) *a.info = d + 1;
+        }
       }
     }
     __syncthreads();
@@ -395,29 +397,26 @@ __global__ void scatter_rows(const cx<T>* Y, long long ldy, cx<T>* B, long long 
 template <typename T, bool LOWER, bool TRANS>
 __global__ void __launch_bounds__(256) diag_solve(const cx<T>* A, long long lda, cx<T>* X, long long ldx, int i0,
                                                    int bs, int nrhs) {
+  constexpr int BSM = sizeof(T) == 4 ? 64 : 32;
   __shared__ cx<T> x[64][8];
-  int r = blockIdx.x;  // one CTA per right-hand side... up to 8 per CTA
-  (void)r;
+  __shared__ cx<T> blk[BSM][BSM + 1];  // the diagonal block, staged once (coalesced)
+  for (int q = threadIdx.x; q < bs * bs; q += blockDim.x) {
+    int r = q % bs, c = q / bs;
+    blk[r][c] = A[(i0 + r) + (long long)(i0 + c) * lda];
+  }
   for (int q = threadIdx.x; q < bs * nrhs; q += blockDim.x) x[q % bs][q / bs] = X[i0 + q % bs + (long long)(q / bs) * ldx];
   __syncthreads();
   for (int s = 0; s < bs; s++) {
     int k = (LOWER != TRANS) ? s : bs - 1 - s;  // forward for L or U^T, backward for U or L^T
-    // finalize x[k]
     if (!LOWER) {
-      if (threadIdx.x < nrhs) {
-        cx<T> d = A[(i0 + k) + (long long)(i0 + k) * lda];
-        x[k][threadIdx.x] = cdiv(x[k][threadIdx.x], d);
-      }
+      if (threadIdx.x < nrhs) x[k][threadIdx.x] = cdiv(x[k][threadIdx.x], blk[k][k]);
       __syncthreads();
-    } else if (TRANS) {
-      // L^T is unit upper: nothing to divide
     }
-    // eliminate x[k] from the remaining rows
     int rem = (LOWER != TRANS) ? bs - k - 1 : k;
     for (int q = threadIdx.x; q < rem * nrhs; q += blockDim.x) {
       int ii = (LOWER != TRANS) ? k + 1 + q % rem : q % rem;
       int rr = q / rem;
-      cx<T> a = TRANS ? A[(i0 + k) + (long long)(i0 + ii) * lda] : A[(i0 + ii) + (long long)(i0 + k) * lda];
+      cx<T> a = TRANS ? blk[k][ii] : blk[ii][k];
       x[ii][rr] = x[ii][rr] - a * x[k][rr];
     }
     __syncthreads();
@@ -446,7 +445,7 @@ __global__ void __launch_bounds__(256) off_update(const cx<T>* A, long long lda,
 template <typename T>
 static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, char trans, int nrhs, cx<T>* B, int ldb,
                               cx<T>* Y, cudaStream_t s) {
-  const int bs = 64;
+  const int bs = sizeof(T) == 4 ? 64 : 32;  // diagonal block staged in shared memory
   cudaError_t e;
   for (int r0 = 0; r0 < nrhs; r0 += 8) {
     int nr = std::min(8, nrhs - r0);

@@ -46,8 +46,8 @@ def test_far_entries_bitwise_formula(golden, ora):
     V, P = gs[0]["V"], gs[0]["P"]
     c = V[P].mean(axis=1)
     r = np.max(np.linalg.norm(V[P] - c[:, None, :], axis=2), axis=1)
-    far_rows = []
     worst = 0.0
+    scale = np.abs(Mr).max()
     for j, col in enumerate(cols):
         pj = [E[col, 4], E[col, 5]]
         for i in range(480):
