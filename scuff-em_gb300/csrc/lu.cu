@@ -161,14 +161,21 @@ __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
     cx<T> piv = u[jj];
     T pn = piv.re * piv.re + piv.im * piv.im;
     if (pn != (T)0) {
-      cx<T> inv = mk(piv.re / pn, -piv.im / pn);
-      int rs = max(0, d + 1 - m0);
-      for (int r = rs + tid; r < nr; r += nt) rows[r * wp + jj] = rows[r * wp + jj] * inv;
-      __syncthreads();
-      int nk = w - jj - 1, nrr = nr - rs;
-      for (int q = tid; q < nrr * nk; q += nt) {
-        int r = rs + q % nrr, k = jj + 1 + q / nrr;
-        rows[r * wp + k] = rows[r * wp + k] - rows[r * wp + jj] * u[k];
+      // thread = (row, column group): the multiplier stays in a register and
+      // the row's remaining columns are strided over the groups
+      const cx<T> inv = mk(piv.re / pn, -piv.im / pn);
+      const int rs = max(0, d + 1 - m0);
+      const int RT = 128, CGN = nt / RT;
+      const int rr = tid % RT, cgi = tid / RT;
+      for (int rb = rs; rb < nr; rb += RT) {
+        const int r = rb + rr;
+        cx<T> l = mk((T)0, (T)0);
+        if (r < nr) l = rows[r * wp + jj] * inv;
+        __syncthreads();
+        if (r < nr) {
+          if (cgi == 0) rows[r * wp + jj] = l;
+          for (int k = jj + 1 + cgi; k < w; k += CGN) rows[r * wp + k] = rows[r * wp + k] - l * u[k];
+        }
       }
     }
     __syncthreads();
@@ -191,30 +198,58 @@ __global__ void laswp_kernel(cx<T>* A, long long ld, const int* ipiv, int r0, in
   }
 }
 
-// U12 = L11^{-1} A12: rows [c0, c0+w), columns [cb, N); 16 columns per CTA
+// U12 = L11^{-1} A12: rows [c0, c0+w), columns [cb, N), 32 columns per CTA.
+// L11 is walked in 32 x 32 tiles staged in shared memory: each diagonal tile
+// is a short sequential solve, each tile below it a small GEMM update.
 template <typename T>
 __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int N) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][16]
-  const int j0 = cb + blockIdx.x * 16;
-  const int nc = min(16, N - j0);
-  for (int q = threadIdx.x; q < w * nc; q += blockDim.x) {
+  cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][33]
+  __shared__ cx<T> Lt[32][33];
+  const int j0 = cb + blockIdx.x * 32;
+  const int nc = min(32, N - j0);
+  const int tid = threadIdx.x;
+  for (int q = tid; q < w * nc; q += blockDim.x) {
     int i = q % w, j = q / w;
-    B[i * 16 + j] = A[(c0 + i) + (long long)(j0 + j) * ld];
+    B[i * 33 + j] = A[(c0 + i) + (long long)(j0 + j) * ld];
   }
-  __syncthreads();
-  for (int k = 0; k < w - 1; k++) {
-    int rem = w - k - 1;
-    for (int q = threadIdx.x; q < rem * nc; q += blockDim.x) {
-      int i = k + 1 + q % rem, j = q / rem;
-      cx<T> l = A[(c0 + i) + (long long)(c0 + k) * ld];
-      B[i * 16 + j] = B[i * 16 + j] - l * B[k * 16 + j];
+  for (int kb = 0; kb < w; kb += 32) {
+    const int kn = min(32, w - kb);
+    __syncthreads();
+    for (int q = tid; q < kn * kn; q += blockDim.x) {
+      int i = q % kn, k = q / kn;
+      Lt[i][k] = A[(c0 + kb + i) + (long long)(c0 + kb + k) * ld];
     }
     __syncthreads();
+    // diagonal tile: unit lower solve, columns in parallel
+    for (int k = 0; k < kn - 1; k++) {
+      for (int q = tid; q < (kn - k - 1) * nc; q += blockDim.x) {
+        int i = k + 1 + q % (kn - k - 1), j = q / (kn - k - 1);
+        B[(kb + i) * 33 + j] = B[(kb + i) * 33 + j] - Lt[i][k] * B[(kb + k) * 33 + j];
+      }
+      __syncthreads();
+    }
+    // tiles below: B[ib] -= L[ib, kb] * B[kb]
+    for (int ib = kb + kn; ib < w; ib += 32) {
+      const int in = min(32, w - ib);
+      __syncthreads();
+      for (int q = tid; q < in * kn; q += blockDim.x) {
+        int i = q % in, k = q / in;
+        Lt[i][k] = A[(c0 + ib + i) + (long long)(c0 + kb + k) * ld];
+      }
+      __syncthreads();
+      for (int q = tid; q < in * nc; q += blockDim.x) {
+        int i = q % in, j = q / in;
+        cx<T> acc = mk((T)0, (T)0);
+        for (int k = 0; k < kn; k++) acc = acc + Lt[i][k] * B[(kb + k) * 33 + j];
+        B[(ib + i) * 33 + j] = B[(ib + i) * 33 + j] - acc;
+      }
+    }
   }
-  for (int q = threadIdx.x; q < w * nc; q += blockDim.x) {
+  __syncthreads();
+  for (int q = tid; q < w * nc; q += blockDim.x) {
     int i = q % w, j = q / w;
-    A[(c0 + i) + (long long)(j0 + j) * ld] = B[i * 16 + j];
+    A[(c0 + i) + (long long)(j0 + j) * ld] = B[i * 33 + j];
   }
 }
 
@@ -327,7 +362,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     const int cb = c0 + wc;
     if (cb >= N) break;
     const int nrest = N - cb;
-    size_t tsm = (size_t)wc * 16 * esz;
+    size_t tsm = (size_t)wc * 33 * esz;
     if (tsm > 48 * 1024) {
       e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
       if (e != cudaSuccess) return cuda_status(e, "trsm smem");
@@ -335,7 +370,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     {
       StatTimer tt(ST_PANEL, s);
       stats_launch(ST_PANEL);
-      trsm_kernel<T><<<(nrest + 15) / 16, 256, tsm, s>>>(A, ld, c0, wc, cb, N);
+      trsm_kernel<T><<<(nrest + 31) / 32, 256, tsm, s>>>(A, ld, c0, wc, cb, N);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
     }
     StatTimer tg(ST_GEMM, s);
@@ -442,6 +477,90 @@ __global__ void __launch_bounds__(256) off_update(const cx<T>* A, long long lda,
   for (int r = 0; r < nrhs; r++) X[i + (long long)r * ldx] = X[i + (long long)r * ldx] - acc[r];
 }
 
+// Inverses of the diagonal blocks of L (unit lower) or U (upper), one CTA
+// per block: Dinv[k] = (A_kk)^{-1}, bs x bs column-major, block k at
+// Dinv + k*bs*bs.  Solved as A_kk X = I column-parallel in shared memory.
+template <typename T, bool LOWER>
+__global__ void __launch_bounds__(256) diag_inverse(const cx<T>* A, long long lda, int N, int bs, cx<T>* Dinv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* blk = reinterpret_cast<cx<T>*>(smem_raw);  // [bs][bs+1] row-major
+  cx<T>* X = blk + bs * (bs + 1);                     // [bs][bs+1]
+  const int kb = blockIdx.x, i0 = kb * bs, n = min(bs, N - i0);
+  for (int q = threadIdx.x; q < n * n; q += blockDim.x) {
+    int r = q % n, c = q / n;
+    blk[r * (bs + 1) + c] = A[(i0 + r) + (long long)(i0 + c) * lda];
+    X[r * (bs + 1) + c] = mk((T)(r == c ? 1 : 0), (T)0);
+  }
+  __syncthreads();
+  for (int s = 0; s < n; s++) {
+    int k = LOWER ? s : n - 1 - s;
+    if (!LOWER) {
+      for (int j = threadIdx.x; j < n; j += blockDim.x) X[k * (bs + 1) + j] = cdiv(X[k * (bs + 1) + j], blk[k * (bs + 1) + k]);
+      __syncthreads();
+    }
+    int rem = LOWER ? n - k - 1 : k;
+    for (int q = threadIdx.x; q < rem * n; q += blockDim.x) {
+      int i = LOWER ? k + 1 + q % rem : q % rem, j = q / rem;
+      X[i * (bs + 1) + j] = X[i * (bs + 1) + j] - blk[i * (bs + 1) + k] * X[k * (bs + 1) + j];
+    }
+    __syncthreads();
+  }
+  cx<T>* out = Dinv + (size_t)kb * bs * bs;
+  for (int q = threadIdx.x; q < bs * bs; q += blockDim.x) {
+    int r = q % bs, c = q / bs;
+    out[r + (size_t)c * bs] = (r < n && c < n) ? X[r * (bs + 1) + c] : mk((T)0, (T)0);
+  }
+}
+
+// Blocked triangular solve in one cooperative launch: for each block k in
+// order, CTA 0 forms x_k = Dinv_k r_k, then every CTA subtracts
+// A[rows, block k] x_k from its share of the remaining rows.  Two grid
+// barriers per block; no per-block kernel launches.
+template <typename T, bool LOWER>
+__global__ void __launch_bounds__(256) trsv_coop(const cx<T>* A, long long lda, int N, int bs, const cx<T>* Dinv,
+                                                  cx<T>* Y, int nrhs) {
+  cg::grid_group grid = cg::this_grid();
+  __shared__ cx<T> xk[64][8];
+  __shared__ cx<T> rk[64][8];
+  const int nb = (N + bs - 1) / bs;
+  const int gthreads = gridDim.x * blockDim.x;
+  for (int s = 0; s < nb; s++) {
+    const int kb = LOWER ? s : nb - 1 - s;
+    const int i0 = kb * bs, n = min(bs, N - i0);
+    if (blockIdx.x == 0) {
+      for (int q = threadIdx.x; q < n * nrhs; q += blockDim.x) rk[q % n][q / n] = Y[i0 + q % n + (long long)(q / n) * N];
+      __syncthreads();
+      const cx<T>* D = Dinv + (size_t)kb * bs * bs;
+      for (int q = threadIdx.x; q < n * nrhs; q += blockDim.x) {
+        int r = q % n, c = q / n;
+        cx<T> acc = mk((T)0, (T)0);
+        for (int k = 0; k < n; k++) acc = acc + D[r + (size_t)k * bs] * rk[k][c];
+        Y[i0 + r + (long long)c * N] = acc;
+      }
+    }
+    __threadfence();
+    grid.sync();
+    // update the rows still to be solved
+    const int r0 = LOWER ? i0 + n : 0, r1 = LOWER ? N : i0;
+    if (r1 > r0) {
+      for (int q = threadIdx.x; q < n * nrhs; q += blockDim.x) xk[q % n][q / n] = Y[i0 + q % n + (long long)(q / n) * N];
+      __syncthreads();
+      for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gthreads) {
+        cx<T> acc[8];
+        for (int c = 0; c < nrhs; c++) acc[c] = mk((T)0, (T)0);
+        for (int k = 0; k < n; k++) {
+          cx<T> a = A[i + (long long)(i0 + k) * lda];
+          for (int c = 0; c < nrhs; c++) acc[c] = acc[c] + a * xk[k][c];
+        }
+        for (int c = 0; c < nrhs; c++) Y[i + (long long)c * N] = Y[i + (long long)c * N] - acc[c];
+      }
+      __syncthreads();
+    }
+    __threadfence();
+    grid.sync();
+  }
+}
+
 template <typename T>
 static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, char trans, int nrhs, cx<T>* B, int ldb,
                               cx<T>* Y, cudaStream_t s) {
@@ -452,17 +571,32 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
     cx<T>* Bc = B + (long long)r0 * ldb;
     if (trans == 'N') {
       gather_rows<T><<<(N + 255) / 256, 256, 0, s>>>(Bc, ldb, Y, N, d_perm, N, nr);
-      stats_launch(ST_SOLVE, 1 + 4 * ((N + bs - 1) / bs));
-      for (int i0 = 0; i0 < N; i0 += bs) {
-        int b = std::min(bs, N - i0);
-        diag_solve<T, true, false><<<1, 256, 0, s>>>(A, ld, Y, N, i0, b, nr);
-        if (i0 + b < N) off_update<T, false><<<(N - i0 - b + 255) / 256, 256, 0, s>>>(A, ld, Y, N, i0, b, i0 + b, N, nr);
-      }
-      for (int i0 = ((N - 1) / bs) * bs; i0 >= 0; i0 -= bs) {
-        int b = std::min(bs, N - i0);
-        diag_solve<T, false, false><<<1, 256, 0, s>>>(A, ld, Y, N, i0, b, nr);
-        if (i0 > 0) off_update<T, false><<<(i0 + 255) / 256, 256, 0, s>>>(A, ld, Y, N, i0, b, 0, i0, nr);
-      }
+      const int nb = (N + bs - 1) / bs;
+      cx<T>* Dinv = nullptr;
+      e = cudaMallocAsync((void**)&Dinv, sizeof(cx<T>) * (size_t)nb * bs * bs * 2, s);
+      if (e != cudaSuccess) return cuda_status(e, "solve workspace");
+      cx<T>* DinvU = Dinv + (size_t)nb * bs * bs;
+      size_t ism = sizeof(cx<T>) * 2 * bs * (bs + 1);
+      cudaFuncSetAttribute(diag_inverse<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+      cudaFuncSetAttribute(diag_inverse<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+      diag_inverse<T, true><<<nb, 256, ism, s>>>(A, ld, N, bs, Dinv);
+      diag_inverse<T, false><<<nb, 256, ism, s>>>(A, ld, N, bs, DinvU);
+      int dev = 0, nsm = 0, per = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, 0);
+      int G = std::max(1, std::min(nsm * std::max(per, 1), (N + 255) / 256));
+      int Nn = N, bsn = bs, nrn = nr;
+      const cx<T>* Ac = A;
+      long long ldl = ld;
+      void* argsL[] = {(void*)&Ac, (void*)&ldl, (void*)&Nn, (void*)&bsn, (void*)&Dinv, (void*)&Y, (void*)&nrn};
+      e = cudaLaunchCooperativeKernel((void*)trsv_coop<T, true>, dim3(G), dim3(256), argsL, 0, s);
+      if (e != cudaSuccess) return cuda_status(e, "trsv lower");
+      void* argsU[] = {(void*)&Ac, (void*)&ldl, (void*)&Nn, (void*)&bsn, (void*)&DinvU, (void*)&Y, (void*)&nrn};
+      e = cudaLaunchCooperativeKernel((void*)trsv_coop<T, false>, dim3(G), dim3(256), argsU, 0, s);
+      if (e != cudaSuccess) return cuda_status(e, "trsv upper");
+      cudaFreeAsync(Dinv, s);
+      stats_launch(ST_SOLVE, 5);
       e = cudaMemcpy2DAsync(Bc, (size_t)ldb * sizeof(cx<T>), Y, (size_t)N * sizeof(cx<T>), (size_t)N * sizeof(cx<T>), nr,
                             cudaMemcpyDeviceToDevice, s);
       if (e != cudaSuccess) return cuda_status(e, "solve copy");
@@ -482,7 +616,7 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
         if (i0 > 0) off_update<T, true><<<(i0 + 255) / 256, 256, 0, s>>>(A, ld, Y, N, i0, b, 0, i0, nr);
       }
       scatter_rows<T><<<(N + 255) / 256, 256, 0, s>>>(Y, N, Bc, ldb, d_perm, N, nr);
-      stats_launch(ST_SOLVE, 1 + 4 * ((N + bs - 1) / bs));
+      stats_launch(ST_SOLVE, 2 + 4 * ((N + bs - 1) / bs));
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "solve");
   }
