@@ -250,32 +250,46 @@ __device__ void store_near(double* dst, int ja, int jb, cx<double> kk, cx<double
   o[0] += kk.re; o[1] += kk.im; o[2] += kn.re; o[3] += kn.im; o[4] += nn.re; o[5] += nn.im;
 }
 
-__global__ void self_kernel(const DevNear* near, const int* list, int n, const double* pv, RegionArgs ra,
-                            double* nearval) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  int i = list[t];
+// one warp per common-triangle pair: the 6*NT_SELF outer points are split
+// over the lanes and the moments reduced with shuffles
+__global__ void __launch_bounds__(128) self_kernel(const DevNear* near, const int* list, int n, const double* pv,
+                                                   RegionArgs ra, double* nearval) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;  // whole warps exit together
+  int i = list[warp];
   DevNear d = near[i];
   double V[9];
   for (int c = 0; c < 9; c++) V[c] = pv[9 * (size_t)d.pa + c];
   double* dst = nearval + 54 * (size_t)i;
-  for (int c = 0; c < 54; c++) dst[c] = 0.0;
+  double acc[54];
+  for (int c = 0; c < 54; c++) acc[c] = 0.0;
   for (int r = 0; r < ra.nreg; r++) {
     cx<double> k = ra.k[r];
     if (k.re == 0.0 && k.im == 0.0) continue;
     cx<double> MG[9], MP[9];
-    self_moments(V, k, c_gx16, c_gw16, NT_SELF, MG);
-    for (int m = 0; m < 9; m++) MP[m] = mk(0.0, 0.0);
-    cx<double> m4ok2 = cdiv(mk(-4.0, 0.0), k * k);
-    for (int ja = 0; ja < 3; ja++)
-      for (int jb = 0; jb < 3; jb++) {
-        double c[9], dd[9];
-        combo_coeffs(V, V, ja, jb, c, dd);
-        cx<double> H0, H1;
-        combine(MG, MP, c, dd, m4ok2, &H0, &H1);
-        store_near(dst, ja, jb, ra.pf1[r] * H0, mk(0.0, 0.0), ra.pf3[r] * H0);
+    self_moments(V, k, c_gx16, c_gw16, NT_SELF, MG, lane, 32);
+    for (int m = 0; m < 9; m++) {
+      for (int o = 16; o > 0; o >>= 1) {
+        MG[m].re += __shfl_xor_sync(0xffffffff, MG[m].re, o);
+        MG[m].im += __shfl_xor_sync(0xffffffff, MG[m].im, o);
       }
+      MP[m] = mk(0.0, 0.0);
+    }
+    cx<double> m4ok2 = cdiv(mk(-4.0, 0.0), k * k);
+    // lane q < 9 forms combination q = 3 ja + jb
+    if (lane < 9) {
+      int ja = lane / 3, jb = lane % 3;
+      double c[9], dd[9];
+      combo_coeffs(V, V, ja, jb, c, dd);
+      cx<double> H0, H1;
+      combine(MG, MP, c, dd, m4ok2, &H0, &H1);
+      cx<double> v0 = ra.pf1[r] * H0, v2 = ra.pf3[r] * H0;
+      acc[6 * lane + 0] += v0.re; acc[6 * lane + 1] += v0.im;
+      acc[6 * lane + 4] += v2.re; acc[6 * lane + 5] += v2.im;
+    }
   }
+  if (lane < 9)
+    for (int c = 0; c < 6; c++) dst[6 * lane + c] = acc[6 * lane + c];
 }
 
 __global__ void near_kernel(const DevNear* near, const int* list, int n, const double* pv, const Fippi* fippi,
@@ -632,7 +646,7 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
       StatTimer tn(ST_NEAR, s);
       if (db->nself) {
         stats_launch(ST_NEAR);
-        self_kernel<<<(db->nself + 63) / 64, 64, 0, s>>>(db->near, db->self_list, db->nself, g->d_pv, ra, db->nearval);
+        self_kernel<<<(db->nself + 3) / 4, 128, 0, s>>>(db->near, db->self_list, db->nself, g->d_pv, ra, db->nearval);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "self_kernel");
       }
       if (db->nother) {

@@ -289,15 +289,19 @@ GB_HD rpoly rp_mul(const rpoly& a, const rpoly& b) {
 // 0 <= s2 <= s1 <= 1, i.e. TCR (u, v) = (s1 - s2, s2).
 //   gx, gw: Gauss-Legendre rule on [0,1] with nt points.
 // ---------------------------------------------------------------------------
-GB_HD void self_moments(const double* V, cx<double> k, const double* gx, const double* gw, int nt, cx<double>* MG) {
+// Outer points (sector, t) with linear index p = sector*nt + t are visited
+// for p = p0, p0 + pstride, ... (a warp can split them over its lanes).
+GB_HD void self_moments(const double* V, cx<double> k, const double* gx, const double* gw, int nt, cx<double>* MG,
+                        int p0 = 0, int pstride = 1) {
   const double inv4pi = 0.079577471545947667884;
   double E1[3], E2[3];
   for (int i = 0; i < 3; i++) { E1[i] = V[3 + i] - V[i]; E2[i] = V[6 + i] - V[3 + i]; }
   const double H[7][2] = {{1, 0}, {1, 1}, {0, 1}, {-1, 0}, {-1, -1}, {0, -1}, {1, 0}};
   const double TP[3][2] = {{0.5, 0.0}, {1.0, 0.5}, {0.5, 0.5}};
   for (int m = 0; m < 9; m++) MG[m] = mk(0.0, 0.0);
-  for (int sct = 0; sct < 6; sct++)
-    for (int it = 0; it < nt; it++) {
+  for (int pp = p0; pp < 6 * nt; pp += pstride) {
+      const int sct = pp / nt, it = pp - sct * nt;
+      {
       double t = gx[it];
       double z0 = H[sct][0] + t * (H[sct + 1][0] - H[sct][0]);
       double z1 = H[sct][1] + t * (H[sct + 1][1] - H[sct][1]);
@@ -330,6 +334,7 @@ GB_HD void self_moments(const double* V, cx<double> k, const double* gx, const d
           }
       }
     }
+  }
 }
 
 

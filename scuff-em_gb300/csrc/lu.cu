@@ -520,6 +520,8 @@ template <typename T, bool LOWER>
 __global__ void __launch_bounds__(256) trsv_coop(const cx<T>* A, long long lda, int N, int bs, const cx<T>* Dinv,
                                                   cx<T>* Y, int nrhs) {
   cg::grid_group grid = cg::this_grid();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* D = reinterpret_cast<cx<T>*>(smem_raw);  // staged Dinv block, bs x bs
   __shared__ cx<T> xk[64][8];
   __shared__ cx<T> rk[64][8];
   const int nb = (N + bs - 1) / bs;
@@ -528,31 +530,52 @@ __global__ void __launch_bounds__(256) trsv_coop(const cx<T>* A, long long lda, 
     const int kb = LOWER ? s : nb - 1 - s;
     const int i0 = kb * bs, n = min(bs, N - i0);
     if (blockIdx.x == 0) {
+      // stage the block inverse and the block's right-hand sides (independent loads)
+      const cx<T>* Dg = Dinv + (size_t)kb * bs * bs;
+      for (int q = threadIdx.x; q < bs * bs; q += blockDim.x) D[q] = Dg[q];
       for (int q = threadIdx.x; q < n * nrhs; q += blockDim.x) rk[q % n][q / n] = Y[i0 + q % n + (long long)(q / n) * N];
       __syncthreads();
-      const cx<T>* D = Dinv + (size_t)kb * bs * bs;
       for (int q = threadIdx.x; q < n * nrhs; q += blockDim.x) {
         int r = q % n, c = q / n;
         cx<T> acc = mk((T)0, (T)0);
-        for (int k = 0; k < n; k++) acc = acc + D[r + (size_t)k * bs] * rk[k][c];
+        for (int k = 0; k < n; k++) acc = acc + D[r + k * bs] * rk[k][c];
         Y[i0 + r + (long long)c * N] = acc;
       }
     }
     __threadfence();
     grid.sync();
-    // update the rows still to be solved
+    // update the rows still to be solved: 4 threads per row split the block's columns
     const int r0 = LOWER ? i0 + n : 0, r1 = LOWER ? N : i0;
     if (r1 > r0) {
       for (int q = threadIdx.x; q < n * nrhs; q += blockDim.x) xk[q % n][q / n] = Y[i0 + q % n + (long long)(q / n) * N];
       __syncthreads();
-      for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gthreads) {
+      const int sub = threadIdx.x & 3;
+      const int nrows = r1 - r0;
+      // the loop trip count is uniform over the CTA, so every lane reaches the shuffles
+      for (int base0 = (blockIdx.x * blockDim.x) >> 2; base0 < nrows; base0 += gthreads >> 2) {
+        const int base = base0 + (threadIdx.x >> 2);
+        const bool valid = base < nrows;
+        const int i = r0 + (valid ? base : 0);
         cx<T> acc[8];
         for (int c = 0; c < nrhs; c++) acc[c] = mk((T)0, (T)0);
-        for (int k = 0; k < n; k++) {
-          cx<T> a = A[i + (long long)(i0 + k) * lda];
-          for (int c = 0; c < nrhs; c++) acc[c] = acc[c] + a * xk[k][c];
+        cx<T> a[16];
+#pragma unroll
+        for (int t = 0; t < 16; t++) {
+          int k = sub + 4 * t;
+          a[t] = (valid && k < n) ? A[i + (long long)(i0 + k) * lda] : mk((T)0, (T)0);
         }
-        for (int c = 0; c < nrhs; c++) Y[i + (long long)c * N] = Y[i + (long long)c * N] - acc[c];
+#pragma unroll
+        for (int t = 0; t < 16; t++) {
+          int k = sub + 4 * t;
+          if (k < n)
+            for (int c = 0; c < nrhs; c++) acc[c] = acc[c] + a[t] * xk[k][c];
+        }
+        for (int c = 0; c < nrhs; c++) {
+          cx<T> v = acc[c];
+          v.re += __shfl_xor_sync(0xffffffff, v.re, 1); v.im += __shfl_xor_sync(0xffffffff, v.im, 1);
+          v.re += __shfl_xor_sync(0xffffffff, v.re, 2); v.im += __shfl_xor_sync(0xffffffff, v.im, 2);
+          if (valid && sub == 0) Y[i + (long long)c * N] = Y[i + (long long)c * N] - v;
+        }
       }
       __syncthreads();
     }
@@ -584,16 +607,20 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
       int dev = 0, nsm = 0, per = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, 0);
-      int G = std::max(1, std::min(nsm * std::max(per, 1), (N + 255) / 256));
+      size_t dsm = sizeof(cx<T>) * bs * bs;
+      cudaFuncSetAttribute(trsv_coop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+      cudaFuncSetAttribute(trsv_coop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, dsm);
+      // 4 threads per row; one CTA per SM is enough to keep the reads in flight
+      int G = std::max(1, std::min(nsm * std::max(per, 1), std::min(nsm, (4 * N + 255) / 256)));
       int Nn = N, bsn = bs, nrn = nr;
       const cx<T>* Ac = A;
       long long ldl = ld;
       void* argsL[] = {(void*)&Ac, (void*)&ldl, (void*)&Nn, (void*)&bsn, (void*)&Dinv, (void*)&Y, (void*)&nrn};
-      e = cudaLaunchCooperativeKernel((void*)trsv_coop<T, true>, dim3(G), dim3(256), argsL, 0, s);
+      e = cudaLaunchCooperativeKernel((void*)trsv_coop<T, true>, dim3(G), dim3(256), argsL, dsm, s);
       if (e != cudaSuccess) return cuda_status(e, "trsv lower");
       void* argsU[] = {(void*)&Ac, (void*)&ldl, (void*)&Nn, (void*)&bsn, (void*)&DinvU, (void*)&Y, (void*)&nrn};
-      e = cudaLaunchCooperativeKernel((void*)trsv_coop<T, false>, dim3(G), dim3(256), argsU, 0, s);
+      e = cudaLaunchCooperativeKernel((void*)trsv_coop<T, false>, dim3(G), dim3(256), argsU, dsm, s);
       if (e != cudaSuccess) return cuda_status(e, "trsv upper");
       cudaFreeAsync(Dinv, s);
       stats_launch(ST_SOLVE, 5);
