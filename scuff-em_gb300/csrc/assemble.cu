@@ -390,6 +390,8 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
   __shared__ double s_pc[2][PMAX][4];
   __shared__ int8_t s_hl[2][3 * PMAX], s_hs[2][3 * PMAX];
   __shared__ int s_gp[2][PMAX];
+  __shared__ float s_ev[2][PMAX][6];  // FP32 edge vectors V1-V0, V2-V0
+  __shared__ float s_cf[2][PMAX][4];  // FP32 centroid and radius (pre-check of rRel)
 
   const int2 tile = a.tiles[blockIdx.x];
   const DevEdgeBlock* RB = a.rows + tile.x;
@@ -404,6 +406,14 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
   for (int q = threadIdx.x; q < PR; q += blockDim.x) s_gp[0][q] = RB->panels[q];
   for (int q = threadIdx.x; q < PC; q += blockDim.x) s_gp[1][q] = CB->panels[q];
   __syncthreads();
+  for (int q = threadIdx.x; q < 2 * PMAX; q += blockDim.x) {
+    const int side = q / PMAX, p = q % PMAX;
+    if (p >= (side ? PC : PR)) continue;
+    const double* V = s_pv[side][p];
+    for (int c = 0; c < 3; c++) { s_ev[side][p][c] = (float)(V[3 + c] - V[c]); s_ev[side][p][3 + c] = (float)(V[6 + c] - V[c]); }
+    for (int c = 0; c < 4; c++) s_cf[side][p][c] = (float)s_pc[side][p][c];
+  }
+  __syncthreads();
 
   const T* rule = lo_rule<T>();
   for (int q = threadIdx.x; q < PR * PC; q += blockDim.x) {
@@ -415,12 +425,26 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
       la[j] = s_hl[0][3 * ia + j]; sa[j] = s_hs[0][3 * ia + j];
       lb[j] = s_hl[1][3 * ib + j]; sb[j] = s_hs[1][3 * ib + j];
     }
-    if (is_far(s_pc[0][ia], s_pc[1][ib], s_pc[0][ia][3], s_pc[1][ib][3])) {
+    // rRel > 4 decides the 6x6 rule; an FP32 estimate settles all but the
+    // pairs within 1e-4 of the threshold, which take the exact FP64 test
+    const float dx = s_cf[0][ia][0] - s_cf[1][ib][0], dy = s_cf[0][ia][1] - s_cf[1][ib][1],
+                dz = s_cf[0][ia][2] - s_cf[1][ib][2];
+    const float d2f = dx * dx + dy * dy + dz * dz, rmf = fmaxf(s_cf[0][ia][3], s_cf[1][ib][3]);
+    bool far;
+    if (d2f > 16.0008f * rmf * rmf) far = true;
+    else if (d2f < 15.9992f * rmf * rmf) far = false;
+    else far = is_far(s_pc[0][ia], s_pc[1][ib], s_pc[0][ia][3], s_pc[1][ib][3]);
+    if (far) {
       PairGeom<T> g;
       for (int c = 0; c < 3; c++) {
         g.D0[c] = (T)(Va[c] - Vb[c]);
-        g.Aa[c] = (T)(Va[3 + c] - Va[c]); g.Ba[c] = (T)(Va[6 + c] - Va[c]);
-        g.Ab[c] = (T)(Vb[3 + c] - Vb[c]); g.Bb[c] = (T)(Vb[6 + c] - Vb[c]);
+        if constexpr (sizeof(T) == 4) {
+          g.Aa[c] = s_ev[0][ia][c]; g.Ba[c] = s_ev[0][ia][3 + c];
+          g.Ab[c] = s_ev[1][ib][c]; g.Bb[c] = s_ev[1][ib][3 + c];
+        } else {
+          g.Aa[c] = (T)(Va[3 + c] - Va[c]); g.Ba[c] = (T)(Va[6 + c] - Va[c]);
+          g.Ab[c] = (T)(Vb[3 + c] - Vb[c]); g.Bb[c] = (T)(Vb[6 + c] - Vb[c]);
+        }
       }
       if constexpr (sizeof(T) == 4) {
         // FP32: moments of every region first, then each (Qa,Qb) combination

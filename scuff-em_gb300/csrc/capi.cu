@@ -115,18 +115,33 @@ static gbem_status ensure_stream(gbem_geometry* g) {
   return cuda_status(e, "device setup");
 }
 
-gbem_status gbem_geometry_destroy(gbem_geometry* g) {
-  if (!g) return GBEM_OK;
+static void geometry_release(gbem_geometry* g) {
   if (g->stream) {
     cudaSetDevice(g->device);
     cudaStreamSynchronize(g->stream);
   }
-  if (g->mixedM) { gbem_matrix_destroy((gbem_matrix*)g->mixedM); gbem_matrix_destroy((gbem_matrix*)g->mixedF); }
   cudaFree(g->mixed_ws);
+  g->mixed_ws = nullptr;
   if (g->d_pv) free_geometry_device(g);
   if (g->own_stream) cudaStreamDestroy(g->own_stream);
   else if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
+}
+
+gbem_status gbem_geometry_destroy(gbem_geometry* g) {
+  if (!g) return GBEM_OK;
+  if (g->mixedM) {
+    gbem_matrix* a = (gbem_matrix*)g->mixedM;
+    gbem_matrix* b = (gbem_matrix*)g->mixedF;
+    g->mixedM = g->mixedF = nullptr;
+    gbem_matrix_destroy(a);
+    gbem_matrix_destroy(b);
+  }
+  if (g->refs > 0) {  // live matrices still use the geometry's stream
+    g->dead = true;
+    return GBEM_OK;
+  }
+  geometry_release(g);
   return GBEM_OK;
 }
 
@@ -183,6 +198,7 @@ gbem_status gbem_matrix_create(const gbem_geometry* g, int dtype, gbem_matrix** 
     delete m;
     return cuda_status(e, "gbem_matrix_create");
   }
+  const_cast<gbem_geometry*>(g)->refs++;
   *out = m;
   return GBEM_OK;
 }
@@ -191,7 +207,9 @@ gbem_status gbem_matrix_destroy(gbem_matrix* m) {
   if (!m) return GBEM_OK;
   cudaStreamSynchronize(m->stream);
   cudaFree(m->d); cudaFree(m->d_ipiv); cudaFree(m->d_perm); cudaFree(m->ws);
+  gbem_geometry* g = const_cast<gbem_geometry*>(static_cast<const gbem_geometry*>(m->g));
   delete m;
+  if (g && --g->refs == 0 && g->dead) geometry_release(g);
   return GBEM_OK;
 }
 

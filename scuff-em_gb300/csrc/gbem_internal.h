@@ -75,6 +75,10 @@ struct Geometry {
   std::vector<DevBlock*> dblocks;
   bool fippi_ready = false;
   std::string err;
+  // matrices created on this geometry keep it alive: destroying the
+  // geometry while matrices exist defers the release to the last of them
+  int refs = 0;
+  bool dead = false;
   // cached buffers of the mixed-precision solve
   void* mixedM = nullptr;
   void* mixedF = nullptr;

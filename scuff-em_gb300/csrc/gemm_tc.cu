@@ -16,11 +16,12 @@
 // whose output columns (2j, 2j+1) are exactly (Re, Im) of C[:, j], so the
 // epilogue writes interleaved complex64 with coalesced stores.
 //
-// Kernel layout (one CTA per 128 x 256 output tile, 6 warps):
+// Kernel layout (one CTA per 128 x 256 output tile, 10 warps):
 //   warp 0   TMA producer (one elected lane), 4-stage ring of (A 16 KB, B 32 KB)
 //   warp 1   TMEM allocator and MMA issuer (one lane): 4 x (M128 N256 K16)
 //            per 64-wide k-block, tcgen05.commit frees the stage
-//   warps 2-5 epilogue: tcgen05.ld 32 lanes x 32 columns at a time, C -= D
+//   warps 2-9 epilogue: tcgen05.ld 32 lanes x 32 columns at a time, C -= D
+//            (C loads issued before the TMEM read so they overlap)
 // Every mbarrier wait is bounded; on timeout the CTA records an error code,
 // drains its outstanding TMA copies (bounded), frees its TMEM and exits.
 #include <cuda.h>
@@ -163,7 +164,7 @@ __global__ void zero_pad(__nv_bfloat16* out, long long rows, int K6, int Kp) {
 }
 
 // ---------------- the GEMM kernel ----------------
-__global__ void __launch_bounds__(192, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA,
+__global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA,
                                                           const __grid_constant__ CUtensorMap mapB, cx<float>* C,
                                                           long long ldc, int m, int n, int kblocks) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -232,27 +233,29 @@ __global__ void __launch_bounds__(192, 1) tc_gemm_kernel(const __grid_constant__
       umma_commit(accum);
     }
   } else {
-    // epilogue warps 2..5 cover TMEM lane quarters (warp % 4)
-    const int q = warp & 3;
+    // epilogue warps 2..9: warp % 4 selects the TMEM lane quarter (row block
+    // of 32), the two warps of a quarter split the 256 accumulator columns
+    const int q = warp & 3, half = (warp - 2) >> 2;
     const int row = tm * tc::BM + q * 32 + lane;
     bool ok = mbar_wait(accum, 0);
     if (!ok) atomicExch(&s_fail, 1);
     tc_fence_after();
     if (ok && !s_fail) {
-      for (int c0 = 0; c0 < tc::BN; c0 += 32) {
+      for (int c0 = half * (tc::BN / 2); c0 < (half + 1) * (tc::BN / 2); c0 += 32) {
+        const int j0 = (tn * tc::BN + c0) >> 1;
+        // issue the 16 loads of C first (independent), then the TMEM read
+        cx<float> z[16];
+#pragma unroll
+        for (int t = 0; t < 16; t++)
+          z[t] = (row < m && j0 + t < n) ? C[row + (long long)(j0 + t) * ldc] : mk(0.0f, 0.0f);
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
-        int j0 = (tn * tc::BN + c0) >> 1;
-        if (row < m) {
-          for (int t = 0; t < 16; t++) {
-            int j = j0 + t;
-            if (j < n) {
-              cx<float>* p = C + row + (long long)j * ldc;
-              cx<float> z = *p;
-              z.re -= v[2 * t];
-              z.im -= v[2 * t + 1];
-              *p = z;
-            }
+#pragma unroll
+        for (int t = 0; t < 16; t++) {
+          if (row < m && j0 + t < n) {
+            z[t].re -= v[2 * t];
+            z[t].im -= v[2 * t + 1];
+            C[row + (long long)(j0 + t) * ldc] = z[t];
           }
         }
       }
@@ -335,7 +338,7 @@ bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long l
     attr = true;
   }
   dim3 grid((m + tc::BM - 1) / tc::BM, (2 * n + tc::BN - 1) / tc::BN);
-  tc_gemm_kernel<<<grid, 192, tc::SMEM_BYTES, s>>>(ma, mb, C, ldc, m, n, Kp / tc::BK);
+  tc_gemm_kernel<<<grid, 320, tc::SMEM_BYTES, s>>>(ma, mb, C, ldc, m, n, Kp / tc::BK);
   *err = cudaGetLastError();
   return *err == cudaSuccess;
 }

@@ -52,6 +52,18 @@ __device__ __forceinline__ void better(double v, int i, double& bv, int& bi) {
   if (bi < 0 || v > bv || (v == bv && i < bi)) { bv = v; bi = i; }
 }
 
+__device__ __forceinline__ void warp_best(double& bv, int& bi) {
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_down_sync(0xffffffff, bv, o);
+    int oi = __shfl_down_sync(0xffffffff, bi, o);
+    better(ov, oi, bv, bi);
+  }
+}
+
+// Per column: the elimination of column jj is fused with the local pivot
+// search of column jj+1; warp 0 publishes the CTA's candidate (value, row,
+// full row copy), one grid barrier, then every warp picks the global winner
+// from the published candidates on its own.  Two CTA barriers per column.
 template <typename T>
 __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
   cg::grid_group grid = cg::this_grid();
@@ -60,9 +72,9 @@ __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
   cx<T>* rows = reinterpret_cast<cx<T>*>(smem_raw);  // [R][w+1]
   cx<T>* u = rows + (size_t)a.R * wp;                 // pivot row [w]
   __shared__ double red_v[32];
-  __shared__ int red_i[32], red_c[32];
-  __shared__ int s_best, s_win, s_p;
+  __shared__ int red_i[32];
   const int G = gridDim.x, c = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   const int m0 = a.c0 + c * a.R;
   const int nr = max(0, min(a.R, a.N - m0));
   for (int q = tid; q < nr * w; q += nt) {
@@ -70,114 +82,89 @@ __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
     rows[r * wp + k] = a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld];
   }
   __syncthreads();
-  for (int jj = 0; jj < w; jj++) {
-    const int d = a.c0 + jj, buf = jj & 1;
-    // local pivot candidate
+  {  // candidates of column 0
     double bv = -1.0;
     int bi = -1;
     for (int r = tid; r < nr; r += nt) {
-      int gi = m0 + r;
-      if (gi < d) continue;
-      cx<T> z = rows[r * wp + jj];
-      // LAPACK's IZAMAX measure |Re| + |Im| (dcabs1), evaluated in FP64
-      double v = fabs((double)z.re) + fabs((double)z.im);
-      better(v, gi, bv, bi);
+      cx<T> z = rows[r * wp];
+      better(fabs((double)z.re) + fabs((double)z.im), m0 + r, bv, bi);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      double ov = __shfl_down_sync(0xffffffff, bv, o);
-      int oi = __shfl_down_sync(0xffffffff, bi, o);
-      better(ov, oi, bv, bi);
+    warp_best(bv, bi);
+    if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
+  }
+  __syncthreads();
+  for (int jj = 0; jj < w; jj++) {
+    const int d = a.c0 + jj, buf = jj & 1;
+    if (warp == 0) {
+      double bv = lane < nw ? red_v[lane] : -1.0;
+      int bi = lane < nw ? red_i[lane] : -1;
+      warp_best(bv, bi);
+      bv = __shfl_sync(0xffffffff, bv, 0);
+      bi = __shfl_sync(0xffffffff, bi, 0);
+      if (lane == 0) { a.st.cand_val[buf * G + c] = bv; a.st.cand_idx[buf * G + c] = bi; }
+      if (bi >= 0)
+        for (int k = lane; k < w; k += 32) a.st.cand_rows[((size_t)buf * G + c) * w + k] = rows[(bi - m0) * wp + k];
+    } else if (warp == 1 && d >= m0 && d < m0 + nr) {
+      for (int k = lane; k < w; k += 32) a.st.diag_row[(size_t)buf * w + k] = rows[(d - m0) * wp + k];
     }
-    if ((tid & 31) == 0) { red_v[tid >> 5] = bv; red_i[tid >> 5] = bi; }
-    __syncthreads();
-    if (tid < 32) {
-      bv = tid < (nt >> 5) ? red_v[tid] : -1.0;
-      bi = tid < (nt >> 5) ? red_i[tid] : -1;
-      for (int o = 16; o > 0; o >>= 1) {
-        double ov = __shfl_down_sync(0xffffffff, bv, o);
-        int oi = __shfl_down_sync(0xffffffff, bi, o);
-        better(ov, oi, bv, bi);
-      }
-      if (tid == 0) {
-        s_best = bi;
-        a.st.cand_val[buf * G + c] = bv;
-        a.st.cand_idx[buf * G + c] = bi;
-      }
-    }
-    __syncthreads();
-    const int cb = s_best;
-    if (cb >= 0)
-      for (int k = tid; k < w; k += nt) a.st.cand_rows[((size_t)buf * G + c) * w + k] = rows[(cb - m0) * wp + k];
-    if (d >= m0 && d < m0 + nr)
-      for (int k = tid; k < w; k += nt) a.st.diag_row[(size_t)buf * w + k] = rows[(d - m0) * wp + k];
     __threadfence();
     grid.sync();
-    // global pivot: best over all CTAs' candidates (value, row, CTA carried together)
-    bv = -1.0; bi = -1;
-    int bc = -1;
-    for (int q = tid; q < G; q += nt) {
+    // global winner, computed by every warp (ties: lowest row, like IZAMAX)
+    double gv = -1.0;
+    int gi = -1, gc = -1;
+    for (int q = lane; q < G; q += 32) {
       int i = a.st.cand_idx[buf * G + q];
       double v = a.st.cand_val[buf * G + q];
-      if (i >= 0 && (bi < 0 || v > bv || (v == bv && i < bi))) { bv = v; bi = i; bc = q; }
+      if (i >= 0 && (gi < 0 || v > gv || (v == gv && i < gi))) { gv = v; gi = i; gc = q; }
     }
     for (int o = 16; o > 0; o >>= 1) {
-      double ov = __shfl_down_sync(0xffffffff, bv, o);
-      int oi = __shfl_down_sync(0xffffffff, bi, o);
-      int oc = __shfl_down_sync(0xffffffff, bc, o);
-      if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; bc = oc; }
+      double ov = __shfl_down_sync(0xffffffff, gv, o);
+      int oi = __shfl_down_sync(0xffffffff, gi, o);
+      int oc = __shfl_down_sync(0xffffffff, gc, o);
+      if (oi >= 0 && (gi < 0 || ov > gv || (ov == gv && oi < gi))) { gv = ov; gi = oi; gc = oc; }
     }
-    if ((tid & 31) == 0) { red_v[tid >> 5] = bv; red_i[tid >> 5] = bi; red_c[tid >> 5] = bc; }
-    __syncthreads();
-    if (tid < 32) {
-      bv = tid < (nt >> 5) ? red_v[tid] : -1.0;
-      bi = tid < (nt >> 5) ? red_i[tid] : -1;
-      bc = tid < (nt >> 5) ? red_c[tid] : -1;
-      for (int o = 16; o > 0; o >>= 1) {
-        double ov = __shfl_down_sync(0xffffffff, bv, o);
-        int oi = __shfl_down_sync(0xffffffff, bi, o);
-        int oc = __shfl_down_sync(0xffffffff, bc, o);
-        if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; bc = oc; }
-      }
-      if (tid == 0) {
-        s_win = bc;
-        s_p = bi;
-        if (c == 0) {
-          a.ipiv[d] = bi;
-          if (bv == 0.0 && *a.info == 0) *a.info = d + 1;
-        }
-      }
+    gv = __shfl_sync(0xffffffff, gv, 0);
+    const int p = __shfl_sync(0xffffffff, gi, 0), wc = __shfl_sync(0xffffffff, gc, 0);
+    if (c == 0 && tid == 0) {
+      a.ipiv[d] = p;
+      if (gv == 0.0 && *a.info == 0) *a.info = d + 1;
     }
-    __syncthreads();
-    const int p = s_p, wc = s_win;
-    for (int k = tid; k < w; k += nt) u[k] = a.st.cand_rows[((size_t)buf * G + wc) * w + k];
-    __syncthreads();
-    // row interchange d <-> p inside the panel
-    if (d >= m0 && d < m0 + nr)
-      for (int k = tid; k < w; k += nt) rows[(d - m0) * wp + k] = u[k];
+    const cx<T>* win = a.st.cand_rows + ((size_t)buf * G + wc) * w;
+    for (int k = tid; k < w; k += nt) {
+      cx<T> x = win[k];
+      u[k] = x;
+      if (d >= m0 && d < m0 + nr) rows[(d - m0) * wp + k] = x;
+    }
     if (p != d && p >= m0 && p < m0 + nr)
       for (int k = tid; k < w; k += nt) rows[(p - m0) * wp + k] = a.st.diag_row[(size_t)buf * w + k];
     __syncthreads();
-    // multipliers and rank-1 update of the rows below d
-    cx<T> piv = u[jj];
-    T pn = piv.re * piv.re + piv.im * piv.im;
-    if (pn != (T)0) {
-      // thread = (row, column group): the multiplier stays in a register and
-      // the row's remaining columns are strided over the groups
-      const cx<T> inv = mk(piv.re / pn, -piv.im / pn);
-      const int rs = max(0, d + 1 - m0);
-      const int RT = 128, CGN = nt / RT;
-      const int rr = tid % RT, cgi = tid / RT;
-      for (int rb = rs; rb < nr; rb += RT) {
-        const int r = rb + rr;
-        cx<T> l = mk((T)0, (T)0);
-        if (r < nr) l = rows[r * wp + jj] * inv;
-        __syncthreads();
-        if (r < nr) {
+    // eliminate column jj (4 adjacent lanes per row) and search column jj+1
+    const cx<T> piv = u[jj];
+    const T pn = piv.re * piv.re + piv.im * piv.im;
+    const cx<T> inv = pn != (T)0 ? mk(piv.re / pn, -piv.im / pn) : mk((T)0, (T)0);
+    const int rs = max(0, d + 1 - m0);
+    const int cgi = tid & 3, RT = nt >> 2;
+    double bv = -1.0;
+    int bi = -1;
+    for (int rb = rs; rb < nr; rb += RT) {
+      const int r = rb + (tid >> 2);
+      const bool valid = r < nr;
+      cx<T> l = mk((T)0, (T)0);
+      if (valid && pn != (T)0) l = rows[r * wp + jj] * inv;
+      __syncwarp();
+      if (valid) {
+        if (pn != (T)0) {
           if (cgi == 0) rows[r * wp + jj] = l;
-          for (int k = jj + 1 + cgi; k < w; k += CGN) rows[r * wp + k] = rows[r * wp + k] - l * u[k];
+          for (int k = jj + 1 + cgi; k < w; k += 4) rows[r * wp + k] = rows[r * wp + k] - l * u[k];
+        }
+        if (cgi == 0 && jj + 1 < w) {
+          cx<T> z = rows[r * wp + jj + 1];
+          better(fabs((double)z.re) + fabs((double)z.im), m0 + r, bv, bi);
         }
       }
     }
+    warp_best(bv, bi);
+    if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
     __syncthreads();
   }
   for (int q = tid; q < nr * w; q += nt) {
