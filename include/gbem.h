@@ -126,6 +126,25 @@ gbem_status gbem_lu_factor(gbem_matrix *M, int *ipiv, int *info);
  * trans is 'N' or 'T'. */
 gbem_status gbem_lu_solve(gbem_matrix *M, char trans, int nrhs, void *B, int ldb);
 
+/* gbem_lu_solve without any device allocation.  No counterpart in the
+ * reference (HMatrix::LUSolve runs LAPACK on host memory).  Same arguments
+ * and results as gbem_lu_solve.  It serves callers that cannot allocate GPU
+ * memory at solve time: a process whose HBM is already taken by its
+ * matrices or held by another allocator's pool (a PyTorch caching allocator,
+ * say), where a cudaMalloc/cudaMallocAsync inside the solve would fail.
+ * Its workspace is one 16 MiB device array of the library, reserved when the
+ * library's LU code first loads on a device, so N is limited: N <= 13088
+ * for a complex128 matrix, N <= 14528 for complex64; larger N returns
+ * GBEM_EINVAL with the limit in gbem_last_error().  The first call on each
+ * device looks up that array's device address (with the device current);
+ * make that first call before any stream capture begins.  Every call on a
+ * device shares the one array and leaves its last contents there; nothing
+ * in it has to start at zero, since each call writes every scratch byte
+ * before reading it.  Calls that overlap in time on one device (other host
+ * threads, other matrices) race on the array and must be serialised by the
+ * caller; each call synchronises the matrix's stream before returning. */
+gbem_status gbem_lu_solve_noalloc(gbem_matrix *M, char trans, int nrhs, void *B, int ldb);
+
 /* Host-buffer drop-in for LUFactorize on a whole HMatrix: factors the host
  * column-major C128 array ZM (N x N, ld) in place and writes 1-based ipiv. */
 gbem_status gbem_lu_factor_host(double *ZM, int N, int ld, int *ipiv, int *info);

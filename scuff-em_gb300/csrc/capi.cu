@@ -303,6 +303,18 @@ gbem_status gbem_lu_solve(gbem_matrix* M, char trans, int nrhs, void* B, int ldb
   return st;
 }
 
+gbem_status gbem_lu_solve_noalloc(gbem_matrix* M, char trans, int nrhs, void* B, int ldb) {
+  if (!M || !B || nrhs <= 0 || ldb < M->N) { set_error("gbem_lu_solve_noalloc: bad arguments"); return GBEM_EINVAL; }
+  CHECK_CUDA(cudaSetDevice(M->g->device), "cudaSetDevice");
+  if (M->N > lu_solve_noalloc_max_n(M->dtype)) {
+    set_error("gbem_lu_solve_noalloc: N = %d exceeds the static scratch (N <= %d for this dtype)", M->N,
+              lu_solve_noalloc_max_n(M->dtype));
+    return GBEM_EINVAL;
+  }
+  if (!M->factored) { set_error("gbem_lu_solve_noalloc: matrix is not factored"); return GBEM_EINVAL; }
+  return lu_solve_static_scratch(M->d, M->N, M->ld, M->dtype, M->d_perm, trans, nrhs, B, ldb, M->stream);
+}
+
 gbem_status gbem_lu_factor_host(double* ZM, int N, int ld, int* ipiv, int* info) {
   if (!ZM || N <= 0 || ld < N) { set_error("gbem_lu_factor_host: bad arguments"); return GBEM_EINVAL; }
   cudaStream_t s;

@@ -114,6 +114,11 @@ gbem_status lu_solve_device(const void* dA, int N, int ld, int dtype, const int*
                             void* dB, int ldb, void* dY, cudaStream_t s);
 gbem_status residual_device(const void* dA, int lda, int dtype, int N, const double* dX, int ldx, const double* dB,
                             int ldb, int nrhs, double* dR, int ldr, void* part, cudaStream_t s);
+// LU solve on a host B whose device workspace is a static array of lu.cu
+// (no device allocation); the caller makes the matrix's device current
+gbem_status lu_solve_static_scratch(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs,
+                                    void* hB, int ldb, cudaStream_t s);
+int lu_solve_noalloc_max_n(int dtype);
 
 // per-stage device timing and launch counts (process-wide; see gbem_stats)
 enum Stage { ST_FAR = 0, ST_NEAR = 1, ST_PANEL = 2, ST_GEMM = 3, ST_SOLVE = 4, ST_RESID = 5, ST_OTHER = 6, ST_N = 8 };

@@ -17,6 +17,7 @@
 #include <cooperative_groups.h>
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <vector>
 #include "bem_math.cuh"
 #include "gbem_internal.h"
@@ -705,6 +706,138 @@ gbem_status residual_device(const void* dA, int lda, int dtype, int N, const dou
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "residual");
   }
   return GBEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// LU solve that allocates no device memory: its workspace is a file-scope
+// device array reserved when this module loads on a device.  Every call on a
+// device shares that device's array and leaves its last contents there;
+// nothing in it has to start at zero, because each call writes every scratch
+// byte before reading it.  Calls that overlap in time on one device race on
+// the array; the call synchronises the matrix's stream before it returns.
+// ---------------------------------------------------------------------------
+static constexpr size_t kSolveScratchBytes = (size_t)16 << 20;
+static __device__ __align__(256) unsigned char g_solve_scratch[kSolveScratchBytes];
+static constexpr int kMaxDevices = 64;
+static void* g_solve_scratch_ptr[kMaxDevices];  // device address per ordinal, set on first use
+static std::mutex g_solve_scratch_mu;
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// bytes of scratch one chunk of <= 8 right-hand sides needs: the chunk's
+// columns, the permuted copy Y, and the inverses of the diagonal blocks
+static size_t solve_scratch_need(int N, int dtype) {
+  const size_t es = dtype == GBEM_C64 ? 8 : 16;
+  const size_t bs = dtype == GBEM_C64 ? 64 : 32;
+  const size_t nb = ((size_t)N + bs - 1) / bs;
+  return 2 * align256((size_t)N * 8 * es) + align256(2 * nb * bs * bs * es);
+}
+
+// one chunk (nr <= 8 columns) of A X = B, 'N' form, with caller-provided Y and
+// Dinv; the same kernels and launch shapes as solve_impl
+template <typename T>
+static gbem_status solve_chunk_n(const cx<T>* A, int N, int ld, const int* d_perm, int nr, cx<T>* Bc, int ldb, cx<T>* Y,
+                                 cx<T>* Dinv, cudaStream_t s) {
+  const int bs = sizeof(T) == 4 ? 64 : 32;
+  const int nb = (N + bs - 1) / bs;
+  cudaError_t e;
+  gather_rows<T><<<(N + 255) / 256, 256, 0, s>>>(Bc, ldb, Y, N, d_perm, N, nr);
+  cx<T>* DinvU = Dinv + (size_t)nb * bs * bs;
+  size_t ism = sizeof(cx<T>) * 2 * bs * (bs + 1);
+  cudaFuncSetAttribute(diag_inverse<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+  cudaFuncSetAttribute(diag_inverse<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+  diag_inverse<T, true><<<nb, 256, ism, s>>>(A, ld, N, bs, Dinv);
+  diag_inverse<T, false><<<nb, 256, ism, s>>>(A, ld, N, bs, DinvU);
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  size_t dsm = sizeof(cx<T>) * bs * bs;
+  cudaFuncSetAttribute(trsv_coop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+  cudaFuncSetAttribute(trsv_coop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, dsm);
+  int G = std::max(1, std::min(nsm * std::max(per, 1), std::min(nsm, (4 * N + 255) / 256)));
+  int Nn = N, bsn = bs, nrn = nr;
+  const cx<T>* Ac = A;
+  long long ldl = ld;
+  void* argsL[] = {(void*)&Ac, (void*)&ldl, (void*)&Nn, (void*)&bsn, (void*)&Dinv, (void*)&Y, (void*)&nrn};
+  e = cudaLaunchCooperativeKernel((void*)trsv_coop<T, true>, dim3(G), dim3(256), argsL, dsm, s);
+  if (e != cudaSuccess) return cuda_status(e, "trsv lower");
+  void* argsU[] = {(void*)&Ac, (void*)&ldl, (void*)&Nn, (void*)&bsn, (void*)&DinvU, (void*)&Y, (void*)&nrn};
+  e = cudaLaunchCooperativeKernel((void*)trsv_coop<T, false>, dim3(G), dim3(256), argsU, dsm, s);
+  if (e != cudaSuccess) return cuda_status(e, "trsv upper");
+  stats_launch(ST_SOLVE, 5);
+  e = cudaMemcpy2DAsync(Bc, (size_t)ldb * sizeof(cx<T>), Y, (size_t)N * sizeof(cx<T>), (size_t)N * sizeof(cx<T>), nr,
+                        cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_status(e, "solve copy");
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "solve");
+  return GBEM_OK;
+}
+
+template <typename T>
+static gbem_status solve_static_impl(const cx<T>* A, int N, int ld, const int* d_perm, char trans, int nrhs, cx<T>* hB,
+                                     int ldb, unsigned char* scratch, cudaStream_t s) {
+  const size_t es = sizeof(cx<T>);
+  cx<T>* Bd = (cx<T>*)scratch;
+  cx<T>* Y = (cx<T>*)(scratch + align256((size_t)N * 8 * es));
+  cx<T>* Dinv = (cx<T>*)(scratch + 2 * align256((size_t)N * 8 * es));
+  for (int r0 = 0; r0 < nrhs; r0 += 8) {
+    const int nr = std::min(8, nrhs - r0);
+    cx<T>* hc = hB + (long long)r0 * ldb;
+    cudaError_t e = cudaMemcpy2DAsync(Bd, (size_t)N * es, hc, (size_t)ldb * es, (size_t)N * es, nr,
+                                      cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_status(e, "solve upload");
+    gbem_status st = trans == 'N' ? solve_chunk_n<T>(A, N, ld, d_perm, nr, Bd, N, Y, Dinv, s)
+                                  : solve_impl<T>(A, N, ld, d_perm, 'T', nr, Bd, N, Y, s);  // the 'T' form allocates nothing
+    if (st != GBEM_OK) return st;
+    e = cudaMemcpy2DAsync(hc, (size_t)ldb * es, Bd, (size_t)N * es, (size_t)N * es, nr, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "solve download");
+  }
+  return GBEM_OK;
+}
+
+gbem_status lu_solve_static_scratch(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs,
+                                    void* hB, int ldb, cudaStream_t s) {
+  if (trans != 'N' && trans != 'T') { set_error("gbem_lu_solve_noalloc: trans must be 'N' or 'T'"); return GBEM_EINVAL; }
+  if (dtype != GBEM_C128 && dtype != GBEM_C64) { set_error("gbem_lu_solve_noalloc: dtype must be C128 or C64"); return GBEM_EINVAL; }
+  const size_t need = solve_scratch_need(N, dtype);
+  if (need > kSolveScratchBytes) {
+    set_error("gbem_lu_solve_noalloc: N = %d needs %zu bytes of scratch; the static scratch holds %zu bytes "
+              "(N <= %d for complex128, N <= %d for complex64)",
+              N, need, kSolveScratchBytes, lu_solve_noalloc_max_n(GBEM_C128), lu_solve_noalloc_max_n(GBEM_C64));
+    return GBEM_EINVAL;
+  }
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) { set_error("gbem_lu_solve_noalloc: device ordinal %d out of range", dev); return GBEM_EINVAL; }
+  void* scratch = nullptr;
+  {
+    // first call on this device (with it current): look up the array's address
+    std::lock_guard<std::mutex> l(g_solve_scratch_mu);
+    if (!g_solve_scratch_ptr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress((void**)&p, g_solve_scratch);
+      if (e != cudaSuccess) return cuda_status(e, "gbem_lu_solve_noalloc: cudaGetSymbolAddress of the scratch array");
+      g_solve_scratch_ptr[dev] = p;
+    }
+    scratch = g_solve_scratch_ptr[dev];
+  }
+  if (dtype == GBEM_C128)
+    return solve_static_impl<double>((const cx<double>*)dA, N, ld, d_perm, trans, nrhs, (cx<double>*)hB, ldb,
+                                     (unsigned char*)scratch, s);
+  return solve_static_impl<float>((const cx<float>*)dA, N, ld, d_perm, trans, nrhs, (cx<float>*)hB, ldb,
+                                  (unsigned char*)scratch, s);
+}
+
+// largest N whose solve fits the static scratch
+int lu_solve_noalloc_max_n(int dtype) {
+  int lo = 0, hi = 1 << 24;
+  while (lo < hi) {
+    int mid = lo + (hi - lo + 1) / 2;
+    if (solve_scratch_need(mid, dtype) <= kSolveScratchBytes) lo = mid; else hi = mid - 1;
+  }
+  return lo;
 }
 
 }  // namespace gbem
