@@ -676,6 +676,76 @@ __global__ void __launch_bounds__(128) residual_partial(const cx<TA>* A, long lo
     for (int r = 0; r < nrhs; r++) part[((size_t)blockIdx.y * nrhs + r) * N + i] = acc[r];
 }
 
+// Double-float residual for a complex-FP32 matrix: every product A_ij * x_j
+// with x_j = xh + xl (two FP32 pieces of the FP64 value) is formed as an
+// exact FP32 pair (p, fma(a, xh, -p)) plus the small term a * xl, and summed
+// with Knuth's two-sum into a (hi, lo) FP32 accumulator; every 64 columns the
+// pair is folded into an FP64 partial sum.  The rounding left is ~64 * 2^-48
+// of the partial sums, far below the refinement tolerance, at FP32 rates.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
+  float s = __fadd_rn(hi, p);
+  float bb = __fadd_rn(s, -hi);
+  float err = __fadd_rn(__fadd_rn(hi, -__fadd_rn(s, -bb)), __fadd_rn(p, -bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
+template <int NR>
+__global__ void __launch_bounds__(128) residual_partial_df(const cx<float>* A, long long lda, const cx<double>* X,
+                                                           long long ldx, int N, int cchunk, cx<double>* part) {
+  __shared__ float4 xs[64][NR];  // (re_hi, re_lo, im_hi, im_lo)
+  const int i = blockIdx.x * 128 + threadIdx.x;
+  const int c0 = blockIdx.y * cchunk, c1 = min(N, c0 + cchunk);
+  double accr[NR], acci[NR];
+  for (int r = 0; r < NR; r++) accr[r] = acci[r] = 0.0;
+  const cx<float>* Ai = A + (i < N ? i : 0);
+  for (int j0 = c0; j0 < c1; j0 += 64) {
+    const int nj = min(64, c1 - j0);
+    __syncthreads();
+    for (int q = threadIdx.x; q < nj * NR; q += 128) {
+      int j = q % nj, r = q / nj;
+      cx<double> x = X[(j0 + j) + (long long)r * ldx];
+      float rh = (float)x.re, ih = (float)x.im;
+      xs[j][r] = make_float4(rh, (float)(x.re - (double)rh), ih, (float)(x.im - (double)ih));
+    }
+    __syncthreads();
+    float hr[NR], lr[NR], hi_[NR], li[NR];
+    for (int r = 0; r < NR; r++) hr[r] = lr[r] = hi_[r] = li[r] = 0.f;
+    if (i < N) {
+#pragma unroll 4
+      for (int j = 0; j < nj; j++) {
+        const cx<float> a = Ai[(long long)(j0 + j) * lda];
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+          const float4 x = xs[j][r];
+          // real part: a.re*xr - a.im*xi
+          float p1 = __fmul_rn(a.re, x.x), e1 = __fmaf_rn(a.re, x.x, -p1);
+          float p2 = __fmul_rn(-a.im, x.z), e2 = __fmaf_rn(-a.im, x.z, -p2);
+          two_sum_acc(hr[r], lr[r], p1);
+          two_sum_acc(hr[r], lr[r], p2);
+          lr[r] = __fadd_rn(lr[r], __fadd_rn(e1, e2));
+          lr[r] = __fmaf_rn(a.re, x.y, lr[r]);
+          lr[r] = __fmaf_rn(-a.im, x.w, lr[r]);
+          // imaginary part: a.re*xi + a.im*xr
+          float p3 = __fmul_rn(a.re, x.z), e3 = __fmaf_rn(a.re, x.z, -p3);
+          float p4 = __fmul_rn(a.im, x.x), e4 = __fmaf_rn(a.im, x.x, -p4);
+          two_sum_acc(hi_[r], li[r], p3);
+          two_sum_acc(hi_[r], li[r], p4);
+          li[r] = __fadd_rn(li[r], __fadd_rn(e3, e4));
+          li[r] = __fmaf_rn(a.re, x.w, li[r]);
+          li[r] = __fmaf_rn(a.im, x.y, li[r]);
+        }
+      }
+    }
+    for (int r = 0; r < NR; r++) {
+      accr[r] += (double)hr[r] + (double)lr[r];
+      acci[r] += (double)hi_[r] + (double)li[r];
+    }
+  }
+  if (i < N)
+    for (int r = 0; r < NR; r++) part[((size_t)blockIdx.y * NR + r) * N + i] = mk(accr[r], acci[r]);
+}
+
 __global__ void residual_finish(const cx<double>* B, long long ldb, const cx<double>* part, int nsplit, int N, int nrhs,
                                 cx<double>* R, long long ldr) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -696,9 +766,20 @@ gbem_status residual_device(const void* dA, int lda, int dtype, int N, const dou
     int nr = std::min(8, nrhs - r0);
     dim3 grid((N + 127) / 128, nsplit);
     const cx<double>* X = (const cx<double>*)dX + (long long)r0 * ldx;
-    if (dtype == GBEM_C64)
-      residual_partial<float><<<grid, 128, 0, s>>>((const cx<float>*)dA, lda, X, ldx, N, nr, cchunk, (cx<double>*)part);
-    else
+    if (dtype == GBEM_C64) {
+      const cx<float>* Af = (const cx<float>*)dA;
+      cx<double>* P = (cx<double>*)part;
+      switch (nr) {
+        case 1: residual_partial_df<1><<<grid, 128, 0, s>>>(Af, lda, X, ldx, N, cchunk, P); break;
+        case 2: residual_partial_df<2><<<grid, 128, 0, s>>>(Af, lda, X, ldx, N, cchunk, P); break;
+        case 3: residual_partial_df<3><<<grid, 128, 0, s>>>(Af, lda, X, ldx, N, cchunk, P); break;
+        case 4: residual_partial_df<4><<<grid, 128, 0, s>>>(Af, lda, X, ldx, N, cchunk, P); break;
+        case 5: residual_partial_df<5><<<grid, 128, 0, s>>>(Af, lda, X, ldx, N, cchunk, P); break;
+        case 6: residual_partial_df<6><<<grid, 128, 0, s>>>(Af, lda, X, ldx, N, cchunk, P); break;
+        case 7: residual_partial_df<7><<<grid, 128, 0, s>>>(Af, lda, X, ldx, N, cchunk, P); break;
+        default: residual_partial_df<8><<<grid, 128, 0, s>>>(Af, lda, X, ldx, N, cchunk, P); break;
+      }
+    } else
       residual_partial<double><<<grid, 128, 0, s>>>((const cx<double>*)dA, lda, X, ldx, N, nr, cchunk, (cx<double>*)part);
     stats_launch(ST_RESID, 2);
     residual_finish<<<(N + 255) / 256, 256, 0, s>>>((const cx<double>*)dB + (long long)r0 * ldb, ldb, (cx<double>*)part,
