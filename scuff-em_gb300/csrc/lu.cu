@@ -32,11 +32,17 @@ bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long l
 size_t tc_gemm_ws_bytes(int m, int n, int k);
 int tc_gemm_error(bool reset);
 
+// one CTA's pivot candidate: |Re|+|Im| (FP64) and its global row, written
+// and read as one 16-byte record
+struct __align__(16) Cand {
+  double v;
+  int i, pad;
+};
+
 template <typename T> struct Stash {
   cx<T>* cand_rows;  // [2][G][w]
   cx<T>* diag_row;   // [2][w]
-  double* cand_val;  // [2][G]
-  int* cand_idx;     // [2][G]
+  Cand* cand;        // [2][G]
 };
 
 template <typename T> struct PanelArgs {
@@ -47,6 +53,28 @@ template <typename T> struct PanelArgs {
   int* info;   // first zero pivot (1-based), 0 if none
   Stash<T> st;
 };
+
+// row stride of the shared-memory panel: w + 4 elements makes the 4 lanes
+// x 8 rows of a warp's elimination step hit distinct banks
+__host__ __device__ constexpr int panel_stride(int w) { return w + 4; }
+
+// L2-coherent loads (bypass L1) of data other CTAs wrote before a grid barrier
+__device__ __forceinline__ cx<float> ldcg_cx(const cx<float>* p) {
+  float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+  return mk(v.x, v.y);
+}
+__device__ __forceinline__ cx<double> ldcg_cx(const cx<double>* p) {
+  double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+  return mk(v.x, v.y);
+}
+__device__ __forceinline__ Cand ldcg_cand(const Cand* p) {
+  int4 r = __ldcg(reinterpret_cast<const int4*>(p));
+  Cand c;
+  c.v = __hiloint2double(r.y, r.x);
+  c.i = r.z;
+  c.pad = r.w;
+  return c;
+}
 
 __device__ __forceinline__ void better(double v, int i, double& bv, int& bi) {
   if (i < 0) return;
@@ -62,18 +90,22 @@ __device__ __forceinline__ void warp_best(double& bv, int& bi) {
 }
 
 // Per column: the elimination of column jj is fused with the local pivot
-// search of column jj+1; warp 0 publishes the CTA's candidate (value, row,
-// full row copy), one grid barrier, then every warp picks the global winner
-// from the published candidates on its own.  Two CTA barriers per column.
+// search of column jj+1; warp 0 publishes the CTA's candidate record and its
+// row, warp 1 the diagonal row; one grid barrier; warp 0 reads all records
+// (one 16-byte load per lane and CTA slot, issued together), picks the global
+// winner and broadcasts it through shared memory.  The CTA's rows are spread
+// over 4 adjacent lanes per row during elimination.
 template <typename T>
 __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
   cg::grid_group grid = cg::this_grid();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int w = a.w, wp = a.w + 1;
-  cx<T>* rows = reinterpret_cast<cx<T>*>(smem_raw);  // [R][w+1]
+  const int w = a.w, wp = panel_stride(a.w);
+  cx<T>* rows = reinterpret_cast<cx<T>*>(smem_raw);  // [R][wp]
   cx<T>* u = rows + (size_t)a.R * wp;                 // pivot row [w]
   __shared__ double red_v[32];
   __shared__ int red_i[32];
+  __shared__ double s_gv;
+  __shared__ int s_p, s_wc;
   const int G = gridDim.x, c = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   const int m0 = a.c0 + c * a.R;
@@ -102,42 +134,62 @@ __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
       warp_best(bv, bi);
       bv = __shfl_sync(0xffffffff, bv, 0);
       bi = __shfl_sync(0xffffffff, bi, 0);
-      if (lane == 0) { a.st.cand_val[buf * G + c] = bv; a.st.cand_idx[buf * G + c] = bi; }
+      if (lane == 0) {
+        Cand cd;
+        cd.v = bv; cd.i = bi; cd.pad = 0;
+        a.st.cand[buf * G + c] = cd;
+      }
       if (bi >= 0)
         for (int k = lane; k < w; k += 32) a.st.cand_rows[((size_t)buf * G + c) * w + k] = rows[(bi - m0) * wp + k];
+      __threadfence();
     } else if (warp == 1 && d >= m0 && d < m0 + nr) {
       for (int k = lane; k < w; k += 32) a.st.diag_row[(size_t)buf * w + k] = rows[(d - m0) * wp + k];
+      __threadfence();
     }
-    __threadfence();
     grid.sync();
-    // global winner, computed by every warp (ties: lowest row, like IZAMAX)
-    double gv = -1.0;
-    int gi = -1, gc = -1;
-    for (int q = lane; q < G; q += 32) {
-      int i = a.st.cand_idx[buf * G + q];
-      double v = a.st.cand_val[buf * G + q];
-      if (i >= 0 && (gi < 0 || v > gv || (v == gv && i < gi))) { gv = v; gi = i; gc = q; }
+    if (warp == 0) {
+      // global winner (ties: lowest row, like IZAMAX); the record loads are
+      // independent of one another, so they are all in flight at once
+      constexpr int MAXT = 8;  // G <= 256
+      Cand rec[MAXT];
+#pragma unroll
+      for (int t = 0; t < MAXT; t++) {
+        const int q = lane + 32 * t;
+        if (q < G) rec[t] = ldcg_cand(&a.st.cand[buf * G + q]);
+        else { rec[t].v = -1.0; rec[t].i = -1; rec[t].pad = 0; }
+      }
+      double gv = -1.0;
+      int gi = -1, gc = -1;
+#pragma unroll
+      for (int t = 0; t < MAXT; t++) {
+        const int i = rec[t].i;
+        const double v = rec[t].v;
+        if (i >= 0 && (gi < 0 || v > gv || (v == gv && i < gi))) { gv = v; gi = i; gc = lane + 32 * t; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_down_sync(0xffffffff, gv, o);
+        int oi = __shfl_down_sync(0xffffffff, gi, o);
+        int oc = __shfl_down_sync(0xffffffff, gc, o);
+        if (oi >= 0 && (gi < 0 || ov > gv || (ov == gv && oi < gi))) { gv = ov; gi = oi; gc = oc; }
+      }
+      if (lane == 0) {
+        s_gv = gv; s_p = gi; s_wc = gc;
+        if (c == 0) {
+          a.ipiv[d] = gi;
+          if (gv == 0.0 && *a.info == 0) *a.info = d + 1;
+        }
+      }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      double ov = __shfl_down_sync(0xffffffff, gv, o);
-      int oi = __shfl_down_sync(0xffffffff, gi, o);
-      int oc = __shfl_down_sync(0xffffffff, gc, o);
-      if (oi >= 0 && (gi < 0 || ov > gv || (ov == gv && oi < gi))) { gv = ov; gi = oi; gc = oc; }
-    }
-    gv = __shfl_sync(0xffffffff, gv, 0);
-    const int p = __shfl_sync(0xffffffff, gi, 0), wc = __shfl_sync(0xffffffff, gc, 0);
-    if (c == 0 && tid == 0) {
-      a.ipiv[d] = p;
-      if (gv == 0.0 && *a.info == 0) *a.info = d + 1;
-    }
+    __syncthreads();
+    const int p = s_p, wc = s_wc;
     const cx<T>* win = a.st.cand_rows + ((size_t)buf * G + wc) * w;
     for (int k = tid; k < w; k += nt) {
-      cx<T> x = win[k];
+      cx<T> x = ldcg_cx(win + k);
       u[k] = x;
       if (d >= m0 && d < m0 + nr) rows[(d - m0) * wp + k] = x;
     }
     if (p != d && p >= m0 && p < m0 + nr)
-      for (int k = tid; k < w; k += nt) rows[(p - m0) * wp + k] = a.st.diag_row[(size_t)buf * w + k];
+      for (int k = tid; k < w; k += nt) rows[(p - m0) * wp + k] = ldcg_cx(a.st.diag_row + (size_t)buf * w + k);
     __syncthreads();
     // eliminate column jj (4 adjacent lanes per row) and search column jj+1
     const cx<T> piv = u[jj];
@@ -295,11 +347,11 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   int R = 0;
   for (;; w /= 2) {
     R = (N + nsm - 1) / nsm;
-    if ((size_t)(R * (w + 1) + w) * esz <= smem_cap || w <= 8) break;
+    if ((size_t)(R * panel_stride(w) + w) * esz <= smem_cap || w <= 8) break;
   }
   if (w > N) w = std::max(1, N);
   R = std::max(R, 1);
-  size_t smem = (size_t)(R * (w + 1) + w) * esz;
+  size_t smem = (size_t)(R * panel_stride(w) + w) * esz;
   cudaError_t e = cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "panel smem");
   int maxb = 0;
@@ -307,7 +359,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   if (e != cudaSuccess || maxb < 1) return cuda_status(e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "panel occupancy");
   // workspace: stash + info + tensor-core scratch
   const int Gmax = nsm * maxb;
-  size_t need = (size_t)2 * Gmax * w * esz + 2 * (size_t)w * esz + 2 * Gmax * (sizeof(double) + sizeof(int)) + 256;
+  size_t need = (size_t)2 * Gmax * w * esz + 2 * (size_t)w * esz + 2 * Gmax * sizeof(Cand) + 256;
   size_t tcb = 0;
   if (sizeof(T) == 4) tcb = tc_gemm_ws_bytes(N, N, w);
   size_t total = need + tcb + 1024;
@@ -323,8 +375,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   Stash<T> st;
   st.cand_rows = (cx<T>*)wp; wp += (size_t)2 * Gmax * w * esz;
   st.diag_row = (cx<T>*)wp; wp += (size_t)2 * w * esz;
-  st.cand_val = (double*)wp; wp += 2 * Gmax * sizeof(double);
-  st.cand_idx = (int*)wp; wp += 2 * Gmax * sizeof(int);
+  st.cand = (Cand*)(((uintptr_t)wp + 15) & ~(uintptr_t)15); wp = (unsigned char*)(st.cand + 2 * Gmax);
   int* d_info = (int*)(((uintptr_t)wp + 15) & ~(uintptr_t)15); wp = (unsigned char*)(d_info + 4);
   void* tcws = (void*)(((uintptr_t)wp + 1023) & ~(uintptr_t)1023);
   e = cudaMemsetAsync(d_info, 0, sizeof(int), s);
@@ -333,10 +384,11 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     const int wc = std::min(w, N - c0);
     const int m = N - c0;
     int G = std::min(Gmax, (m + R - 1) / R);
+    if (G > 256) { set_error("LU panel: %d CTAs exceed the 256 candidate slots", G); return GBEM_ENOTSUP; }
     PanelArgs<T> pa;
     pa.A = A; pa.ld = ld; pa.N = N; pa.c0 = c0; pa.w = wc; pa.R = (m + G - 1) / G;
     pa.ipiv = d_ipiv; pa.info = d_info; pa.st = st;
-    size_t sm = (size_t)(pa.R * (wc + 1) + wc) * esz;
+    size_t sm = (size_t)(pa.R * panel_stride(wc) + wc) * esz;
     void* args[] = {&pa};
     {
       StatTimer tp(ST_PANEL, s);
@@ -500,74 +552,131 @@ __global__ void __launch_bounds__(256) diag_inverse(const cx<T>* A, long long ld
   }
 }
 
-// Blocked triangular solve in one cooperative launch: for each block k in
-// order, CTA 0 forms x_k = Dinv_k r_k, then every CTA subtracts
-// A[rows, block k] x_k from its share of the remaining rows.  Two grid
-// barriers per block; no per-block kernel launches.
+// Blocked triangular solve in one cooperative launch, one grid barrier per
+// block.  Step s applies x_k (k = the s-th block in solve order) to the rows
+// still unsolved: CTA 0 takes the rows of the next block k1 and at once solves
+// that block from shared memory (x_k1 = Dinv_k1 (y_k1 - A(k1, k) x_k)), while
+// the other CTAs update every row beyond k1.  Before the barrier CTA 0 stages
+// the next step's Dinv block and A(k2 rows, k1 columns) in shared memory.
+// Dynamic shared memory: 2 * bs * bs elements (bs <= 64, nrhs <= 8).
 template <typename T, bool LOWER>
 __global__ void __launch_bounds__(256) trsv_coop(const cx<T>* A, long long lda, int N, int bs, const cx<T>* Dinv,
                                                   cx<T>* Y, int nrhs) {
   cg::grid_group grid = cg::this_grid();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<T>* D = reinterpret_cast<cx<T>*>(smem_raw);  // staged Dinv block, bs x bs
-  __shared__ cx<T> xk[64][8];
+  cx<T>* D = reinterpret_cast<cx<T>*>(smem_raw);  // Dinv of the block CTA 0 solves next, bs x bs column-major
+  cx<T>* Ab = D + bs * bs;                          // A(rows of that block, columns of the current one)
+  __shared__ cx<T> xs[64][8];                       // x of the block CTA 0 solved last
   __shared__ cx<T> rk[64][8];
+  __shared__ cx<T> xk[64][8];                       // x_k for the general update
   const int nb = (N + bs - 1) / bs;
-  const int gthreads = gridDim.x * blockDim.x;
-  for (int s = 0; s < nb; s++) {
-    const int kb = LOWER ? s : nb - 1 - s;
-    const int i0 = kb * bs, n = min(bs, N - i0);
-    if (blockIdx.x == 0) {
-      // stage the block inverse and the block's right-hand sides (independent loads)
-      const cx<T>* Dg = Dinv + (size_t)kb * bs * bs;
-      for (int q = threadIdx.x; q < bs * bs; q += blockDim.x) D[q] = Dg[q];
-      for (int q = threadIdx.x; q < n * nrhs; q += blockDim.x) rk[q % n][q / n] = Y[i0 + q % n + (long long)(q / n) * N];
-      __syncthreads();
-      for (int q = threadIdx.x; q < n * nrhs; q += blockDim.x) {
-        int r = q % n, c = q / n;
-        cx<T> acc = mk((T)0, (T)0);
-        for (int k = 0; k < n; k++) acc = acc + D[r + k * bs] * rk[k][c];
-        Y[i0 + r + (long long)c * N] = acc;
+  const int tid = threadIdx.x, nt = blockDim.x, G = gridDim.x;
+  const cx<T> zero = mk((T)0, (T)0);
+  auto kb_of = [&](int s) { return LOWER ? s : nb - 1 - s; };
+  auto n_of = [&](int k) { return min(bs, N - k * bs); };
+  // CTA 0: D <- Dinv[kd], Ab <- A(rows of block kr, columns of block kc); loads batched 8 deep
+  auto stage = [&](int kd, int kr, int kc) {
+    const cx<T>* Dg = Dinv + (size_t)kd * bs * bs;
+    const int nr_ = n_of(kr), nc_ = n_of(kc), r0_ = kr * bs, c0_ = kc * bs, bb = bs * bs;
+    for (int q0 = 0; q0 < bb; q0 += nt * 8) {
+      cx<T> v[8], u[8];
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int q = q0 + t * nt + tid, r = q % bs, cc = q / bs;
+        v[t] = q < bb ? Dg[q] : zero;
+        u[t] = (q < bb && r < nr_ && cc < nc_) ? A[(r0_ + r) + (long long)(c0_ + cc) * lda] : zero;
+      }
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int q = q0 + t * nt + tid;
+        if (q < bb) { D[q] = v[t]; Ab[q] = u[t]; }
       }
     }
+  };
+  if (blockIdx.x == 0) {
+    // first block: x = Dinv y
+    const int k = kb_of(0), i0 = k * bs, n = n_of(k);
+    stage(k, k, k);
+    for (int q = tid; q < n * nrhs; q += nt) rk[q % n][q / n] = ldcg_cx(Y + i0 + q % n + (long long)(q / n) * N);
+    __syncthreads();
+    for (int q = tid; q < n * nrhs; q += nt) {
+      const int r = q % n, c = q / n;
+      cx<T> acc = zero;
+      for (int kk = 0; kk < n; kk++) acc = acc + D[r + kk * bs] * rk[kk][c];
+      Y[i0 + r + (long long)c * N] = acc;
+      xs[r][c] = acc;
+    }
+    __syncthreads();
+    if (nb > 1) stage(kb_of(1), kb_of(1), k);
     __threadfence();
-    grid.sync();
-    // update the rows still to be solved: 4 threads per row split the block's columns
-    const int r0 = LOWER ? i0 + n : 0, r1 = LOWER ? N : i0;
-    if (r1 > r0) {
-      for (int q = threadIdx.x; q < n * nrhs; q += blockDim.x) xk[q % n][q / n] = Y[i0 + q % n + (long long)(q / n) * N];
+  }
+  grid.sync();
+  for (int s = 0; s + 1 < nb; s++) {
+    const int k = kb_of(s), k1 = kb_of(s + 1);
+    const int i0 = k * bs, n = n_of(k), i1 = k1 * bs, n1 = n_of(k1);
+    if (blockIdx.x == 0) {
+      // rows of k1: r = y - A(k1, k) x_k, then x_k1 = Dinv_k1 r
+      for (int q = tid; q < n1 * nrhs; q += nt) {
+        const int r = q % n1, c = q / n1;
+        cx<T> acc = ldcg_cx(Y + i1 + r + (long long)c * N);
+        for (int kk = 0; kk < n; kk++) acc = acc - Ab[r + kk * bs] * xs[kk][c];
+        rk[r][c] = acc;
+      }
       __syncthreads();
-      const int sub = threadIdx.x & 3;
+      for (int q = tid; q < n1 * nrhs; q += nt) {
+        const int r = q % n1, c = q / n1;
+        cx<T> acc = zero;
+        for (int kk = 0; kk < n1; kk++) acc = acc + D[r + kk * bs] * rk[kk][c];
+        Y[i1 + r + (long long)c * N] = acc;
+        xs[r][c] = acc;
+      }
+      __syncthreads();
+      if (s + 2 < nb) stage(kb_of(s + 2), kb_of(s + 2), k1);
+      __threadfence();
+    }
+    // rows beyond k1 (below it for L, above it for U), 4 threads per row
+    const int r0 = LOWER ? i1 + n1 : 0, r1 = LOWER ? N : i1;
+    if ((blockIdx.x != 0 || G == 1) && r1 > r0) {
+      const int cb = G == 1 ? 0 : blockIdx.x - 1, GC = G == 1 ? 1 : G - 1;
+      for (int q = tid; q < n * nrhs; q += nt) xk[q % n][q / n] = ldcg_cx(Y + i0 + q % n + (long long)(q / n) * N);
+      __syncthreads();
+      const int sub = tid & 3;
       const int nrows = r1 - r0;
       // the loop trip count is uniform over the CTA, so every lane reaches the shuffles
-      for (int base0 = (blockIdx.x * blockDim.x) >> 2; base0 < nrows; base0 += gthreads >> 2) {
-        const int base = base0 + (threadIdx.x >> 2);
+      for (int base0 = (cb * nt) >> 2; base0 < nrows; base0 += (GC * nt) >> 2) {
+        const int base = base0 + (tid >> 2);
         const bool valid = base < nrows;
         const int i = r0 + (valid ? base : 0);
         cx<T> acc[8];
-        for (int c = 0; c < nrhs; c++) acc[c] = mk((T)0, (T)0);
+#pragma unroll
+        for (int c = 0; c < 8; c++) acc[c] = zero;
         cx<T> a[16];
 #pragma unroll
         for (int t = 0; t < 16; t++) {
-          int k = sub + 4 * t;
-          a[t] = (valid && k < n) ? A[i + (long long)(i0 + k) * lda] : mk((T)0, (T)0);
+          const int kk = sub + 4 * t;
+          a[t] = (valid && kk < n) ? A[i + (long long)(i0 + kk) * lda] : zero;
         }
 #pragma unroll
         for (int t = 0; t < 16; t++) {
-          int k = sub + 4 * t;
-          if (k < n)
-            for (int c = 0; c < nrhs; c++) acc[c] = acc[c] + a[t] * xk[k][c];
+          const int kk = sub + 4 * t;
+          if (kk < n) {
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+              if (c < nrhs) acc[c] = acc[c] + a[t] * xk[kk][c];
+          }
         }
-        for (int c = 0; c < nrhs; c++) {
-          cx<T> v = acc[c];
-          v.re += __shfl_xor_sync(0xffffffff, v.re, 1); v.im += __shfl_xor_sync(0xffffffff, v.im, 1);
-          v.re += __shfl_xor_sync(0xffffffff, v.re, 2); v.im += __shfl_xor_sync(0xffffffff, v.im, 2);
-          if (valid && sub == 0) Y[i + (long long)c * N] = Y[i + (long long)c * N] - v;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          if (c < nrhs) {  // nrhs is uniform: every lane takes the shuffles
+            cx<T> v = acc[c];
+            v.re += __shfl_xor_sync(0xffffffff, v.re, 1); v.im += __shfl_xor_sync(0xffffffff, v.im, 1);
+            v.re += __shfl_xor_sync(0xffffffff, v.re, 2); v.im += __shfl_xor_sync(0xffffffff, v.im, 2);
+            if (valid && sub == 0) Y[i + (long long)c * N] = ldcg_cx(Y + i + (long long)c * N) - v;
+          }
         }
       }
-      __syncthreads();
+      __threadfence();
     }
-    __threadfence();
     grid.sync();
   }
 }
@@ -595,7 +704,7 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
       int dev = 0, nsm = 0, per = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      size_t dsm = sizeof(cx<T>) * bs * bs;
+      size_t dsm = sizeof(cx<T>) * 2 * bs * bs;
       cudaFuncSetAttribute(trsv_coop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
       cudaFuncSetAttribute(trsv_coop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, dsm);
@@ -832,7 +941,7 @@ static gbem_status solve_chunk_n(const cx<T>* A, int N, int ld, const int* d_per
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  size_t dsm = sizeof(cx<T>) * bs * bs;
+  size_t dsm = sizeof(cx<T>) * 2 * bs * bs;
   cudaFuncSetAttribute(trsv_coop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
   cudaFuncSetAttribute(trsv_coop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, dsm);
