@@ -27,6 +27,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -39,6 +40,7 @@ namespace tc {
 constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
 constexpr int A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+static_assert((2 * STAGES + 5) * 8 + 4 <= 256, "barrier area");
 constexpr uint32_t TMEM_COLS = 256;
 constexpr long long SPIN_LIMIT = 1ll << 20;  // bounded waits (about a second at most)
 }  // namespace tc
@@ -53,6 +55,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
@@ -126,19 +131,41 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16* hi, __nv_bflo
   *lo = __float2bfloat16_rn(x - __bfloat162float(h));
 }
 
-// Ahat rows: one thread per (row i, kk)
-__global__ void pack_a(const cx<float>* A, long long lda, int m, int k, int Kp, __nv_bfloat16* out) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)m * k) return;
-  int i = (int)(t % m), kk = (int)(t / m);
-  cx<float> a = A[i + (long long)kk * lda];
-  __nv_bfloat16 rh, rl, ih, il;
-  split_bf16(a.re, &rh, &rl);
-  split_bf16(a.im, &ih, &il);
-  __nv_bfloat16* row = out + (long long)i * Kp;
-  row[kk] = rh; row[k + kk] = ih;
-  row[2 * k + kk] = rh; row[3 * k + kk] = ih;
-  row[4 * k + kk] = rl; row[5 * k + kk] = il;
+// Ahat rows, 16 rows per CTA (k <= 256): the rows' k complex values are staged
+// in shared memory by coalesced column reads, then each row (Kp bf16, zero
+// padded past 6k) is written with contiguous 8-byte stores.
+__global__ void __launch_bounds__(256) pack_a(const cx<float>* A, long long lda, int m, int k, int Kp,
+                                              __nv_bfloat16* out) {
+  __shared__ cx<float> t[256][17];
+  const int i0 = blockIdx.x * 16;
+  for (int q = threadIdx.x; q < 16 * k; q += blockDim.x) {
+    const int r = q & 15, kk = q >> 4, i = i0 + r;
+    t[kk][r] = i < m ? A[i + (long long)kk * lda] : mk(0.0f, 0.0f);
+  }
+  __syncthreads();
+  const int words = Kp >> 2;  // 4 bf16 per 8-byte store
+  for (int q = threadIdx.x; q < 16 * words; q += blockDim.x) {
+    const int r = q / words, w4 = q - r * words, i = i0 + r;
+    if (i >= m) continue;
+    __nv_bfloat16 v[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int p = 4 * w4 + e, seg = p / k, kk = p - seg * k;
+      float x = 0.0f;
+      bool lo = false;
+      if (seg < 6) {
+        const cx<float> z = t[kk][r];
+        x = (seg & 1) ? z.im : z.re;
+        lo = seg >= 4;
+      }
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      v[e] = lo ? __float2bfloat16_rn(x - __bfloat162float(h)) : h;
+    }
+    uint2 pk;
+    pk.x = (uint32_t)__bfloat16_as_ushort(v[0]) | ((uint32_t)__bfloat16_as_ushort(v[1]) << 16);
+    pk.y = (uint32_t)__bfloat16_as_ushort(v[2]) | ((uint32_t)__bfloat16_as_ushort(v[3]) << 16);
+    *reinterpret_cast<uint2*>(out + (long long)i * Kp + 4 * w4) = pk;
+  }
 }
 
 __global__ void pack_b(const cx<float>* B, long long ldb, int k, int n, int Kp, __nv_bfloat16* out) {
@@ -164,32 +191,39 @@ __global__ void zero_pad(__nv_bfloat16* out, long long rows, int K6, int Kp) {
 }
 
 // ---------------- the GEMM kernel ----------------
+// Persistent: CTA c takes output tiles c, c + P, c + 2P, ... (P = gridDim.x;
+// tiles ordered with the m index fastest, so the CTAs of a wave share their B
+// tile).  Two 256-column accumulators in TMEM: the MMAs of tile i+1 run while
+// the epilogue warps drain tile i.
 __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA,
                                                           const __grid_constant__ CUtensorMap mapB, cx<float>* C,
-                                                          long long ldc, int m, int n, int kblocks) {
+                                                          long long ldc, int m, int n, int kblocks, int mt,
+                                                          int ntiles) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   uintptr_t base = ((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023;
   unsigned char* tiles = (unsigned char*)base;
   uint64_t* full = (uint64_t*)(tiles + tc::STAGES * tc::STAGE_BYTES);
   uint64_t* empty = full + tc::STAGES;
-  uint64_t* accum = empty + tc::STAGES;
-  uint32_t* tmem_slot = (uint32_t*)(accum + 1);
+  uint64_t* acc_full = empty + tc::STAGES;  // [2] MMA -> epilogue
+  uint64_t* acc_empty = acc_full + 2;       // [2] epilogue -> MMA (8 warp arrivals)
+  uint64_t* drain = acc_empty + 2;          // all MMAs retired
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
   __shared__ int s_fail;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tm = blockIdx.x, tn = blockIdx.y;
   // once any CTA has given up on a wait, the rest of the grid does no work
   if (*(volatile int*)&g_tc_error) return;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < tc::STAGES; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-    mbar_init(accum, 1);
+    for (int a = 0; a < 2; a++) { mbar_init(&acc_full[a], 1); mbar_init(&acc_empty[a], 8); }
+    mbar_init(drain, 1);
     s_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(tc::TMEM_COLS));
+                 "r"(2 * tc::TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -199,63 +233,92 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
 
   if (warp == 0) {
     if (lane == 0) {
-      // producer
-      int issued = 0;
-      for (int kb = 0; kb < kblocks; kb++) {
-        int s = kb % tc::STAGES;
-        if (kb >= tc::STAGES) {
-          if (!mbar_wait(&empty[s], ((kb / tc::STAGES) - 1) & 1)) { atomicExch(&s_fail, 1); break; }
+      // producer: one ring of STAGES slots across all of this CTA's tiles
+      long long g = 0, issued = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int tm = t % mt, tn = t / mt;
+        for (int kb = 0; kb < kblocks; kb++, g++) {
+          const int s = (int)(g % tc::STAGES);
+          if (g >= tc::STAGES) {
+            if (!mbar_wait(&empty[s], (uint32_t)(((g / tc::STAGES) - 1) & 1))) { atomicExch(&s_fail, 1); ok = false; break; }
+          }
+          unsigned char* sa = tiles + s * tc::STAGE_BYTES;
+          mbar_arrive_expect_tx(&full[s], tc::STAGE_BYTES);
+          tma_load_2d(sa, &mapA, &full[s], kb * tc::BK, tm * tc::BM);
+          tma_load_2d(sa + tc::A_BYTES, &mapB, &full[s], kb * tc::BK, tn * tc::BN);
+          issued = g + 1;
         }
-        unsigned char* sa = tiles + s * tc::STAGE_BYTES;
-        mbar_arrive_expect_tx(&full[s], tc::STAGE_BYTES);
-        tma_load_2d(sa, &mapA, &full[s], kb * tc::BK, tm * tc::BM);
-        tma_load_2d(sa + tc::A_BYTES, &mapB, &full[s], kb * tc::BK, tn * tc::BN);
-        issued = kb + 1;
       }
-      // drain: make sure no TMA write is still in flight before the CTA exits
-      for (int kb = (issued > tc::STAGES ? issued - tc::STAGES : 0); kb < issued; kb++)
-        mbar_wait(&full[kb % tc::STAGES], (kb / tc::STAGES) & 1);
+      // drain: no TMA write may still be in flight when the CTA exits
+      for (long long q = (issued > tc::STAGES ? issued - tc::STAGES : 0); q < issued; q++)
+        mbar_wait(&full[q % tc::STAGES], (uint32_t)((q / tc::STAGES) & 1));
     }
   } else if (warp == 1) {
     if (lane == 0) {
+      long long g = 0;
       bool ok = true;
-      for (int kb = 0; kb < kblocks && ok; kb++) {
-        int s = kb % tc::STAGES;
-        if (!mbar_wait(&full[s], (kb / tc::STAGES) & 1)) { atomicExch(&s_fail, 1); ok = false; break; }
-        tc_fence_after();
-        uint32_t a0 = smem_u32(tiles + s * tc::STAGE_BYTES), b0 = a0 + tc::A_BYTES;
-        for (int kk = 0; kk < tc::BK / 16; kk++) {
-          uint64_t da = sdesc_sw128(a0 + kk * 32), db = sdesc_sw128(b0 + kk * 32);
-          umma_f16(tmem, da, db, (kb > 0 || kk > 0) ? 1u : 0u);
+      int i = 0;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, i++) {
+        const int acc = i & 1;
+        if (i >= 2 && !mbar_wait(&acc_empty[acc], (uint32_t)(((i >> 1) - 1) & 1))) {
+          atomicExch(&s_fail, 1);
+          break;
         }
-        umma_commit(&empty[s]);
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(acc * tc::TMEM_COLS);
+        for (int kb = 0; kb < kblocks; kb++, g++) {
+          const int s = (int)(g % tc::STAGES);
+          if (!mbar_wait(&full[s], (uint32_t)((g / tc::STAGES) & 1))) { atomicExch(&s_fail, 1); ok = false; break; }
+          tc_fence_after();
+          uint32_t a0 = smem_u32(tiles + s * tc::STAGE_BYTES), b0 = a0 + tc::A_BYTES;
+          for (int kk = 0; kk < tc::BK / 16; kk++) {
+            uint64_t da = sdesc_sw128(a0 + kk * 32), db = sdesc_sw128(b0 + kk * 32);
+            umma_f16(d, da, db, (kb > 0 || kk > 0) ? 1u : 0u);
+          }
+          umma_commit(&empty[s]);
+        }
+        if (ok) umma_commit(&acc_full[acc]);
       }
-      umma_commit(accum);
+      // every MMA issued so far has retired once this barrier completes
+      umma_commit(drain);
+      if (!mbar_wait(drain, 0)) atomicExch(&s_fail, 1);
     }
   } else {
     // epilogue warps 2..9: warp % 4 selects the TMEM lane quarter (row block
     // of 32), the two warps of a quarter split the 256 accumulator columns
     const int q = warp & 3, half = (warp - 2) >> 2;
-    const int row = tm * tc::BM + q * 32 + lane;
-    bool ok = mbar_wait(accum, 0);
-    if (!ok) atomicExch(&s_fail, 1);
-    tc_fence_after();
-    if (ok && !s_fail) {
+    int i = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+      const int acc = i & 1;
+      const int tm = t % mt, tn = t / mt;
+      const int row = tm * tc::BM + q * 32 + lane;
+      const bool ok = mbar_wait(&acc_full[acc], (uint32_t)((i >> 1) & 1));
+      if (!ok) atomicExch(&s_fail, 1);
+      if (!ok || *(volatile int*)&s_fail) break;
+      tc_fence_after();
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * tc::TMEM_COLS);
       for (int c0 = half * (tc::BN / 2); c0 < (half + 1) * (tc::BN / 2); c0 += 32) {
         const int j0 = (tn * tc::BN + c0) >> 1;
         // issue the 16 loads of C first (independent), then the TMEM read
         cx<float> z[16];
 #pragma unroll
-        for (int t = 0; t < 16; t++)
-          z[t] = (row < m && j0 + t < n) ? C[row + (long long)(j0 + t) * ldc] : mk(0.0f, 0.0f);
+        for (int u = 0; u < 16; u++)
+          z[u] = (row < m && j0 + u < n) ? C[row + (long long)(j0 + u) * ldc] : mk(0.0f, 0.0f);
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        tmem_ld32(tbase + (uint32_t)c0, v);
+        if (c0 + 32 >= (half + 1) * (tc::BN / 2)) {
+          // last TMEM read of this warp for the tile: hand the accumulator back
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acc_empty[acc]);
+        }
 #pragma unroll
-        for (int t = 0; t < 16; t++) {
-          if (row < m && j0 + t < n) {
-            z[t].re -= v[2 * t];
-            z[t].im -= v[2 * t + 1];
-            C[row + (long long)(j0 + t) * ldc] = z[t];
+        for (int u = 0; u < 16; u++) {
+          if (row < m && j0 + u < n) {
+            z[u].re -= v[2 * u];
+            z[u].im -= v[2 * u + 1];
+            C[row + (long long)(j0 + u) * ldc] = z[u];
           }
         }
       }
@@ -265,7 +328,7 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tc::TMEM_COLS));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * tc::TMEM_COLS));
   }
   if (threadIdx.x == 0 && s_fail) atomicExch(&g_tc_error, 1);
 }
@@ -321,12 +384,12 @@ bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long l
   if (!ws || ws_bytes < need) return false;
   __nv_bfloat16* pa = (__nv_bfloat16*)ws;
   __nv_bfloat16* pb = pa + (size_t)m * Kp;
-  long long ta = (long long)m * k, tb = (long long)k * n;
-  pack_a<<<(unsigned)((ta + 255) / 256), 256, 0, s>>>(A, lda, m, k, Kp, pa);
+  if (k > 256) return false;
+  long long tb = (long long)k * n;
+  pack_a<<<(unsigned)((m + 15) / 16), 256, 0, s>>>(A, lda, m, k, Kp, pa);
   pack_b<<<(unsigned)((tb + 255) / 256), 256, 0, s>>>(B, ldb, k, n, Kp, pb);
   if (Kp > 6 * k) {
     long long pw = (long long)(Kp - 6 * k);
-    zero_pad<<<(unsigned)(((long long)m * pw + 255) / 256), 256, 0, s>>>(pa, m, 6 * k, Kp);
     zero_pad<<<(unsigned)(((long long)2 * n * pw + 255) / 256), 256, 0, s>>>(pb, 2LL * n, 6 * k, Kp);
   }
   CUtensorMap ma, mb;
@@ -337,8 +400,15 @@ bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long l
     if (*err != cudaSuccess) return false;
     attr = true;
   }
-  dim3 grid((m + tc::BM - 1) / tc::BM, (2 * n + tc::BN - 1) / tc::BN);
-  tc_gemm_kernel<<<grid, 320, tc::SMEM_BYTES, s>>>(ma, mb, C, ldc, m, n, Kp / tc::BK);
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int mt = (m + tc::BM - 1) / tc::BM, ntn = (2 * n + tc::BN - 1) / tc::BN;
+  const int ntiles = mt * ntn;
+  tc_gemm_kernel<<<std::min(ntiles, nsm), 320, tc::SMEM_BYTES, s>>>(ma, mb, C, ldc, m, n, Kp / tc::BK, mt, ntiles);
   *err = cudaGetLastError();
   return *err == cudaSuccess;
 }
