@@ -17,6 +17,7 @@
 #include <cooperative_groups.h>
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 #include "bem_math.cuh"
@@ -226,6 +227,132 @@ __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Leaf of the recursive panel factorisation (complex FP32): columns
+// [c0, c0+w) (w <= LEAF_W) of rows [c0, N), held by the CTAs of ONE thread-block
+// cluster (rank r owns rows [c0 + r*Rr, c0 + (r+1)*Rr)).  Partial pivoting with
+// LAPACK's |Re|+|Im| measure (FP64), ties to the lowest row; per column one
+// cluster barrier, with the candidate records, candidate rows and the
+// diagonal row exchanged through distributed shared memory.
+// ---------------------------------------------------------------------------
+constexpr int LEAF_W = 16;
+constexpr int LEAF_STRIDE = LEAF_W + 1;  // odd: thread-per-row access is conflict-free
+
+struct LeafArgs {
+  cx<float>* A;
+  long long ld;
+  int N, c0, w, Rr;
+  int* ipiv;  // 0-based global pivot rows
+  int* info;
+};
+
+__global__ void __launch_bounds__(512) leaf_kernel(LeafArgs a) {
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<float>* rows = reinterpret_cast<cx<float>*>(smem_raw);  // [Rr][LEAF_STRIDE]
+  __shared__ Cand pub[2];
+  __shared__ cx<float> prow[2][LEAF_W];
+  __shared__ cx<float> drow[2][LEAF_W];
+  __shared__ cx<float> u[LEAF_W];
+  __shared__ double red_v[16];
+  __shared__ int red_i[16];
+  __shared__ int s_p, s_own;
+  const int rank = (int)cl.block_rank(), CL = (int)cl.num_blocks();
+  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  const int w = a.w;
+  const int m0 = a.c0 + rank * a.Rr;
+  const int nr = max(0, min(a.Rr, a.N - m0));
+  for (int q = tid; q < nr * w; q += nt) {
+    const int r = q % nr, k = q / nr;
+    rows[r * LEAF_STRIDE + k] = a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld];
+  }
+  __syncthreads();
+  {
+    double bv = -1.0;
+    int bi = -1;
+    for (int r = tid; r < nr; r += nt) {
+      const cx<float> z = rows[r * LEAF_STRIDE];
+      better(fabs((double)z.re) + fabs((double)z.im), m0 + r, bv, bi);
+    }
+    warp_best(bv, bi);
+    if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
+  }
+  __syncthreads();
+  for (int jj = 0; jj < w; jj++) {
+    const int d = a.c0 + jj, buf = jj & 1;
+    if (warp == 0) {
+      double bv = lane < nw ? red_v[lane] : -1.0;
+      int bi = lane < nw ? red_i[lane] : -1;
+      warp_best(bv, bi);
+      bv = __shfl_sync(0xffffffff, bv, 0);
+      bi = __shfl_sync(0xffffffff, bi, 0);
+      if (lane == 0) { pub[buf].v = bv; pub[buf].i = bi; pub[buf].pad = 0; }
+      if (bi >= 0 && lane < w) prow[buf][lane] = rows[(bi - m0) * LEAF_STRIDE + lane];
+    } else if (warp == 1 && d >= m0 && d < m0 + nr && lane < w) {
+      drow[buf][lane] = rows[(d - m0) * LEAF_STRIDE + lane];
+    }
+    cl.sync();
+    if (warp == 0) {
+      double gv = -1.0;
+      int gi = -1, gc = -1;
+      if (lane < CL) {
+        const Cand x = *cl.map_shared_rank(&pub[buf], lane);
+        gv = x.v; gi = x.i; gc = lane;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_down_sync(0xffffffff, gv, o);
+        int oi = __shfl_down_sync(0xffffffff, gi, o);
+        int oc = __shfl_down_sync(0xffffffff, gc, o);
+        if (oi >= 0 && (gi < 0 || ov > gv || (ov == gv && oi < gi))) { gv = ov; gi = oi; gc = oc; }
+      }
+      if (lane == 0) {
+        s_p = gi; s_own = gc;
+        if (rank == 0) {
+          a.ipiv[d] = gi;
+          if (gv == 0.0 && *a.info == 0) *a.info = d + 1;
+        }
+      }
+    }
+    __syncthreads();
+    const int p = s_p, own = s_own;
+    if (tid < w) {
+      const cx<float> x = cl.map_shared_rank(&prow[buf][0], own)[tid];
+      u[tid] = x;
+      if (d >= m0 && d < m0 + nr) rows[(d - m0) * LEAF_STRIDE + tid] = x;
+      if (p != d && p >= m0 && p < m0 + nr)
+        rows[(p - m0) * LEAF_STRIDE + tid] = cl.map_shared_rank(&drow[buf][0], (d - a.c0) / a.Rr)[tid];
+    }
+    __syncthreads();
+    // eliminate column jj (one thread per row) and search column jj+1
+    const cx<float> piv = u[jj];
+    const float pn = piv.re * piv.re + piv.im * piv.im;
+    const cx<float> inv = pn != 0.0f ? mk(piv.re / pn, -piv.im / pn) : mk(0.0f, 0.0f);
+    double bv = -1.0;
+    int bi = -1;
+    for (int r = max(0, d + 1 - m0) + tid; r < nr; r += nt) {
+      cx<float>* row = rows + r * LEAF_STRIDE;
+      if (pn != 0.0f) {
+        const cx<float> l = row[jj] * inv;
+        row[jj] = l;
+        for (int k = jj + 1; k < w; k++) row[k] = row[k] - l * u[k];
+      }
+      if (jj + 1 < w) {
+        const cx<float> z = row[jj + 1];
+        better(fabs((double)z.re) + fabs((double)z.im), m0 + r, bv, bi);
+      }
+    }
+    warp_best(bv, bi);
+    if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
+    __syncthreads();
+  }
+  // no CTA leaves while another may still read its shared memory
+  cl.sync();
+  for (int q = tid; q < nr * w; q += nt) {
+    const int r = q % nr, k = q / nr;
+    a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld] = rows[r * LEAF_STRIDE + k];
+  }
+}
+
 // row interchanges of columns [cb, ce) for pivots of rows [r0, r1)
 template <typename T>
 __global__ void laswp_kernel(cx<T>* A, long long ld, const int* ipiv, int r0, int r1, int cb, int ce, int skip0, int skip1) {
@@ -333,6 +460,86 @@ __global__ void __launch_bounds__(256) gemm_simt(cx<T>* C, long long ldc, const 
     }
 }
 
+// ---- recursive panel (complex FP32) with cluster leaves ----
+// Cluster size for the leaves of an N-row panel: 16 CTAs (non-portable) when
+// the device schedules them, else 8; 0 if the rows do not fit.
+static int leaf_cluster_size(int N, int smem_optin) {
+  static int disabled = -1;
+  if (disabled < 0) {
+    const char* e = getenv("GBEM_LU_LEAF");
+    disabled = (e && e[0] == '0') ? 1 : 0;
+  }
+  if (disabled) return 0;
+  for (int CL : {16, 8}) {
+    const size_t smem = (size_t)((N + CL - 1) / CL) * LEAF_STRIDE * sizeof(cx<float>);
+    if (smem + 2048 > (size_t)smem_optin) continue;
+    if (cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) continue;
+    if (CL > 8 && cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+      continue;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CL);
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, leaf_kernel, &cfg) == cudaSuccess && ncl >= 1) return CL;
+    cudaGetLastError();
+  }
+  return 0;
+}
+
+static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w, int* ipiv, int* info, int CL,
+                               cudaStream_t s) {
+  const int m = N - c0;
+  LeafArgs la;
+  la.A = A; la.ld = ld; la.N = N; la.c0 = c0; la.w = w; la.Rr = (m + CL - 1) / CL; la.ipiv = ipiv; la.info = info;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CL);
+  cfg.blockDim = dim3(512);
+  cfg.dynamicSmemBytes = (size_t)la.Rr * LEAF_STRIDE * sizeof(cx<float>);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, leaf_kernel, la);
+}
+
+// factor columns [c, c+w) of rows [c, N): left half, its interchanges on the
+// right half, U12 = L11^{-1} A12, A22 -= L21 U12, right half, its
+// interchanges on the left half.
+static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, int* ipiv, int* info, int CL,
+                             cudaStream_t s, int* launches) {
+  if (w <= LEAF_W) {
+    ++*launches;
+    return leaf_launch(A, ld, N, c, w, ipiv, info, CL, s);
+  }
+  const int h = ((w / 2 + LEAF_W - 1) / LEAF_W) * LEAF_W;
+  cudaError_t e = rec_panel(A, ld, N, c, h, ipiv, info, CL, s, launches);
+  if (e != cudaSuccess) return e;
+  const int wr = w - h, m2 = N - c - h;
+  laswp_kernel<float><<<(wr + 255) / 256, 256, 0, s>>>(A, ld, ipiv, c, c + h, c + h, c + w, 0, 0);
+  trsm_kernel<float><<<(wr + 31) / 32, 256, (size_t)h * 33 * sizeof(cx<float>), s>>>(A, ld, c, h, c + h, c + w);
+  if (m2 > 0) {
+    gemm_simt<float><<<dim3((m2 + 63) / 64, (wr + 63) / 64), 256, 0, s>>>(
+        A + (c + h) + (long long)(c + h) * ld, ld, A + (c + h) + (long long)c * ld, ld, A + c + (long long)(c + h) * ld,
+        ld, m2, wr, h);
+    ++*launches;
+  }
+  *launches += 2;
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  e = rec_panel(A, ld, N, c + h, wr, ipiv, info, CL, s, launches);
+  if (e != cudaSuccess) return e;
+  laswp_kernel<float><<<(h + 255) / 256, 256, 0, s>>>(A, ld, ipiv, c + h, c + w, c, c + h, 0, 0);
+  ++*launches;
+  return cudaGetLastError();
+}
+
 template <typename T>
 static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info, cudaStream_t s, void** ws,
                                size_t* ws_bytes) {
@@ -349,9 +556,12 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     R = (N + nsm - 1) / nsm;
     if ((size_t)(R * panel_stride(w) + w) * esz <= smem_cap || w <= 8) break;
   }
+  // complex FP32: recursive panels with cluster leaves where the leaf rows fit
+  const int leaf_cl = sizeof(T) == 4 ? leaf_cluster_size(N, smem_optin) : 0;
+  if (leaf_cl) w = 256;
   if (w > N) w = std::max(1, N);
   R = std::max(R, 1);
-  size_t smem = (size_t)(R * panel_stride(w) + w) * esz;
+  size_t smem = std::min((size_t)(R * panel_stride(w) + w) * esz, smem_cap);
   cudaError_t e = cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "panel smem");
   int maxb = 0;
@@ -384,7 +594,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     const int wc = std::min(w, N - c0);
     const int m = N - c0;
     int G = std::min(Gmax, (m + R - 1) / R);
-    if (G > 256) { set_error("LU panel: %d CTAs exceed the 256 candidate slots", G); return GBEM_ENOTSUP; }
+    if (!leaf_cl && G > 256) { set_error("LU panel: %d CTAs exceed the 256 candidate slots", G); return GBEM_ENOTSUP; }
     PanelArgs<T> pa;
     pa.A = A; pa.ld = ld; pa.N = N; pa.c0 = c0; pa.w = wc; pa.R = (m + G - 1) / G;
     pa.ipiv = d_ipiv; pa.info = d_info; pa.st = st;
@@ -392,9 +602,16 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     void* args[] = {&pa};
     {
       StatTimer tp(ST_PANEL, s);
-      stats_launch(ST_PANEL, 2);
-      e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(512), args, sm, s);
-      if (e != cudaSuccess) return cuda_status(e, "panel_kernel");
+      if (leaf_cl) {
+        int nl = 0;
+        e = rec_panel((cx<float>*)A, ld, N, c0, wc, d_ipiv, d_info, leaf_cl, s, &nl);
+        stats_launch(ST_PANEL, nl + 1);
+        if (e != cudaSuccess) return cuda_status(e, "recursive panel");
+      } else {
+        stats_launch(ST_PANEL, 2);
+        e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(512), args, sm, s);
+        if (e != cudaSuccess) return cuda_status(e, "panel_kernel");
+      }
       // interchanges to the left and right of the panel
       laswp_kernel<T><<<(N + 255) / 256, 256, 0, s>>>(A, ld, d_ipiv, c0, c0 + wc, 0, N, c0, c0 + wc);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "laswp");

@@ -94,3 +94,37 @@ def test_complex64_lu_tensor_core_update():
     x = M.LUSolve(b.astype(np.complex64)).astype(np.complex128)
     xr = sl.lu_solve((lu_ref, piv_ref), b)
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 2e-4
+
+
+@pytest.mark.parametrize("subdiv,pec,tol", [(1, False, 2e-6), (2, False, 2e-3), (3, True, 2e-3)])
+def test_complex64_lu_random_matrix(subdiv, pec, tol):
+    """C64 LU of a random matrix uploaded into a BEM-sized HMatrix.  N = 240
+    is one panel (recursive cluster leaves and FP32 updates only: backward
+    error at FP32 level); N = 960, 1920 add split-BF16 tensor-core trailing
+    updates, whose products keep about 16 mantissa bits."""
+    import scipy.linalg as sl
+    from gbem import C64, RWGGeometry, mesh
+    from gbem.api import HMatrix, Material
+    V, P = mesh.icosphere(subdiv)
+    G = RWGGeometry([{"V": V, "P": P, "material": None if pec else Material(2.25)}])
+    M = HMatrix(G, C64)
+    N = M.N
+    rng = np.random.default_rng(N)
+    A = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))).astype(np.complex64)
+    M.set(A)
+    assert M.LUFactorize() == 0
+    A = A.astype(np.complex128)
+    LU = M.numpy().astype(np.complex128)
+    L = np.tril(LU, -1) + np.eye(N)
+    U = np.triu(LU)
+    perm = np.arange(N)
+    for i, p in enumerate(M.ipiv - 1):  # LAPACK-style sequential interchanges
+        assert i <= p < N
+        perm[[i, p]] = perm[[p, i]]
+    # backward error of P A = L U; the |Re|+|Im| pivot bounds |l| by sqrt(2)
+    assert np.linalg.norm(A[perm] - L @ U) / np.linalg.norm(A) < tol
+    assert np.abs(L).max() <= np.sqrt(2.0) * (1 + 1e-5)
+    b = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    x = M.LUSolve(b.astype(np.complex64)).astype(np.complex128)
+    xr = sl.solve(A, b)
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 500 * tol
