@@ -447,41 +447,48 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
         }
       }
       if constexpr (sizeof(T) == 4) {
-        // FP32: moments of every region first, then each (Qa,Qb) combination
-        // once, with coefficients in FP32 (no FP64 work per pair)
+        // FP32: per region, the 9+9 moments in vector form, then every needed
+        // (Qa,Qb) from them (vec_combine); the slot takes the first region's
+        // value and adds the second's (one writer per slot: deterministic)
         constexpr int R2 = NC == 1 ? 1 : 2;
-        cx<T> MG[R2][9], MP[R2][9];
-        cx<T> p1[R2], pc[R2], p3[R2], m4[R2];
         for (int r = 0; r < R2; r++) {
-          cx<double> kd = r < ra.nreg ? ra.k[r] : mk(0.0, 0.0);
-          bool live = !(kd.re == 0.0 && kd.im == 0.0);
-          if (live) pair_moments<T, 0>(g, mk((T)kd.re, (T)kd.im), rule, 6, MG[r], MP[r]);
-          cx<double> m4d = live ? cdiv(mk(-4.0, 0.0), kd * kd) : mk(0.0, 0.0);
-          m4[r] = mk((T)m4d.re, (T)m4d.im);
-          p1[r] = live ? mk((T)ra.pf1[r].re, (T)ra.pf1[r].im) : mk((T)0, (T)0);
-          pc[r] = live ? mk((T)ra.pfc[r].re, (T)ra.pfc[r].im) : mk((T)0, (T)0);
-          p3[r] = live ? mk((T)ra.pf3[r].re, (T)ra.pf3[r].im) : mk((T)0, (T)0);
-          if (!live)
-            for (int m = 0; m < 9; m++) { MG[r][m] = mk((T)0, (T)0); MP[r][m] = mk((T)0, (T)0); }
-        }
-        for (int ja = 0; ja < 3; ja++) {
-          if (la[ja] < 0) continue;
-          for (int jb = 0; jb < 3; jb++) {
-            if (lb[jb] < 0) continue;
-            T c[9], d[9];
-            combo_coeffs_t(g, ja, jb, c, d);
-            cx<T> v0 = mk((T)0, (T)0), v1 = v0, v2 = v0;
-            for (int r = 0; r < R2; r++) {
-              cx<T> H0, H1;
-              combine(MG[r], MP[r], c, d, m4[r], &H0, &H1);
-              v0 = v0 + p1[r] * H0;
-              v1 = v1 + pc[r] * H1;
-              v2 = v2 + p3[r] * H0;
+          const cx<double> kd = r < ra.nreg ? ra.k[r] : mk(0.0, 0.0);
+          const bool live = !(kd.re == 0.0 && kd.im == 0.0);
+          VecMoments<T> vm;
+          cx<T> m4 = mk((T)0, (T)0), p1 = m4, pc = m4, p3 = m4;
+          if (live) {
+            cx<T> MG[9], MP[9];
+            pair_moments<T, 0>(g, mk((T)kd.re, (T)kd.im), rule, 6, MG, MP);
+            vec_moments(g, MG, MP, &vm);
+            const cx<double> m4d = cdiv(mk(-4.0, 0.0), kd * kd);
+            m4 = mk((T)m4d.re, (T)m4d.im);
+            p1 = mk((T)ra.pf1[r].re, (T)ra.pf1[r].im);
+            pc = mk((T)ra.pfc[r].re, (T)ra.pfc[r].im);
+            p3 = mk((T)ra.pf3[r].re, (T)ra.pf3[r].im);
+          }
+          for (int ja = 0; ja < 3; ja++) {
+            if (la[ja] < 0) continue;
+            for (int jb = 0; jb < 3; jb++) {
+              if (lb[jb] < 0) continue;
+              cx<T> v0 = mk((T)0, (T)0), v1 = v0, v2 = v0;
+              if (live) {
+                cx<T> H0, H1;
+                vec_combine(g, vm, ja, jb, m4, &H0, &H1);
+                v0 = p1 * H0;
+                v1 = pc * H1;
+                v2 = p3 * H0;
+              }
+              cx<T>* sl = slots + ((size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb]) * NC;
+              if (r == 0) {
+                sl[0] = v0;
+                if (NC > 1) sl[1] = v1;
+                if (NC > 2) sl[2] = v2;
+              } else {
+                sl[0] = sl[0] + v0;
+                if (NC > 1) sl[1] = sl[1] + v1;
+                if (NC > 2) sl[2] = sl[2] + v2;
+              }
             }
-            cx<T>* s = slots + ((size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb]) * NC;
-            s[0] = v0;
-            if (NC > 1) s[1] = v1;
-            if (NC > 2) s[2] = v2;
           }
         }
       } else {

@@ -222,6 +222,71 @@ GB_HD void combo_coeffs_t(const PairGeom<T>& g, int ja, int jb, T* c, T* d) {
 #undef GB_DET
 }
 
+// Vector form of a pair's moments.  With u = x - V0a = u Aa + v Ba and
+// v = x' - V0b = u' Ab + v' Bb:
+//   W0 = int G,  Wx = int u G,  Wy = int v G,  Wxy = int u.v G,
+//   P0 = int Psi, Pu = int u Psi, Pv = int v Psi, Puv = int u x v Psi,
+// all linear combinations of the 9+9 monomial moments.  For Q's with
+// alpha = V0a - Qa, beta = V0b - Qb and q = Qa - Qb = D0 - alpha + beta:
+//   H0 = Wxy + beta.Wx + alpha.Wy + (alpha.beta - 4/k^2) W0
+//   H1 = q.Puv + Pu.(beta x q) + Pv.(q x alpha) + (q.(alpha x beta)) P0
+// which is the monomial combination above, regrouped (about a third of its
+// arithmetic per (Qa, Qb)).
+template <typename T> struct VecMoments {
+  cx<T> W0, Wx[3], Wy[3], Wxy, P0, Pu[3], Pv[3], Puv[3];
+};
+
+template <typename T>
+GB_HD void vec_moments(const PairGeom<T>& g, const cx<T>* MG, const cx<T>* MP, VecMoments<T>* vm) {
+  const T* ea[2] = {g.Aa, g.Ba};
+  const T* eb[2] = {g.Ab, g.Bb};
+  vm->W0 = MG[0];
+  vm->P0 = MP[0];
+  for (int c = 0; c < 3; c++) {
+    vm->Wx[c] = g.Aa[c] * MG[3] + g.Ba[c] * MG[6];
+    vm->Wy[c] = g.Ab[c] * MG[1] + g.Bb[c] * MG[2];
+    vm->Pu[c] = g.Aa[c] * MP[3] + g.Ba[c] * MP[6];
+    vm->Pv[c] = g.Ab[c] * MP[1] + g.Bb[c] * MP[2];
+    vm->Puv[c] = mk((T)0, (T)0);
+  }
+  vm->Wxy = mk((T)0, (T)0);
+  for (int al = 0; al < 2; al++)
+    for (int be = 0; be < 2; be++) {
+      const T* x = ea[al];
+      const T* y = eb[be];
+      const int m = 3 * (al + 1) + (be + 1);
+      const T dot = x[0] * y[0] + x[1] * y[1] + x[2] * y[2];
+      const T cr[3] = {x[1] * y[2] - x[2] * y[1], x[2] * y[0] - x[0] * y[2], x[0] * y[1] - x[1] * y[0]};
+      vm->Wxy = vm->Wxy + dot * MG[m];
+      for (int c = 0; c < 3; c++) vm->Puv[c] = vm->Puv[c] + cr[c] * MP[m];
+    }
+}
+
+// H0, H1 for the Q's at local vertices ja, jb (0, 1, 2) of the two panels
+template <typename T>
+GB_HD void vec_combine(const PairGeom<T>& g, const VecMoments<T>& vm, int ja, int jb, cx<T> m4ok2, cx<T>* H0,
+                       cx<T>* H1) {
+  T al[3], be[3], q[3];
+  for (int c = 0; c < 3; c++) {
+    al[c] = ja == 0 ? (T)0 : (ja == 1 ? -g.Aa[c] : -g.Ba[c]);
+    be[c] = jb == 0 ? (T)0 : (jb == 1 ? -g.Ab[c] : -g.Bb[c]);
+    q[c] = g.D0[c] - al[c] + be[c];
+  }
+  const T ab = al[0] * be[0] + al[1] * be[1] + al[2] * be[2];
+  const T bxq[3] = {be[1] * q[2] - be[2] * q[1], be[2] * q[0] - be[0] * q[2], be[0] * q[1] - be[1] * q[0]};
+  const T qxa[3] = {q[1] * al[2] - q[2] * al[1], q[2] * al[0] - q[0] * al[2], q[0] * al[1] - q[1] * al[0]};
+  // q.(alpha x beta) = alpha.(beta x q)
+  const T tq = al[0] * bxq[0] + al[1] * bxq[1] + al[2] * bxq[2];
+  cx<T> h0 = vm.Wxy + ab * vm.W0 + m4ok2 * vm.W0;
+  cx<T> h1 = tq * vm.P0;
+  for (int c = 0; c < 3; c++) {
+    h0 = h0 + be[c] * vm.Wx[c] + al[c] * vm.Wy[c];
+    h1 = h1 + q[c] * vm.Puv[c] + bxq[c] * vm.Pu[c] + qxa[c] * vm.Pv[c];
+  }
+  *H0 = h0;
+  *H1 = h1;
+}
+
 // H0 = sum c MG - (4/k^2) MG[0];  H1 = sum d MP.
 template <typename T>
 GB_HD void combine(const cx<T>* MG, const cx<T>* MP, const T* c, const T* d, cx<T> m4ok2, cx<T>* H0, cx<T>* H1) {

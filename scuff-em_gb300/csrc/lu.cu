@@ -77,6 +77,22 @@ __device__ __forceinline__ Cand ldcg_cand(const Cand* p) {
   return c;
 }
 
+// asynchronous global -> shared copies (8 or 16 bytes), all in flight at once
+__device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)), "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)), "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+template <typename T>
+__device__ __forceinline__ void cp_async_cx(cx<T>* sdst, const cx<T>* gsrc) {
+  if constexpr (sizeof(T) == 4) cp_async8(sdst, gsrc);
+  else cp_async16(sdst, gsrc);
+}
+
 __device__ __forceinline__ void better(double v, int i, double& bv, int& bi) {
   if (i < 0) return;
   if (bi < 0 || v > bv || (v == bv && i < bi)) { bv = v; bi = i; }
@@ -242,7 +258,8 @@ struct LeafArgs {
   cx<float>* A;
   long long ld;
   int N, c0, w, Rr;
-  int* ipiv;  // 0-based global pivot rows
+  int pc0, pc1;  // the enclosing panel's columns: the leaf's interchanges are applied to all of them
+  int* ipiv;     // 0-based global pivot rows
   int* info;
 };
 
@@ -264,9 +281,24 @@ __global__ void __launch_bounds__(512) leaf_kernel(LeafArgs a) {
   const int nr = max(0, min(a.Rr, a.N - m0));
   for (int q = tid; q < nr * w; q += nt) {
     const int r = q % nr, k = q / nr;
-    rows[r * LEAF_STRIDE + k] = a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld];
+    cp_async8(&rows[r * LEAF_STRIDE + k], &a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld]);
   }
+  cp_async_wait_all();
   __syncthreads();
+  // this CTA's share of the panel's other columns, whose rows it interchanges
+  // one pivot behind (the loads of pivot jj are in flight during column jj+1)
+  int scol = -1;
+  {
+    int cnt = 0;
+    for (int col = a.pc0 + rank; col < a.pc1; col += CL) {
+      if (col >= a.c0 && col < a.c0 + w) continue;
+      if (cnt == tid) scol = col;
+      cnt++;
+    }
+  }
+  bool pend = false;
+  int pd = 0, pp = 0;
+  cx<float> xd = mk(0.0f, 0.0f), xp = xd;
   {
     double bv = -1.0;
     int bi = -1;
@@ -315,6 +347,11 @@ __global__ void __launch_bounds__(512) leaf_kernel(LeafArgs a) {
     }
     __syncthreads();
     const int p = s_p, own = s_own;
+    if (scol >= 0) {
+      cx<float>* colp = a.A + (long long)scol * a.ld;
+      if (pend) { colp[pp] = xd; colp[pd] = xp; pend = false; }
+      if (p != d && p >= 0) { xd = colp[d]; xp = colp[p]; pd = d; pp = p; pend = true; }
+    }
     if (tid < w) {
       const cx<float> x = cl.map_shared_rank(&prow[buf][0], own)[tid];
       u[tid] = x;
@@ -345,6 +382,11 @@ __global__ void __launch_bounds__(512) leaf_kernel(LeafArgs a) {
     if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
     __syncthreads();
   }
+  if (pend) {
+    cx<float>* colp = a.A + (long long)scol * a.ld;
+    colp[pp] = xd;
+    colp[pd] = xp;
+  }
   // no CTA leaves while another may still read its shared memory
   cl.sync();
   for (int q = tid; q < nr * w; q += nt) {
@@ -372,21 +414,23 @@ template <typename T>
 __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int N) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][33]
-  __shared__ cx<T> Lt[32][33];
+  __shared__ __align__(16) cx<T> Lt[32][33];       // cp.async targets: element-aligned
   const int j0 = cb + blockIdx.x * 32;
   const int nc = min(32, N - j0);
   const int tid = threadIdx.x;
   for (int q = tid; q < w * nc; q += blockDim.x) {
     int i = q % w, j = q / w;
-    B[i * 33 + j] = A[(c0 + i) + (long long)(j0 + j) * ld];
+    cp_async_cx(&B[i * 33 + j], &A[(c0 + i) + (long long)(j0 + j) * ld]);
   }
+  cp_async_wait_all();
   for (int kb = 0; kb < w; kb += 32) {
     const int kn = min(32, w - kb);
     __syncthreads();
     for (int q = tid; q < kn * kn; q += blockDim.x) {
       int i = q % kn, k = q / kn;
-      Lt[i][k] = A[(c0 + kb + i) + (long long)(c0 + kb + k) * ld];
+      cp_async_cx(&Lt[i][k], &A[(c0 + kb + i) + (long long)(c0 + kb + k) * ld]);
     }
+    cp_async_wait_all();
     __syncthreads();
     // diagonal tile: unit lower solve, columns in parallel
     for (int k = 0; k < kn - 1; k++) {
@@ -402,8 +446,9 @@ __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c
       __syncthreads();
       for (int q = tid; q < in * kn; q += blockDim.x) {
         int i = q % in, k = q / in;
-        Lt[i][k] = A[(c0 + ib + i) + (long long)(c0 + kb + k) * ld];
+        cp_async_cx(&Lt[i][k], &A[(c0 + ib + i) + (long long)(c0 + kb + k) * ld]);
       }
+      cp_async_wait_all();
       __syncthreads();
       for (int q = tid; q < in * nc; q += blockDim.x) {
         int i = q % in, j = q / in;
@@ -492,11 +537,12 @@ static int leaf_cluster_size(int N, int smem_optin) {
   return 0;
 }
 
-static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w, int* ipiv, int* info, int CL,
-                               cudaStream_t s) {
+static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w, int pc0, int pc1, int* ipiv, int* info,
+                               int CL, cudaStream_t s) {
   const int m = N - c0;
   LeafArgs la;
   la.A = A; la.ld = ld; la.N = N; la.c0 = c0; la.w = w; la.Rr = (m + CL - 1) / CL; la.ipiv = ipiv; la.info = info;
+  la.pc0 = pc0; la.pc1 = pc1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CL);
   cfg.blockDim = dim3(512);
@@ -510,34 +556,29 @@ static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w,
   return cudaLaunchKernelEx(&cfg, leaf_kernel, la);
 }
 
-// factor columns [c, c+w) of rows [c, N): left half, its interchanges on the
-// right half, U12 = L11^{-1} A12, A22 -= L21 U12, right half, its
-// interchanges on the left half.
-static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, int* ipiv, int* info, int CL,
-                             cudaStream_t s, int* launches) {
+// factor columns [c, c+w) of rows [c, N) inside the panel [pc0, pc1): left
+// half, U12 = L11^{-1} A12, A22 -= L21 U12, right half.  The leaves apply
+// their row interchanges to every column of the panel themselves.
+static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, int pc0, int pc1, int* ipiv, int* info,
+                             int CL, cudaStream_t s, int* launches) {
   if (w <= LEAF_W) {
     ++*launches;
-    return leaf_launch(A, ld, N, c, w, ipiv, info, CL, s);
+    return leaf_launch(A, ld, N, c, w, pc0, pc1, ipiv, info, CL, s);
   }
   const int h = ((w / 2 + LEAF_W - 1) / LEAF_W) * LEAF_W;
-  cudaError_t e = rec_panel(A, ld, N, c, h, ipiv, info, CL, s, launches);
+  cudaError_t e = rec_panel(A, ld, N, c, h, pc0, pc1, ipiv, info, CL, s, launches);
   if (e != cudaSuccess) return e;
   const int wr = w - h, m2 = N - c - h;
-  laswp_kernel<float><<<(wr + 255) / 256, 256, 0, s>>>(A, ld, ipiv, c, c + h, c + h, c + w, 0, 0);
   trsm_kernel<float><<<(wr + 31) / 32, 256, (size_t)h * 33 * sizeof(cx<float>), s>>>(A, ld, c, h, c + h, c + w);
+  ++*launches;
   if (m2 > 0) {
     gemm_simt<float><<<dim3((m2 + 63) / 64, (wr + 63) / 64), 256, 0, s>>>(
         A + (c + h) + (long long)(c + h) * ld, ld, A + (c + h) + (long long)c * ld, ld, A + c + (long long)(c + h) * ld,
         ld, m2, wr, h);
     ++*launches;
   }
-  *launches += 2;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  e = rec_panel(A, ld, N, c + h, wr, ipiv, info, CL, s, launches);
-  if (e != cudaSuccess) return e;
-  laswp_kernel<float><<<(h + 255) / 256, 256, 0, s>>>(A, ld, ipiv, c + h, c + w, c, c + h, 0, 0);
-  ++*launches;
-  return cudaGetLastError();
+  return rec_panel(A, ld, N, c + h, wr, pc0, pc1, ipiv, info, CL, s, launches);
 }
 
 template <typename T>
@@ -604,7 +645,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
       StatTimer tp(ST_PANEL, s);
       if (leaf_cl) {
         int nl = 0;
-        e = rec_panel((cx<float>*)A, ld, N, c0, wc, d_ipiv, d_info, leaf_cl, s, &nl);
+        e = rec_panel((cx<float>*)A, ld, N, c0, wc, c0, c0 + wc, d_ipiv, d_info, leaf_cl, s, &nl);
         stats_launch(ST_PANEL, nl + 1);
         if (e != cudaSuccess) return cuda_status(e, "recursive panel");
       } else {
