@@ -395,6 +395,187 @@ __global__ void __launch_bounds__(512) leaf_kernel(LeafArgs a) {
   }
 }
 
+// Register-resident leaf (same contract as leaf_kernel): each thread holds RT
+// rows of the leaf (r = tid + t * 512) in registers, so elimination is pure
+// register arithmetic.  Pivot search uses LAPACK's complex-FP32 measure
+// |Re|+|Im| in FP32 (ICAMAX), first maximum; warp candidates come from
+// redux.sync max/min, the CTA candidate from warp 0, the cluster winner from
+// the CTAs' records in distributed shared memory.  Three barriers per column
+// (one of them the cluster barrier).
+__device__ __forceinline__ void warp_cand(unsigned vb, int row, unsigned& wvb, int& wrow) {
+  const unsigned mx = __reduce_max_sync(0xffffffffu, vb);
+  const int cand = (vb == mx && row >= 0) ? row : 0x7fffffff;
+  wvb = mx;
+  wrow = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
+}
+
+template <int RT>
+__global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
+  cg::cluster_group cl = cg::this_cluster();
+  __shared__ Cand pub[2];
+  __shared__ __align__(16) cx<float> prow[2][LEAF_W];
+  __shared__ __align__(16) cx<float> drow[2][LEAF_W];
+  __shared__ __align__(16) cx<float> u[LEAF_W];
+  __shared__ __align__(16) cx<float> wrow[16][LEAF_W];
+  __shared__ unsigned w_vb[16];
+  __shared__ int w_row[16];
+  __shared__ int s_p, s_own;
+  const int rank = (int)cl.block_rank(), CL = (int)cl.num_blocks();
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr int NT = 512;
+  const int w = a.w;
+  const int m0 = a.c0 + rank * a.Rr;
+  const int nr = max(0, min(a.Rr, a.N - m0));
+  cx<float> R[RT][LEAF_W];
+#pragma unroll
+  for (int t = 0; t < RT; t++) {
+    const int r = tid + t * NT;
+#pragma unroll
+    for (int k = 0; k < LEAF_W; k++)
+      R[t][k] = (r < nr && k < w) ? a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld] : mk(0.0f, 0.0f);
+  }
+  // the panel's other columns whose rows this CTA interchanges, one pivot behind
+  int scol = -1;
+  {
+    int cnt = 0;
+    for (int col = a.pc0 + rank; col < a.pc1; col += CL) {
+      if (col >= a.c0 && col < a.c0 + w) continue;
+      if (cnt == tid) scol = col;
+      cnt++;
+    }
+  }
+  bool pend = false;
+  int pd = 0, pp = 0;
+  cx<float> xd = mk(0.0f, 0.0f), xp = xd;
+  // candidates of column 0
+  unsigned cvb = 0u;
+  int crow = -1;
+#pragma unroll
+  for (int t = 0; t < RT; t++) {
+    const int r = tid + t * NT;
+    if (r < nr) {
+      const unsigned vb = __float_as_uint(fabsf(R[t][0].re) + fabsf(R[t][0].im));
+      if (crow < 0 || vb > cvb) { cvb = vb; crow = m0 + r; }
+    }
+  }
+#pragma unroll
+  for (int jj = 0; jj < LEAF_W; jj++) {
+    if (jj >= w) break;
+    const int d = a.c0 + jj, buf = jj & 1;
+    // warp candidate; its owner lane stages the row; the owner of row d stages it too
+    {
+      unsigned wvb;
+      int wr;
+      warp_cand(cvb, crow, wvb, wr);
+      if (lane == 0) { w_vb[warp] = wvb; w_row[warp] = wr; }
+#pragma unroll
+      for (int t = 0; t < RT; t++) {
+        const int g = m0 + tid + t * NT;
+        if (tid + t * NT < nr) {
+          if (g == wr)
+#pragma unroll
+            for (int k = 0; k < LEAF_W; k++) wrow[warp][k] = R[t][k];
+          if (g == d)
+#pragma unroll
+            for (int k = 0; k < LEAF_W; k++) drow[buf][k] = R[t][k];
+        }
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const unsigned vb = lane < 16 ? w_vb[lane] : 0u;
+      const int rw = lane < 16 ? w_row[lane] : 0x7fffffff;
+      const unsigned mx = __reduce_max_sync(0xffffffffu, rw != 0x7fffffff ? vb : 0u);
+      const int cand = (rw != 0x7fffffff && vb == mx) ? rw : 0x7fffffff;
+      const int best = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
+      const unsigned who = __ballot_sync(0xffffffffu, rw == best && best != 0x7fffffff);
+      const int bw = who ? __ffs(who) - 1 : 0;
+      if (lane == 0) {
+        pub[buf].v = best != 0x7fffffff ? (double)__uint_as_float(mx) : -1.0;
+        pub[buf].i = best != 0x7fffffff ? best : -1;
+        pub[buf].pad = 0;
+      }
+      if (lane < LEAF_W && best != 0x7fffffff) prow[buf][lane] = wrow[bw][lane];
+    }
+    cl.sync();
+    if (warp == 0) {
+      unsigned vb = 0u;
+      int ri = 0x7fffffff;
+      if (lane < CL) {
+        const Cand x = *cl.map_shared_rank(&pub[buf], lane);
+        if (x.i >= 0) { vb = __float_as_uint((float)x.v); ri = x.i; }
+      }
+      const unsigned mx = __reduce_max_sync(0xffffffffu, vb);
+      const int cand = (ri != 0x7fffffff && vb == mx) ? ri : 0x7fffffff;
+      const int best = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
+      const unsigned who = __ballot_sync(0xffffffffu, lane < CL && ri == best);
+      const int own = who ? __ffs(who) - 1 : 0;
+      if (lane < w) u[lane] = cl.map_shared_rank(&prow[buf][0], own)[lane];
+      if (lane == 0) {
+        s_p = best; s_own = own;
+        if (rank == 0) {
+          a.ipiv[d] = best;
+          if (mx == 0u && *a.info == 0) *a.info = d + 1;
+        }
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (scol >= 0) {
+      cx<float>* colp = a.A + (long long)scol * a.ld;
+      if (pend) { colp[pp] = xd; colp[pd] = xp; pend = false; }
+      if (p != d) { xd = colp[d]; xp = colp[p]; pd = d; pp = p; pend = true; }
+    }
+    // interchange rows d and p in registers, eliminate column jj, search jj+1
+    const cx<float> piv = u[jj];
+    const float pn = piv.re * piv.re + piv.im * piv.im;
+    const cx<float> inv = pn != 0.0f ? mk(piv.re / pn, -piv.im / pn) : mk(0.0f, 0.0f);
+    cvb = 0u;
+    crow = -1;
+#pragma unroll
+    for (int t = 0; t < RT; t++) {
+      const int r = tid + t * NT, g = m0 + r;
+      if (r < nr) {
+        if (g == d) {
+#pragma unroll
+          for (int k = 0; k < LEAF_W; k++) R[t][k] = u[k];
+        } else if (g == p) {
+          const cx<float>* src = cl.map_shared_rank(&drow[buf][0], (d - a.c0) / a.Rr);
+#pragma unroll
+          for (int k = 0; k < LEAF_W; k++) R[t][k] = src[k];
+        }
+        if (g > d) {
+          if (pn != 0.0f) {
+            const cx<float> l = R[t][jj] * inv;
+            R[t][jj] = l;
+#pragma unroll
+            for (int k = jj + 1; k < LEAF_W; k++) R[t][k] = R[t][k] - l * u[k];
+          }
+          if (jj + 1 < LEAF_W) {
+            const unsigned vb = __float_as_uint(fabsf(R[t][jj + 1].re) + fabsf(R[t][jj + 1].im));
+            if (crow < 0 || vb > cvb) { cvb = vb; crow = g; }
+          }
+        }
+      }
+    }
+  }
+  if (pend) {
+    cx<float>* colp = a.A + (long long)scol * a.ld;
+    colp[pp] = xd;
+    colp[pd] = xp;
+  }
+  // no CTA leaves while another may still read its shared memory
+  cl.sync();
+#pragma unroll
+  for (int t = 0; t < RT; t++) {
+    const int r = tid + t * NT;
+    if (r < nr)
+#pragma unroll
+      for (int k = 0; k < LEAF_W; k++)
+        if (k < w) a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld] = R[t][k];
+  }
+}
+
 // row interchanges of columns [cb, ce) for pivots of rows [r0, r1)
 template <typename T>
 __global__ void laswp_kernel(cx<T>* A, long long ld, const int* ipiv, int r0, int r1, int cb, int ce, int skip0, int skip1) {
@@ -519,7 +700,11 @@ static int leaf_cluster_size(int N, int smem_optin) {
     const size_t smem = (size_t)((N + CL - 1) / CL) * LEAF_STRIDE * sizeof(cx<float>);
     if (smem + 2048 > (size_t)smem_optin) continue;
     if (cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) continue;
-    if (CL > 8 && cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+    if (CL > 8 && (cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+                   cudaFuncSetAttribute(leaf_kernel_reg<1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                       cudaSuccess ||
+                   cudaFuncSetAttribute(leaf_kernel_reg<2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                       cudaSuccess))
       continue;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(CL);
@@ -546,13 +731,16 @@ static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w,
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CL);
   cfg.blockDim = dim3(512);
-  cfg.dynamicSmemBytes = (size_t)la.Rr * LEAF_STRIDE * sizeof(cx<float>);
   cfg.stream = s;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
+  // rows in registers when each thread holds at most two, else in shared memory
+  if (la.Rr <= 512) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<1>, la);
+  if (la.Rr <= 1024) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<2>, la);
+  cfg.dynamicSmemBytes = (size_t)la.Rr * LEAF_STRIDE * sizeof(cx<float>);
   return cudaLaunchKernelEx(&cfg, leaf_kernel, la);
 }
 
