@@ -261,8 +261,8 @@ __global__ void __launch_bounds__(128) self_kernel(const DevNear* near, const in
   double V[9];
   for (int c = 0; c < 9; c++) V[c] = pv[9 * (size_t)d.pa + c];
   double* dst = nearval + 54 * (size_t)i;
-  double acc[54];
-  for (int c = 0; c < 54; c++) acc[c] = 0.0;
+  // lane q < 9 accumulates combination q = 3 ja + jb: KK (re, im), KN (zero), NN (re, im)
+  double acc0 = 0.0, acc1 = 0.0, acc4 = 0.0, acc5 = 0.0;
   for (int r = 0; r < ra.nreg; r++) {
     cx<double> k = ra.k[r];
     if (k.re == 0.0 && k.im == 0.0) continue;
@@ -276,7 +276,6 @@ __global__ void __launch_bounds__(128) self_kernel(const DevNear* near, const in
       MP[m] = mk(0.0, 0.0);
     }
     cx<double> m4ok2 = cdiv(mk(-4.0, 0.0), k * k);
-    // lane q < 9 forms combination q = 3 ja + jb
     if (lane < 9) {
       int ja = lane / 3, jb = lane % 3;
       double c[9], dd[9];
@@ -284,12 +283,14 @@ __global__ void __launch_bounds__(128) self_kernel(const DevNear* near, const in
       cx<double> H0, H1;
       combine(MG, MP, c, dd, m4ok2, &H0, &H1);
       cx<double> v0 = ra.pf1[r] * H0, v2 = ra.pf3[r] * H0;
-      acc[6 * lane + 0] += v0.re; acc[6 * lane + 1] += v0.im;
-      acc[6 * lane + 4] += v2.re; acc[6 * lane + 5] += v2.im;
+      acc0 += v0.re; acc1 += v0.im;
+      acc4 += v2.re; acc5 += v2.im;
     }
   }
-  if (lane < 9)
-    for (int c = 0; c < 6; c++) dst[6 * lane + c] = acc[6 * lane + c];
+  if (lane < 9) {
+    double* o = dst + 6 * lane;
+    o[0] = acc0; o[1] = acc1; o[2] = 0.0; o[3] = 0.0; o[4] = acc4; o[5] = acc5;
+  }
 }
 
 __global__ void near_kernel(const DevNear* near, const int* list, int n, const double* pv, const Fippi* fippi,
@@ -308,7 +309,7 @@ __global__ void near_kernel(const DevNear* near, const int* list, int n, const d
   }
   double* dst = nearval + 54 * (size_t)i;
   for (int c = 0; c < 54; c++) dst[c] = 0.0;
-  Fippi F = fippi[i];
+  const Fippi& F = fippi[i];  // read where used: keeps 33 doubles out of registers
   for (int r = 0; r < ra.nreg; r++) {
     cx<double> k = ra.k[r];
     if (k.re == 0.0 && k.im == 0.0) continue;
@@ -330,12 +331,12 @@ __global__ void near_kernel(const DevNear* near, const int* list, int n, const d
       continue;
     }
     cx<double> m4ok2 = cdiv(mk(-4.0, 0.0), k * k);
+    VecMoments<double> vm;
+    vec_moments(g, MG, MP, &vm);
     for (int ja = 0; ja < 3; ja++)
       for (int jb = 0; jb < 3; jb++) {
-        double c[9], dd[9];
-        combo_coeffs(Va, Vb, ja, jb, c, dd);
         cx<double> H0, H1;
-        combine(MG, MP, c, dd, m4ok2, &H0, &H1);
+        vec_combine(g, vm, ja, jb, m4ok2, &H0, &H1);
         if (desing) H1 = H1 + mk(-0.079577471545947667884 * htimes_rm3(F, Va, Vb, ja, jb), 0.0);
         store_near(dst, ja, jb, ra.pf1[r] * H0, ra.pfc[r] * H1, ra.pf3[r] * H0);
       }
@@ -386,19 +387,26 @@ template <typename T, int NC>
 __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* slots = reinterpret_cast<cx<T>*>(smem_raw);  // [TE][TE][4][NC]
-  __shared__ double s_pv[2][PMAX][9];
+  constexpr int PVN = sizeof(T) == 4 ? 1 : 9;  // the FP32 kernel keeps FP32 geometry only
+  __shared__ double s_pv[2][PMAX][PVN];
   __shared__ double s_pc[2][PMAX][4];
   __shared__ int8_t s_hl[2][3 * PMAX], s_hs[2][3 * PMAX];
   __shared__ int s_gp[2][PMAX];
   __shared__ float s_ev[2][PMAX][6];  // FP32 edge vectors V1-V0, V2-V0
   __shared__ float s_cf[2][PMAX][4];  // FP32 centroid and radius (pre-check of rRel)
+  __shared__ float s_v0[2][PMAX][6];  // V0 as FP32 (hi, lo) pairs: D0 to FP32 relative accuracy
+  __shared__ cx<float> s_rk[2], s_rm4[2], s_rp1[2], s_rpc[2], s_rp3[2];  // per-region FP32 constants
+  __shared__ int s_live[2];
+  __shared__ T s_el[2][TE];  // edge lengths of the tile's rows and columns
 
   const int2 tile = a.tiles[blockIdx.x];
   const DevEdgeBlock* RB = a.rows + tile.x;
   const DevEdgeBlock* CB = a.cols + tile.y;
   const int PR = RB->np, PC = CB->np, NR = RB->ne, NCc = CB->ne;
-  for (int q = threadIdx.x; q < PR * 9; q += blockDim.x) s_pv[0][q / 9][q % 9] = a.pv[9 * (size_t)RB->panels[q / 9] + q % 9];
-  for (int q = threadIdx.x; q < PC * 9; q += blockDim.x) s_pv[1][q / 9][q % 9] = a.pv[9 * (size_t)CB->panels[q / 9] + q % 9];
+  if constexpr (sizeof(T) == 8) {
+    for (int q = threadIdx.x; q < PR * 9; q += blockDim.x) s_pv[0][q / 9][q % 9] = a.pv[9 * (size_t)RB->panels[q / 9] + q % 9];
+    for (int q = threadIdx.x; q < PC * 9; q += blockDim.x) s_pv[1][q / 9][q % 9] = a.pv[9 * (size_t)CB->panels[q / 9] + q % 9];
+  }
   for (int q = threadIdx.x; q < PR * 4; q += blockDim.x) s_pc[0][q / 4][q % 4] = a.pc[4 * (size_t)RB->panels[q / 4] + q % 4];
   for (int q = threadIdx.x; q < PC * 4; q += blockDim.x) s_pc[1][q / 4][q % 4] = a.pc[4 * (size_t)CB->panels[q / 4] + q % 4];
   for (int q = threadIdx.x; q < 3 * PR; q += blockDim.x) { s_hl[0][q] = RB->hl[q]; s_hs[0][q] = RB->hs[q]; }
@@ -409,9 +417,31 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
   for (int q = threadIdx.x; q < 2 * PMAX; q += blockDim.x) {
     const int side = q / PMAX, p = q % PMAX;
     if (p >= (side ? PC : PR)) continue;
-    const double* V = s_pv[side][p];
+    const double* V = a.pv + 9 * (size_t)(side ? CB->panels[p] : RB->panels[p]);
     for (int c = 0; c < 3; c++) { s_ev[side][p][c] = (float)(V[3 + c] - V[c]); s_ev[side][p][3 + c] = (float)(V[6 + c] - V[c]); }
     for (int c = 0; c < 4; c++) s_cf[side][p][c] = (float)s_pc[side][p][c];
+    for (int c = 0; c < 3; c++) {
+      const float hi = (float)V[c];
+      s_v0[side][p][c] = hi;
+      s_v0[side][p][3 + c] = (float)(V[c] - (double)hi);
+    }
+  }
+  for (int q = threadIdx.x; q < 2 * TE; q += blockDim.x) {
+    const int side = q / TE, e = q % TE;
+    if (e < (side ? NCc : NR)) s_el[side][e] = (T)(side ? a.elen_b[CB->e0 + e] : a.elen_a[RB->e0 + e]);
+  }
+  if (threadIdx.x < 2) {
+    // region constants in FP32, formed once per CTA in FP64
+    const int r = threadIdx.x;
+    const cx<double> kd = r < ra.nreg ? ra.k[r] : mk(0.0, 0.0);
+    const bool live = !(kd.re == 0.0 && kd.im == 0.0);
+    s_live[r] = live;
+    const cx<double> m4d = live ? cdiv(mk(-4.0, 0.0), kd * kd) : mk(0.0, 0.0);
+    s_rk[r] = mk((float)kd.re, (float)kd.im);
+    s_rm4[r] = mk((float)m4d.re, (float)m4d.im);
+    s_rp1[r] = live ? mk((float)ra.pf1[r].re, (float)ra.pf1[r].im) : mk(0.0f, 0.0f);
+    s_rpc[r] = live ? mk((float)ra.pfc[r].re, (float)ra.pfc[r].im) : mk(0.0f, 0.0f);
+    s_rp3[r] = live ? mk((float)ra.pf3[r].re, (float)ra.pf3[r].im) : mk(0.0f, 0.0f);
   }
   __syncthreads();
 
@@ -437,7 +467,10 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
     if (far) {
       PairGeom<T> g;
       for (int c = 0; c < 3; c++) {
-        g.D0[c] = (T)(Va[c] - Vb[c]);
+        if constexpr (sizeof(T) == 4)
+          g.D0[c] = (s_v0[0][ia][c] - s_v0[1][ib][c]) + (s_v0[0][ia][3 + c] - s_v0[1][ib][3 + c]);
+        else
+          g.D0[c] = (T)(Va[c] - Vb[c]);
         if constexpr (sizeof(T) == 4) {
           g.Aa[c] = s_ev[0][ia][c]; g.Ba[c] = s_ev[0][ia][3 + c];
           g.Ab[c] = s_ev[1][ib][c]; g.Bb[c] = s_ev[1][ib][3 + c];
@@ -452,19 +485,13 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
         // value and adds the second's (one writer per slot: deterministic)
         constexpr int R2 = NC == 1 ? 1 : 2;
         for (int r = 0; r < R2; r++) {
-          const cx<double> kd = r < ra.nreg ? ra.k[r] : mk(0.0, 0.0);
-          const bool live = !(kd.re == 0.0 && kd.im == 0.0);
+          const bool live = s_live[r];
           VecMoments<T> vm;
-          cx<T> m4 = mk((T)0, (T)0), p1 = m4, pc = m4, p3 = m4;
+          const cx<T> m4 = s_rm4[r], p1 = s_rp1[r], pc = s_rpc[r], p3 = s_rp3[r];
           if (live) {
             cx<T> MG[9], MP[9];
-            pair_moments<T, 0>(g, mk((T)kd.re, (T)kd.im), rule, 6, MG, MP);
+            pair_moments<T, 0>(g, s_rk[r], rule, 6, MG, MP);
             vec_moments(g, MG, MP, &vm);
-            const cx<double> m4d = cdiv(mk(-4.0, 0.0), kd * kd);
-            m4 = mk((T)m4d.re, (T)m4d.im);
-            p1 = mk((T)ra.pf1[r].re, (T)ra.pf1[r].im);
-            pc = mk((T)ra.pfc[r].re, (T)ra.pfc[r].im);
-            p3 = mk((T)ra.pf3[r].re, (T)ra.pf3[r].im);
           }
           for (int ja = 0; ja < 3; ja++) {
             if (la[ja] < 0) continue;
@@ -569,7 +596,9 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
       const cx<T>* s = slots + (size_t)(i * TE + j) * 4 * NC;
       cx<T> v[3];
       for (int c = 0; c < NC; c++) v[c] = (s[c] - s[NC + c]) - (s[2 * NC + c] - s[3 * NC + c]);
-      T L = (T)(a.elen_a[RB->e0 + i] * a.elen_b[CB->e0 + j]);
+      T L;
+      if constexpr (sizeof(T) == 4) L = s_el[0][i] * s_el[1][j];
+      else L = (T)(a.elen_a[RB->e0 + i] * a.elen_b[CB->e0 + j]);
       for (int c = 0; c < NC; c++) v[c] = L * v[c];
       long long X = a.row_off + (long long)a.bpe_a * (RB->e0 + i);
       long long Y = a.col_off + (long long)a.bpe_b * (CB->e0 + j);

@@ -62,15 +62,29 @@ GB_HD double vdet(const double* a, const double* b, const double* c) {
   return vdot(t, c);
 }
 
+// 1/m for m = 1..100 (index m-1), so the series below multiplies instead of
+// dividing (the same correctly rounded values as 1.0 / m)
+#define GB_RECIP_VALUES 1.0 / 1, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 1.0 / 7, 1.0 / 8, 1.0 / 9, 1.0 / 10, 1.0 / 11, 1.0 / 12, 1.0 / 13, 1.0 / 14, 1.0 / 15, 1.0 / 16, 1.0 / 17, 1.0 / 18, 1.0 / 19, 1.0 / 20, 1.0 / 21, 1.0 / 22, 1.0 / 23, 1.0 / 24, 1.0 / 25, 1.0 / 26, 1.0 / 27, 1.0 / 28, 1.0 / 29, 1.0 / 30, 1.0 / 31, 1.0 / 32, 1.0 / 33, 1.0 / 34, 1.0 / 35, 1.0 / 36, 1.0 / 37, 1.0 / 38, 1.0 / 39, 1.0 / 40, 1.0 / 41, 1.0 / 42, 1.0 / 43, 1.0 / 44, 1.0 / 45, 1.0 / 46, 1.0 / 47, 1.0 / 48, 1.0 / 49, 1.0 / 50, 1.0 / 51, 1.0 / 52, 1.0 / 53, 1.0 / 54, 1.0 / 55, 1.0 / 56, 1.0 / 57, 1.0 / 58, 1.0 / 59, 1.0 / 60, 1.0 / 61, 1.0 / 62, 1.0 / 63, 1.0 / 64, 1.0 / 65, 1.0 / 66, 1.0 / 67, 1.0 / 68, 1.0 / 69, 1.0 / 70, 1.0 / 71, 1.0 / 72, 1.0 / 73, 1.0 / 74, 1.0 / 75, 1.0 / 76, 1.0 / 77, 1.0 / 78, 1.0 / 79, 1.0 / 80, 1.0 / 81, 1.0 / 82, 1.0 / 83, 1.0 / 84, 1.0 / 85, 1.0 / 86, 1.0 / 87, 1.0 / 88, 1.0 / 89, 1.0 / 90, 1.0 / 91, 1.0 / 92, 1.0 / 93, 1.0 / 94, 1.0 / 95, 1.0 / 96, 1.0 / 97, 1.0 / 98, 1.0 / 99, 1.0 / 100
+static __constant__ double c_recip_dev[100] = {GB_RECIP_VALUES};
+static const double c_recip_host[100] = {GB_RECIP_VALUES};
+#undef GB_RECIP_VALUES
+GB_HD double recip_int(int m) {
+#ifdef __CUDA_ARCH__
+  return c_recip_dev[m - 1];
+#else
+  return c_recip_host[m - 1];
+#endif
+}
+
 // ExpRel(x, 4) = sum_{m>=4} x^m/m!, summed until a term falls below 1e-8 of
 // the running sum (PanelPanelInteractions.cc:86-103; same truncation so the
 // desingularised remainder matches the reference term for term).
 GB_HD cx<double> exprel4(cx<double> x) {
   cx<double> term = mk(1.0, 0.0);
-  for (int m = 1; m < 4; m++) term = (1.0 / m) * (term * x);
+  for (int m = 1; m < 4; m++) term = recip_int(m) * (term * x);
   cx<double> sum = mk(0.0, 0.0);
   for (int m = 4; m < 100; m++) {
-    term = (1.0 / m) * (term * x);
+    term = recip_int(m) * (term * x);
     sum = sum + term;
     if (cnorm2(term) < 1.0e-16 * cnorm2(sum)) break;
   }
@@ -306,20 +320,23 @@ template <int NMAX>
 GB_HD void expint_moments(cx<double> z, cx<double>* E) {
   double az2 = cnorm2(z);
   if (az2 < 4.0) {
-    for (int n = 0; n <= NMAX; n++) {
-      cx<double> term = mk(1.0, 0.0), sum = mk(1.0 / (n + 1.0), 0.0);
-      for (int m = 1; m < 60; m++) {
-        term = (1.0 / m) * (term * z);
-        cx<double> t = (1.0 / (n + m + 1.0)) * term;
-        sum = sum + t;
-        if (cnorm2(t) < 1e-36 * cnorm2(sum)) break;
+    // E_n = sum_m z^m/m! / (n+m+1): one pass over m serves every n
+    cx<double> term = mk(1.0, 0.0);
+    for (int n = 0; n <= NMAX; n++) E[n] = mk(recip_int(n + 1), 0.0);
+    for (int m = 1; m < 60; m++) {
+      term = recip_int(m) * (term * z);
+      double worst = 0.0;
+      for (int n = 0; n <= NMAX; n++) {
+        const cx<double> t = recip_int(n + m + 1) * term;
+        E[n] = E[n] + t;
+        worst = fmax(worst, cnorm2(t) / cnorm2(E[n]));
       }
-      E[n] = sum;
+      if (worst < 1e-36) break;
     }
   } else {
-    cx<double> ez = cexpo(z);
-    E[0] = cdiv(ez - mk(1.0, 0.0), z);
-    for (int n = 1; n <= NMAX; n++) E[n] = cdiv(ez - (double)n * E[n - 1], z);
+    const cx<double> ez = cexpo(z), zi = cdiv(mk(1.0, 0.0), z);
+    E[0] = (ez - mk(1.0, 0.0)) * zi;
+    for (int n = 1; n <= NMAX; n++) E[n] = (ez - (double)n * E[n - 1]) * zi;
   }
 }
 
@@ -375,28 +392,42 @@ GB_HD void self_moments(const double* V, cx<double> k, const double* gx, const d
       double D[3];
       for (int i = 0; i < 3; i++) D[i] = z0 * E1[i] + z1 * E2[i];
       double X = sqrt(vdot(D, D));
-      cx<double> E[7];
-      expint_moments<6>(mk(-k.im * X, k.re * X), E);
-      rpoly lam = rp_aff(1.0, -sig);
-      rpoly om = rp_mul(lam, lam);  // w lambda^2 / w  (the 1/w of G is taken here)
-      double W = gw[it] * (1.0 / 6.0) * inv4pi / X;
+      cx<double> E[5];
+      expint_moments<4>(mk(-k.im * X, k.re * X), E);
+      // om = lambda^2 = (1 - sig w)^2 (the w lambda^2 of the Jacobian over the 1/w of G)
+      const double om0 = 1.0, om1 = -2.0 * sig, om2 = sig * sig;
+      const double W = gw[it] * (1.0 / 6.0) * inv4pi / X;
+      // sum over the three s' points of the degree-4 polynomials om * ma * mb, then
+      // one combination with E_0..E_4 per monomial pair
+      double Q[9][5];
+      for (int m = 0; m < 9; m++)
+        for (int n = 0; n < 5; n++) Q[m][n] = 0.0;
       for (int ip = 0; ip < 3; ip++) {
         double p1 = TP[ip][0], p2 = TP[ip][1];
         // s' = (p1, p2) + w ((am - cm) - sig p1, am - sig p2);  s = s' + w z
         double sb0 = p1, sb1 = (am - cm) - sig * p1, tb0 = p2, tb1 = am - sig * p2;
         double sa0 = sb0, sa1 = sb1 + z0, ta0 = tb0, ta1 = tb1 + z1;
-        // TCR coordinates u = s1 - s2, v = s2
-        rpoly ua = rp_aff(sa0 - ta0, sa1 - ta1), va = rp_aff(ta0, ta1);
-        rpoly ub = rp_aff(sb0 - tb0, sb1 - tb1), vb = rp_aff(tb0, tb1);
-        rpoly one = rp_aff(1.0, 0.0);
-        const rpoly ma[3] = {one, ua, va}, mb[3] = {one, ub, vb};
-        for (int al = 0; al < 3; al++)
+        // TCR coordinates u = s1 - s2, v = s2, affine in w: (c0, c1)
+        const double ma[3][2] = {{1.0, 0.0}, {sa0 - ta0, sa1 - ta1}, {ta0, ta1}};
+        const double mb[3][2] = {{1.0, 0.0}, {sb0 - tb0, sb1 - tb1}, {tb0, tb1}};
+        for (int al = 0; al < 3; al++) {
+          const double P0 = om0 * ma[al][0], P1 = om0 * ma[al][1] + om1 * ma[al][0],
+                       P2 = om1 * ma[al][1] + om2 * ma[al][0], P3 = om2 * ma[al][1];
           for (int be = 0; be < 3; be++) {
-            rpoly q = rp_mul(om, rp_mul(ma[al], mb[be]));
-            cx<double> s = mk(0.0, 0.0);
-            for (int n = 0; n < 7; n++) s = s + q.c[n] * E[n];
-            MG[3 * al + be] = MG[3 * al + be] + W * s;
+            const double n0 = mb[be][0], n1 = mb[be][1];
+            double* q = Q[3 * al + be];
+            q[0] += P0 * n0;
+            q[1] += P0 * n1 + P1 * n0;
+            q[2] += P1 * n1 + P2 * n0;
+            q[3] += P2 * n1 + P3 * n0;
+            q[4] += P3 * n1;
           }
+        }
+      }
+      for (int m = 0; m < 9; m++) {
+        cx<double> sm = mk(0.0, 0.0);
+        for (int n = 0; n < 5; n++) sm = sm + Q[m][n] * E[n];
+        MG[m] = MG[m] + W * sm;
       }
     }
   }
