@@ -415,10 +415,11 @@ __global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
   __shared__ Cand pub[2];
   __shared__ __align__(16) cx<float> prow[2][LEAF_W];
   __shared__ __align__(16) cx<float> drow[2][LEAF_W];
-  __shared__ __align__(16) cx<float> u[LEAF_W];
   __shared__ __align__(16) cx<float> wrow[16][LEAF_W];
   __shared__ unsigned w_vb[16];
   __shared__ int w_row[16];
+  __shared__ __align__(16) cx<float> allrows[16][LEAF_W];  // every CTA's candidate row
+  __shared__ __align__(16) cx<float> dcopy[LEAF_W];        // the diagonal row before the interchange
   __shared__ int s_p, s_own;
   const int rank = (int)cl.block_rank(), CL = (int)cl.num_blocks();
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -498,7 +499,15 @@ __global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
       if (lane < LEAF_W && best != 0x7fffffff) prow[buf][lane] = wrow[bw][lane];
     }
     cl.sync();
-    if (warp == 0) {
+    // one round trip through distributed shared memory: every CTA's record and
+    // candidate row, and the diagonal row, read in parallel
+    if (tid < 16 * LEAF_W) {
+      const int rk = tid / LEAF_W, k = tid % LEAF_W;
+      if (rk < CL && k < w) allrows[rk][k] = cl.map_shared_rank(&prow[buf][0], rk)[k];
+    } else if (tid < 17 * LEAF_W) {
+      const int k = tid - 16 * LEAF_W;
+      if (k < w) dcopy[k] = cl.map_shared_rank(&drow[buf][0], (d - a.c0) / a.Rr)[k];
+    } else if (warp == 9) {
       unsigned vb = 0u;
       int ri = 0x7fffffff;
       if (lane < CL) {
@@ -510,7 +519,6 @@ __global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
       const int best = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
       const unsigned who = __ballot_sync(0xffffffffu, lane < CL && ri == best);
       const int own = who ? __ffs(who) - 1 : 0;
-      if (lane < w) u[lane] = cl.map_shared_rank(&prow[buf][0], own)[lane];
       if (lane == 0) {
         s_p = best; s_own = own;
         if (rank == 0) {
@@ -520,6 +528,7 @@ __global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
       }
     }
     __syncthreads();
+    const cx<float>* u = allrows[s_own];  // the pivot row
     const int p = s_p;
     if (scol >= 0) {
       cx<float>* colp = a.A + (long long)scol * a.ld;
@@ -540,9 +549,8 @@ __global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
 #pragma unroll
           for (int k = 0; k < LEAF_W; k++) R[t][k] = u[k];
         } else if (g == p) {
-          const cx<float>* src = cl.map_shared_rank(&drow[buf][0], (d - a.c0) / a.Rr);
 #pragma unroll
-          for (int k = 0; k < LEAF_W; k++) R[t][k] = src[k];
+          for (int k = 0; k < LEAF_W; k++) R[t][k] = dcopy[k];
         }
         if (g > d) {
           if (pn != 0.0f) {
@@ -588,60 +596,70 @@ __global__ void laswp_kernel(cx<T>* A, long long ld, const int* ipiv, int r0, in
   }
 }
 
-// U12 = L11^{-1} A12: rows [c0, c0+w), columns [cb, N), 32 columns per CTA.
-// L11 is walked in 32 x 32 tiles staged in shared memory: each diagonal tile
-// is a short sequential solve, each tile below it a small GEMM update.
+// U12 = L11^{-1} A12: rows [c0, c0+w), columns [cb, ce), 32 columns per CTA.
+// L11 is walked in 32 x 32 tiles (each diagonal tile, then the tiles below it)
+// through two shared-memory buffers: the next tile's cp.async copy is in
+// flight while the current one is used.  A diagonal tile is a short
+// sequential solve, a tile below it a small GEMM update.
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
 template <typename T>
-__global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int N) {
+__global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int ce) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][33]
-  __shared__ __align__(16) cx<T> Lt[32][33];       // cp.async targets: element-aligned
+  __shared__ __align__(16) cx<T> Lt[2][32][33];    // cp.async targets: element-aligned
   const int j0 = cb + blockIdx.x * 32;
-  const int nc = min(32, N - j0);
+  const int nc = min(32, ce - j0);
   const int tid = threadIdx.x;
+  auto issue = [&](int buf, int kb, int ib) {
+    const int kn = min(32, w - kb), in = min(32, w - ib);
+    for (int q = tid; q < in * kn; q += blockDim.x) {
+      const int i = q % in, k = q / in;
+      cp_async_cx(&Lt[buf][i][k], &A[(c0 + ib + i) + (long long)(c0 + kb + k) * ld]);
+    }
+  };
   for (int q = tid; q < w * nc; q += blockDim.x) {
-    int i = q % w, j = q / w;
+    const int i = q % w, j = q / w;
     cp_async_cx(&B[i * 33 + j], &A[(c0 + i) + (long long)(j0 + j) * ld]);
   }
-  cp_async_wait_all();
+  issue(0, 0, 0);
+  cp_async_commit();
+  int buf = 0;
   for (int kb = 0; kb < w; kb += 32) {
     const int kn = min(32, w - kb);
-    __syncthreads();
-    for (int q = tid; q < kn * kn; q += blockDim.x) {
-      int i = q % kn, k = q / kn;
-      cp_async_cx(&Lt[i][k], &A[(c0 + kb + i) + (long long)(c0 + kb + k) * ld]);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    // diagonal tile: unit lower solve, columns in parallel
-    for (int k = 0; k < kn - 1; k++) {
-      for (int q = tid; q < (kn - k - 1) * nc; q += blockDim.x) {
-        int i = k + 1 + q % (kn - k - 1), j = q / (kn - k - 1);
-        B[(kb + i) * 33 + j] = B[(kb + i) * 33 + j] - Lt[i][k] * B[(kb + k) * 33 + j];
+    for (int ib = kb; ib < w; ib += 32) {
+      int nkb = kb, nib = ib + 32;
+      if (nib >= w) { nkb = kb + 32; nib = nkb; }
+      if (nkb < w) issue(buf ^ 1, nkb, nib);
+      cp_async_commit();
+      cp_async_wait_1();
+      __syncthreads();
+      if (ib == kb) {
+        // diagonal tile: unit lower solve, columns in parallel
+        for (int k = 0; k < kn - 1; k++) {
+          for (int q = tid; q < (kn - k - 1) * nc; q += blockDim.x) {
+            const int i = k + 1 + q % (kn - k - 1), j = q / (kn - k - 1);
+            B[(kb + i) * 33 + j] = B[(kb + i) * 33 + j] - Lt[buf][i][k] * B[(kb + k) * 33 + j];
+          }
+          __syncthreads();
+        }
+      } else {
+        // tile below: B[ib] -= L[ib, kb] * B[kb]
+        const int in = min(32, w - ib);
+        for (int q = tid; q < in * nc; q += blockDim.x) {
+          const int i = q % in, j = q / in;
+          cx<T> acc = mk((T)0, (T)0);
+          for (int k = 0; k < kn; k++) acc = acc + Lt[buf][i][k] * B[(kb + k) * 33 + j];
+          B[(ib + i) * 33 + j] = B[(ib + i) * 33 + j] - acc;
+        }
       }
       __syncthreads();
-    }
-    // tiles below: B[ib] -= L[ib, kb] * B[kb]
-    for (int ib = kb + kn; ib < w; ib += 32) {
-      const int in = min(32, w - ib);
-      __syncthreads();
-      for (int q = tid; q < in * kn; q += blockDim.x) {
-        int i = q % in, k = q / in;
-        cp_async_cx(&Lt[i][k], &A[(c0 + ib + i) + (long long)(c0 + kb + k) * ld]);
-      }
-      cp_async_wait_all();
-      __syncthreads();
-      for (int q = tid; q < in * nc; q += blockDim.x) {
-        int i = q % in, j = q / in;
-        cx<T> acc = mk((T)0, (T)0);
-        for (int k = 0; k < kn; k++) acc = acc + Lt[i][k] * B[(kb + k) * 33 + j];
-        B[(ib + i) * 33 + j] = B[(ib + i) * 33 + j] - acc;
-      }
+      buf ^= 1;
     }
   }
-  __syncthreads();
   for (int q = tid; q < w * nc; q += blockDim.x) {
-    int i = q % w, j = q / w;
+    const int i = q % w, j = q / w;
     A[(c0 + i) + (long long)(j0 + j) * ld] = B[i * 33 + j];
   }
 }
@@ -819,6 +837,9 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   void* tcws = (void*)(((uintptr_t)wp + 1023) & ~(uintptr_t)1023);
   e = cudaMemsetAsync(d_info, 0, sizeof(int), s);
   if (e != cudaSuccess) return cuda_status(e, "info");
+  // the U12 solves (outer and inside recursive panels) stage at most w rows
+  e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)((size_t)w * 33 * esz));
+  if (e != cudaSuccess) return cuda_status(e, "trsm smem");
   for (int c0 = 0; c0 < N; c0 += w) {
     const int wc = std::min(w, N - c0);
     const int m = N - c0;
@@ -849,10 +870,6 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     if (cb >= N) break;
     const int nrest = N - cb;
     size_t tsm = (size_t)wc * 33 * esz;
-    if (tsm > 48 * 1024) {
-      e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
-      if (e != cudaSuccess) return cuda_status(e, "trsm smem");
-    }
     {
       StatTimer tt(ST_PANEL, s);
       stats_launch(ST_PANEL);
