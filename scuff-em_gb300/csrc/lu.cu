@@ -190,6 +190,8 @@ __global__ void __launch_bounds__(512) panel_kernel(PanelArgs<T> a) {
         if (oi >= 0 && (gi < 0 || ov > gv || (ov == gv && oi < gi))) { gv = ov; gi = oi; gc = oc; }
       }
       if (lane == 0) {
+        // a missing candidate cannot happen (row d is one); it would read as a zero pivot at d
+        if (gi < 0) { gi = d; gc = min(G - 1, (d - a.c0) / a.R); gv = 0.0; }
         s_gv = gv; s_p = gi; s_wc = gc;
         if (c == 0) {
           a.ipiv[d] = gi;
@@ -338,6 +340,8 @@ __global__ void __launch_bounds__(512) leaf_kernel(LeafArgs a) {
         if (oi >= 0 && (gi < 0 || ov > gv || (ov == gv && oi < gi))) { gv = ov; gi = oi; gc = oc; }
       }
       if (lane == 0) {
+        // a missing candidate cannot happen (row d is one); it would read as a zero pivot at d
+        if (gi < 0) { gi = d; gc = (d - a.c0) / a.Rr; gv = 0.0; }
         s_p = gi; s_own = gc;
         if (rank == 0) {
           a.ipiv[d] = gi;
@@ -520,10 +524,13 @@ __global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
       const unsigned who = __ballot_sync(0xffffffffu, lane < CL && ri == best);
       const int own = who ? __ffs(who) - 1 : 0;
       if (lane == 0) {
-        s_p = best; s_own = own;
+        // no candidate anywhere cannot happen (row d itself is one); treat it
+        // as a zero pivot at d so no index is ever out of range
+        s_p = best != 0x7fffffff ? best : d;
+        s_own = own;
         if (rank == 0) {
-          a.ipiv[d] = best;
-          if (mx == 0u && *a.info == 0) *a.info = d + 1;
+          a.ipiv[d] = best != 0x7fffffff ? best : d;
+          if ((mx == 0u || best == 0x7fffffff) && *a.info == 0) *a.info = d + 1;
         }
       }
     }
@@ -533,7 +540,7 @@ __global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
     if (scol >= 0) {
       cx<float>* colp = a.A + (long long)scol * a.ld;
       if (pend) { colp[pp] = xd; colp[pd] = xp; pend = false; }
-      if (p != d) { xd = colp[d]; xp = colp[p]; pd = d; pp = p; pend = true; }
+      if (p != d && p > d && p < a.N) { xd = colp[d]; xp = colp[p]; pd = d; pp = p; pend = true; }
     }
     // interchange rows d and p in registers, eliminate column jj, search jj+1
     const cx<float> piv = u[jj];
@@ -766,25 +773,35 @@ static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w,
 // half, U12 = L11^{-1} A12, A22 -= L21 U12, right half.  The leaves apply
 // their row interchanges to every column of the panel themselves.
 static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, int pc0, int pc1, int* ipiv, int* info,
-                             int CL, cudaStream_t s, int* launches) {
+                             int CL, void* tcws, size_t tcb, cudaStream_t s, int* launches) {
   if (w <= LEAF_W) {
     ++*launches;
     return leaf_launch(A, ld, N, c, w, pc0, pc1, ipiv, info, CL, s);
   }
   const int h = ((w / 2 + LEAF_W - 1) / LEAF_W) * LEAF_W;
-  cudaError_t e = rec_panel(A, ld, N, c, h, pc0, pc1, ipiv, info, CL, s, launches);
+  cudaError_t e = rec_panel(A, ld, N, c, h, pc0, pc1, ipiv, info, CL, tcws, tcb, s, launches);
   if (e != cudaSuccess) return e;
   const int wr = w - h, m2 = N - c - h;
   trsm_kernel<float><<<(wr + 31) / 32, 256, (size_t)h * 33 * sizeof(cx<float>), s>>>(A, ld, c, h, c + h, c + w);
   ++*launches;
   if (m2 > 0) {
-    gemm_simt<float><<<dim3((m2 + 63) / 64, (wr + 63) / 64), 256, 0, s>>>(
-        A + (c + h) + (long long)(c + h) * ld, ld, A + (c + h) + (long long)c * ld, ld, A + c + (long long)(c + h) * ld,
-        ld, m2, wr, h);
-    ++*launches;
+    cx<float>* C = A + (c + h) + (long long)(c + h) * ld;
+    const cx<float>* L21 = A + (c + h) + (long long)c * ld;
+    const cx<float>* U12 = A + c + (long long)(c + h) * ld;
+    // the wide updates of the upper levels on the tensor cores (split BF16)
+    bool done = false;
+    if (h >= 64 && m2 >= 128) {
+      done = tc_gemm_update(C, ld, L21, ld, U12, ld, m2, wr, h, tcws, tcb, s, &e);
+      if (e != cudaSuccess) return e;
+      if (done) *launches += 3;
+    }
+    if (!done) {
+      gemm_simt<float><<<dim3((m2 + 63) / 64, (wr + 63) / 64), 256, 0, s>>>(C, ld, L21, ld, U12, ld, m2, wr, h);
+      ++*launches;
+    }
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  return rec_panel(A, ld, N, c + h, wr, pc0, pc1, ipiv, info, CL, s, launches);
+  return rec_panel(A, ld, N, c + h, wr, pc0, pc1, ipiv, info, CL, tcws, tcb, s, launches);
 }
 
 template <typename T>
@@ -854,7 +871,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
       StatTimer tp(ST_PANEL, s);
       if (leaf_cl) {
         int nl = 0;
-        e = rec_panel((cx<float>*)A, ld, N, c0, wc, c0, c0 + wc, d_ipiv, d_info, leaf_cl, s, &nl);
+        e = rec_panel((cx<float>*)A, ld, N, c0, wc, c0, c0 + wc, d_ipiv, d_info, leaf_cl, tcws, tcb, s, &nl);
         stats_launch(ST_PANEL, nl + 1);
         if (e != cudaSuccess) return cuda_status(e, "recursive panel");
       } else {

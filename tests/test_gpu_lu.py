@@ -96,12 +96,12 @@ def test_complex64_lu_tensor_core_update():
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 2e-4
 
 
-@pytest.mark.parametrize("subdiv,pec,tol", [(1, False, 2e-6), (2, False, 2e-3), (3, True, 2e-3)])
+@pytest.mark.parametrize("subdiv,pec,tol", [(1, False, 1e-4), (2, False, 2e-3), (3, True, 2e-3)])
 def test_complex64_lu_random_matrix(subdiv, pec, tol):
     """C64 LU of a random matrix uploaded into a BEM-sized HMatrix.  N = 240
-    is one panel (recursive cluster leaves and FP32 updates only: backward
-    error at FP32 level); N = 960, 1920 add split-BF16 tensor-core trailing
-    updates, whose products keep about 16 mantissa bits."""
+    is one panel (recursive cluster leaves; split-BF16 tensor-core updates at
+    the upper recursion levels); N = 960, 1920 add split-BF16 trailing
+    updates.  The split keeps about 16 mantissa bits per product."""
     import scipy.linalg as sl
     from gbem import C64, RWGGeometry, mesh
     from gbem.api import HMatrix, Material
