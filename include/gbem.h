@@ -102,8 +102,9 @@ gbem_status gbem_matrix_upload(gbem_matrix *m, const void *host, int ldh);
  * (AssembleBEMMatrix.cc:684-765, compact geometries, kBloch = NULL).
  * eps/mu: 2*num_regions doubles each (re, im) at this frequency (the values
  * RWGGeometry::UpdateCachedEpsMuValues caches, RWGGeometry.cc:1093-1113).
- * precision: gbem_precision.  The matrix dtype must be C128 for FP64 and
- * C64 for MIXED (F64 is accepted for FP64 at purely imaginary Omega). */
+ * precision: gbem_precision.  The matrix dtype must be C128 or F64 for FP64
+ * and C64 for MIXED; F64 (the reference's real storage, used at purely
+ * imaginary Omega where the matrix is real) keeps the real part. */
 gbem_status gbem_assemble(gbem_geometry *g, double omega_re, double omega_im,
                           const double *eps, const double *mu, int precision,
                           gbem_matrix *M);
@@ -113,17 +114,35 @@ gbem_status gbem_assemble(gbem_geometry *g, double omega_re, double omega_im,
 gbem_status gbem_assemble_host(gbem_geometry *g, double omega_re, double omega_im,
                                const double *eps, const double *mu, double *ZM, int ld);
 
+/* Replaces RWGGeometry::AssembleBEMMatrixBlock(nsa, nsb, Omega, kBloch=NULL, M,
+ * GradM=NULL, RowOffset, ColOffset) (AssembleBEMMatrix.cc:349-391, compact
+ * geometries): the block of rows of surface nsa's basis functions and columns
+ * of surface nsb's, written to the device array dst (column-major, leading
+ * dimension ld) at (row0, col0).  dtype C128 or F64 with GBEM_PREC_FP64 (F64:
+ * real storage, the reference's LHM_REAL at imaginary frequency, where the
+ * block is real), C64 with GBEM_PREC_MIXED.  This entry produces no gradient
+ * (GradM) or torque (dMdT) blocks. */
+gbem_status gbem_assemble_block(gbem_geometry *g, int nsa, int nsb, double omega_re, double omega_im,
+                                const double *eps, const double *mu, int precision, void *dst, int ld,
+                                int row0, int col0, int dtype);
+/* Host-buffer variant of gbem_assemble_block (FP64; dtype C128 or F64): fills
+ * rows row0.. and columns col0.. of the host column-major array host. */
+gbem_status gbem_assemble_block_host(gbem_geometry *g, int nsa, int nsb, double omega_re, double omega_im,
+                                     const double *eps, const double *mu, void *host, int ld, int row0,
+                                     int col0, int dtype);
+
 /* ---- dense LU ------------------------------------------------------------ */
 /* Replaces HMatrix::LUFactorize (libs/libhmat/LBWrappers.cc:151-171):
- * in-place LU with partial pivoting of a C128 (zgetrf semantics) or C64
+ * in-place LU with partial pivoting of a C128 (zgetrf semantics), F64
+ * (dgetrf semantics, computed as complex128 with zero imaginary parts) or C64
  * matrix.  ipiv (optional, host, N ints) receives 1-based pivots; info is 0,
  * or k > 0 if U(k,k) is exactly zero. */
 gbem_status gbem_lu_factor(gbem_matrix *M, int *ipiv, int *info);
 
 /* Replaces HMatrix::LUSolve(HMatrix *X, char Trans, int nrhs)
  * (LBWrappers.cc:208-236): solves op(M) X = B in place on a host
- * column-major C128 (or C64 for a C64 factor) array B (N x nrhs, ldb);
- * trans is 'N' or 'T'. */
+ * column-major array B (N x nrhs, ldb) of the factor's type (C128, C64, or
+ * real F64); trans is 'N' or 'T'. */
 gbem_status gbem_lu_solve(gbem_matrix *M, char trans, int nrhs, void *B, int ldb);
 
 /* gbem_lu_solve without any device allocation.  No counterpart in the

@@ -325,9 +325,8 @@ __global__ void near_kernel(const DevNear* near, const int* list, int n, const d
     } else if (d.ncv == 0) {
       pair_moments<double, 0>(g, k, c_ho, HO_N * HO_N, MG, MP);
     } else {
-      // touching pair in the short-wavelength regime (the reference switches
-      // to Taylor-Duffy with the full Helmholtz kernel there): not built yet
-      atomicOr(status, 1);
+      // touching pair in the short-wavelength regime: td_touch_kernel adds
+      // this region's full-kernel Taylor-Duffy values after this kernel
       continue;
     }
     cx<double> m4ok2 = cdiv(mk(-4.0, 0.0), k * k);
@@ -340,6 +339,57 @@ __global__ void near_kernel(const DevNear* near, const int* list, int n, const d
         if (desing) H1 = H1 + mk(-0.079577471545947667884 * htimes_rm3(F, Va, Vb, ja, jb), 0.0);
         store_near(dst, ja, jb, ra.pf1[r] * H0, ra.pfc[r] * H1, ra.pf3[r] * H0);
       }
+  }
+}
+
+// One warp per touching pair (ncv = 1, 2) in the short-wavelength regime
+// (|k rmax| > pi, PanelPanelInteractions.cc:416-418): the Duffy points are
+// split over the lanes, the 9 G moments and 10 H1 moments reduced with
+// shuffles, and lanes 0..8 add the nine (Qa,Qb) combinations.
+constexpr int N_TD = 12;  // Gauss points per Duffy dimension
+__global__ void __launch_bounds__(128) td_touch_kernel(const DevNear* near, const int* list, int n, const double* pv,
+                                                       RegionArgs ra, double* nearval) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;  // whole warps exit together
+  const int i = list[warp];
+  const DevNear d = near[i];
+  if (d.ncv < 1 || d.ncv > 2) return;
+  double Va[9], Vb[9];
+  for (int c = 0; c < 9; c++) { Va[c] = pv[9 * (size_t)d.pa + c]; Vb[c] = pv[9 * (size_t)d.pb + c]; }
+  PairGeom<double> g;
+  for (int c = 0; c < 3; c++) {
+    g.D0[c] = Va[c] - Vb[c];
+    g.Aa[c] = Va[3 + c] - Va[c]; g.Ba[c] = Va[6 + c] - Va[c];
+    g.Ab[c] = Vb[3 + c] - Vb[c]; g.Bb[c] = Vb[6 + c] - Vb[c];
+  }
+  double* dst = nearval + 54 * (size_t)i;
+  for (int r = 0; r < ra.nreg; r++) {
+    const cx<double> k = ra.k[r];
+    if (k.re == 0.0 && k.im == 0.0) continue;
+    if (!(hypot(k.re * d.rmax, k.im * d.rmax) > M_PI)) continue;  // near_kernel's desingularised branch
+    cx<double> MG[9], T[10];
+    td_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, k, c_gx12, c_gw12, N_TD, lane, 32, MG, T);
+    for (int m = 0; m < 9; m++)
+      for (int o = 16; o > 0; o >>= 1) {
+        MG[m].re += __shfl_xor_sync(0xffffffff, MG[m].re, o);
+        MG[m].im += __shfl_xor_sync(0xffffffff, MG[m].im, o);
+      }
+    for (int m = 0; m < 10; m++)
+      for (int o = 16; o > 0; o >>= 1) {
+        T[m].re += __shfl_xor_sync(0xffffffff, T[m].re, o);
+        T[m].im += __shfl_xor_sync(0xffffffff, T[m].im, o);
+      }
+    if (lane < 9) {
+      const int ja = lane / 3, jb = lane % 3;
+      cx<double> MP[9];
+      for (int m = 0; m < 9; m++) MP[m] = mk(0.0, 0.0);
+      VecMoments<double> vm;
+      vec_moments(g, MG, MP, &vm);
+      cx<double> H0, H1unused;
+      vec_combine(g, vm, ja, jb, cdiv(mk(-4.0, 0.0), k * k), &H0, &H1unused);
+      const cx<double> H1 = td_h1(Va, Vb, T, ja, jb);
+      store_near(dst, ja, jb, ra.pf1[r] * H0, ra.pfc[r] * H1, ra.pf3[r] * H0);
+    }
   }
 }
 
@@ -360,7 +410,9 @@ struct TileArgs {
   const double* nearval;
   int row_panel_offset;
   int bpe_a, bpe_b;
-  int row_off, col_off;
+  int row_off, col_off;    // where entry (row edge, col edge) of the block goes
+  int mrow_off, mcol_off;  // where its mirror (col edge, row edge) goes
+  int passes;              // bit 0: write the block, bit 1: write the mirror
   int sym;
   void* out;
   long long ld;
@@ -589,6 +641,7 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
   // mirrors it, so the matrix is exactly symmetric (AssembleBEMMatrix.cc:753-758).
   const bool diag = a.sym && tile.x == tile.y;
   for (int pass = 0; pass < 2; pass++) {
+    if (!(a.passes & (1 << pass))) continue;
     for (int q = threadIdx.x; q < NR * NCc; q += blockDim.x) {
       int i, j;
       if (pass == 0) { i = q % NR; j = q / NR; } else { j = q % NCc; i = q / NCc; }
@@ -600,8 +653,10 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
       if constexpr (sizeof(T) == 4) L = s_el[0][i] * s_el[1][j];
       else L = (T)(a.elen_a[RB->e0 + i] * a.elen_b[CB->e0 + j]);
       for (int c = 0; c < NC; c++) v[c] = L * v[c];
-      long long X = a.row_off + (long long)a.bpe_a * (RB->e0 + i);
-      long long Y = a.col_off + (long long)a.bpe_b * (CB->e0 + j);
+      // pass 0: entry (X, Y) of the block; pass 1: its mirror at (Y, X), with
+      // the mirror's own offsets (block assembly places either one anywhere)
+      long long X = (pass == 0 ? a.row_off : a.mcol_off) + (long long)a.bpe_a * (RB->e0 + i);
+      long long Y = (pass == 0 ? a.col_off : a.mrow_off) + (long long)a.bpe_b * (CB->e0 + j);
       // block entries (dx, dy) -> value
       cx<T> e00 = v[0], e01, e10, e11;
       if (a.bpe_a == 1 && a.bpe_b == 1) {
@@ -654,7 +709,7 @@ gbem_status compute_fippi(Geometry* g, cudaStream_t s) {
 }
 
 gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int precision,
-                            void* dM, int ld, int dtype, cudaStream_t s) {
+                            void* dM, int ld, int dtype, cudaStream_t s, const BlockSel* only) {
   if ((precision == GBEM_PREC_FP64 && dtype != GBEM_C128) || (precision == GBEM_PREC_MIXED && dtype != GBEM_C64)) {
     set_error("gbem_assemble: matrix dtype does not match the precision (C128 for FP64, C64 for MIXED)");
     return GBEM_EINVAL;
@@ -666,10 +721,21 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
     if (st != GBEM_OK) return st;
   }
   bool any_empty = false;
-  for (const Block& b : g->blocks) any_empty |= (b.nreg == 0);
+  for (const Block& b : g->blocks)
+    if (!only || (b.sa == std::min(only->nsa, only->nsb) && b.sb == std::max(only->nsa, only->nsb)))
+      any_empty |= (b.nreg == 0);
   size_t esz = dtype == GBEM_C128 ? 16 : 8;
   if (any_empty) {
-    cudaError_t e = cudaMemset2DAsync(dM, (size_t)ld * esz, 0, (size_t)g->N * esz, g->N, s);
+    // surfaces that share no region interact with zero: clear what is written
+    cudaError_t e;
+    if (!only) {
+      e = cudaMemset2DAsync(dM, (size_t)ld * esz, 0, (size_t)g->N * esz, g->N, s);
+    } else {
+      const int na = g->S[only->nsa].ne * (g->S[only->nsa].pec ? 1 : 2);
+      const int nb = g->S[only->nsb].ne * (g->S[only->nsb].pec ? 1 : 2);
+      e = cudaMemset2DAsync((char*)dM + ((size_t)only->row0 + (size_t)only->col0 * ld) * esz, (size_t)ld * esz, 0,
+                            (size_t)na * esz, nb, s);
+    }
     if (e != cudaSuccess) return cuda_status(e, "memset matrix");
   }
   int* d_status = nullptr;
@@ -681,6 +747,7 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
     const Block& b = g->blocks[bi];
     DevBlock* db = g->dblocks[bi];
     if (b.nreg == 0) continue;
+    if (only && !(b.sa == std::min(only->nsa, only->nsb) && b.sb == std::max(only->nsa, only->nsb))) continue;
     RegionArgs ra;
     memset(&ra, 0, sizeof ra);
     ra.nreg = b.nreg;
@@ -714,6 +781,15 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
         near_kernel<<<(db->nother + 63) / 64, 64, 0, s>>>(db->near, db->other_list, db->nother, g->d_pv, db->fippi,
                                                           ra, db->nearval, d_status);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "near_kernel");
+        // touching pairs in the short-wavelength regime (only when some k |r| can exceed pi)
+        double kmax = 0.0;
+        for (int r = 0; r < b.nreg; r++) kmax = std::fmax(kmax, std::hypot(ra.k[r].re, ra.k[r].im));
+        if (kmax * b.rmax_touch > M_PI) {
+          stats_launch(ST_NEAR);
+          td_touch_kernel<<<(db->nother + 3) / 4, 128, 0, s>>>(db->near, db->other_list, db->nother, g->d_pv, ra,
+                                                               db->nearval);
+          if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "td_touch_kernel");
+        }
       }
     }
     TileArgs ta;
@@ -723,6 +799,19 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
     ta.row_panel_offset = g->S[b.sa].panel_offset;
     ta.bpe_a = b.bpe_a; ta.bpe_b = b.bpe_b;
     ta.row_off = g->S[b.sa].bf_offset; ta.col_off = g->S[b.sb].bf_offset;
+    ta.mrow_off = ta.col_off; ta.mcol_off = ta.row_off;
+    ta.passes = 3;
+    if (only) {
+      // block assembly: the (nsa, nsb) block at (row0, col0) of dM
+      if (b.sa == only->nsa) {
+        ta.row_off = only->row0; ta.col_off = only->col0;
+        ta.mrow_off = only->row0; ta.mcol_off = only->col0;  // a self block mirrors into itself
+        ta.passes = b.sym ? 3 : 1;
+      } else {
+        ta.mrow_off = only->row0; ta.mcol_off = only->col0;  // (nsa, nsb) is the mirror of (sb, sa)
+        ta.passes = 2;
+      }
+    }
     ta.sym = b.sym ? 1 : 0;
     ta.out = dM; ta.ld = ld;
     int nc = (b.bpe_a == 2 && b.bpe_b == 2) ? 3 : ((b.bpe_a == 1 && b.bpe_b == 1) ? 1 : 2);

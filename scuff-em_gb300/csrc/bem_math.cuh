@@ -350,6 +350,22 @@ GB_HD rpoly rp_aff(double a0, double a1) {
   p.c[0] = a0; p.c[1] = a1;
   return p;
 }
+GB_HD rpoly rp_add(const rpoly& a, const rpoly& b) {
+  rpoly p;
+  for (int i = 0; i < 8; i++) p.c[i] = a.c[i] + b.c[i];
+  return p;
+}
+GB_HD rpoly rp_scale(const rpoly& a, double s) {
+  rpoly p;
+  for (int i = 0; i < 8; i++) p.c[i] = a.c[i] * s;
+  return p;
+}
+GB_HD rpoly rp_shift(const rpoly& a) {  // times w
+  rpoly p;
+  p.c[0] = 0.0;
+  for (int i = 0; i + 1 < 8; i++) p.c[i + 1] = a.c[i];
+  return p;
+}
 GB_HD rpoly rp_mul(const rpoly& a, const rpoly& b) {
   rpoly p;
   for (int i = 0; i < 8; i++) p.c[i] = 0.0;
@@ -638,6 +654,139 @@ GB_HD void fippi_touch(int ncv, const double* Va, const double* Vb, const int* p
           }
         }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Touching pairs with the full Helmholtz kernel (the short-wavelength branch
+// of PanelPanelInteractions.cc:449-491, which the reference evaluates by
+// Taylor-Duffy with KIndex HELMHOLTZ / GRADHELMHOLTZ).  Same Duffy cells as
+// fippi_touch; along each ray x - x' = w D (r = w X) the radial integrals are
+// the E_n(ikX) of expint_moments.  Outputs, per (pair, region):
+//   MG[9]  = int int mono_m G                     (H0 as for far pairs)
+//   T[10]  = { int int (u x v).(x-x') Psi,  int int (x-x') x u Psi [3],
+//              int int v x (x-x') Psi [3],  int int (x-x') Psi [3] }
+// with u = x - V0a, v = x' - V0b (mesh order).  For Q's with alpha = V0a - Qa,
+// beta = V0b - Qb:  H1 = T0 + beta.Tu + alpha.Tv + (alpha x beta).Tr, since
+// ((u+alpha) x (v+beta)).(x-x') splits that way; every integrand keeps the
+// factor (x - x') that makes the r^-3 of Psi integrable.
+// ---------------------------------------------------------------------------
+GB_HD_NOINLINE void td_touch_point(const double* Ea, const double* Eb, const int* pa, const int* pb,
+                                   const double* Va, const double* Vb, cx<double> k, const DuffyPt& pt,
+                                   cx<double>* MG, cx<double>* T) {
+  const double inv4pi = 0.079577471545947667884;
+  double A[3], B[3], Ap[3], Bp[3], D[3];
+  for (int i = 0; i < 3; i++) {
+    A[i] = Ea[3 + i] - Ea[i]; B[i] = Ea[6 + i] - Ea[3 + i];
+    Ap[i] = Eb[3 + i] - Eb[i]; Bp[i] = Eb[6 + i] - Eb[3 + i];
+    D[i] = pt.sa1[0] * A[i] + pt.sa1[1] * B[i] - pt.sb1[0] * Ap[i] - pt.sb1[1] * Bp[i];
+  }
+  const double X = sqrt(vdot(D, D));
+  rpoly ua, va, ub, vb;
+  tcr_from_edge(pa, pt.sa0, pt.sa1, &ua, &va);
+  tcr_from_edge(pb, pt.sb0, pt.sb1, &ub, &vb);
+  cx<double> E[5];
+  expint_moments<4>(mk(-k.im * X, k.re * X), E);
+  // G: sum_n p_n E_{n-1} / (4 pi X), p = om ma mb
+  const rpoly one = rp_aff(1.0, 0.0);
+  const rpoly ma[3] = {one, ua, va}, mb[3] = {one, ub, vb};
+  const double gfac = pt.W * inv4pi / X;
+  for (int al = 0; al < 3; al++)
+    for (int be = 0; be < 3; be++) {
+      const rpoly q = rp_mul(pt.om, rp_mul(ma[al], mb[be]));
+      cx<double> sm = mk(0.0, 0.0);
+      for (int n = 1; n <= 5; n++) sm = sm + q.c[n] * E[n - 1];
+      MG[3 * al + be] = MG[3 * al + be] + gfac * sm;
+    }
+  // Psi: p = om w S(w); L[p] = sum_n p_n (ik/(4 pi X^2) E_{n-2} - 1/(4 pi X^3) E_{n-3})
+  const cx<double> c2 = (pt.W * inv4pi / (X * X)) * mk(-k.im, k.re);
+  const double c3 = -pt.W * inv4pi / (X * X * X);
+  auto Lpsi = [&](const rpoly& Sw) {
+    const rpoly p = rp_mul(pt.om, rp_shift(Sw));
+    cx<double> acc = mk(0.0, 0.0);
+    for (int n = 2; n <= 6; n++) acc = acc + p.c[n] * (c2 * E[n - 2]);
+    for (int n = 3; n <= 7; n++) acc = acc + (c3 * p.c[n]) * E[n - 3];
+    return acc;
+  };
+  double Aa[3], Ba[3], Ab[3], Bb[3];
+  for (int i = 0; i < 3; i++) {
+    Aa[i] = Va[3 + i] - Va[i]; Ba[i] = Va[6 + i] - Va[i];
+    Ab[i] = Vb[3 + i] - Vb[i]; Bb[i] = Vb[6 + i] - Vb[i];
+  }
+  double x1[3], x2[3], x3[3], x4[3];
+  vcross(Aa, Ab, x1); vcross(Aa, Bb, x2); vcross(Ba, Ab, x3); vcross(Ba, Bb, x4);
+  // (u x v).D with u = ua Aa + va Ba, v = ub Ab + vb Bb
+  const rpoly S0 = rp_add(rp_add(rp_scale(rp_mul(ua, ub), vdot(x1, D)), rp_scale(rp_mul(ua, vb), vdot(x2, D))),
+                          rp_add(rp_scale(rp_mul(va, ub), vdot(x3, D)), rp_scale(rp_mul(va, vb), vdot(x4, D))));
+  T[0] = T[0] + Lpsi(S0);
+  double dA[3], dB[3], aD[3], bD[3];
+  vcross(D, Aa, dA); vcross(D, Ba, dB); vcross(Ab, D, aD); vcross(Bb, D, bD);
+  const cx<double> L1 = Lpsi(one);
+  for (int c = 0; c < 3; c++) {
+    T[1 + c] = T[1 + c] + Lpsi(rp_add(rp_scale(ua, dA[c]), rp_scale(va, dB[c])));   // (x-x') x u
+    T[4 + c] = T[4 + c] + Lpsi(rp_add(rp_scale(ub, aD[c]), rp_scale(vb, bD[c])));   // v x (x-x')
+    T[7 + c] = T[7 + c] + D[c] * L1;                                                  // (x-x')
+  }
+}
+
+// Duffy cells of fippi_touch with the full kernel (ncv = 1 or 2); pt index
+// range [p0, npts) in steps of pstride lets a warp split the points.
+GB_HD int td_touch_npts(int ncv, int n) { return ncv == 1 ? 2 * n * n * n : 8 * n * n; }
+
+GB_HD void td_touch(int ncv, const double* Va, const double* Vb, const int* pa, const int* pb, cx<double> k,
+                    const double* gx, const double* gw, int n, int p0, int pstride, cx<double>* MG, cx<double>* T) {
+  double Ea[9], Eb[9];
+  for (int i = 0; i < 3; i++)
+    for (int c = 0; c < 3; c++) {
+      Ea[3 * i + c] = pa[i] == 0 ? Va[c] : (pa[i] == 1 ? Va[3 + c] : Va[6 + c]);
+      Eb[3 * i + c] = pb[i] == 0 ? Vb[c] : (pb[i] == 1 ? Vb[3 + c] : Vb[6 + c]);
+    }
+  for (int m = 0; m < 9; m++) MG[m] = mk(0.0, 0.0);
+  for (int m = 0; m < 10; m++) T[m] = mk(0.0, 0.0);
+  const int np = td_touch_npts(ncv, n);
+  DuffyPt pt;
+  for (int q = p0; q < np; q += pstride) {
+    if (ncv == 1) {
+      const int reg = q / (n * n * n), rem = q % (n * n * n);
+      const int i1 = rem / (n * n), i2 = (rem / n) % n, i3 = rem % n;
+      const double al = gx[i1], be = gx[i2], ga = gx[i3];
+      pt.sa0[0] = pt.sa0[1] = pt.sb0[0] = pt.sb0[1] = 0.0;
+      if (reg == 0) { pt.sa1[0] = 1.0; pt.sa1[1] = al; pt.sb1[0] = be; pt.sb1[1] = be * ga; }
+      else { pt.sb1[0] = 1.0; pt.sb1[1] = al; pt.sa1[0] = be; pt.sa1[1] = be * ga; }
+      pt.om = rp_aff(0.0, 0.0); pt.om.c[3] = be;
+      pt.W = gw[i1] * gw[i2] * gw[i3];
+    } else {
+      const double tx[2] = {0.21132486540518711775, 0.78867513459481288225};
+      const int reg = q / (2 * n * n), rem = q % (2 * n * n);
+      const int ia = rem / (2 * n), ib = (rem / 2) % n, it = rem % 2;
+      const double al = gx[ia], be = gx[ib];
+      double z[3], J, lo;
+      if (reg == 0) { z[0] = 1.0 - al; z[1] = be; z[2] = al; J = 1.0; lo = al; }
+      else if (reg == 1) { z[0] = al; z[1] = 1.0; z[2] = (1.0 - al) * be; J = 1.0 - al; lo = 1.0 - al; }
+      else if (reg == 2) { z[0] = -al; z[1] = (1.0 - al) * be; z[2] = 1.0; J = 1.0 - al; lo = 1.0; }
+      else { z[0] = -al; z[1] = 1.0 - al; z[2] = be; J = 1.0; lo = 1.0; }
+      const double tau = tx[it];
+      pt.sb0[0] = tau; pt.sb1[0] = lo - tau;
+      pt.sb0[1] = 0.0; pt.sb1[1] = z[2];
+      pt.sa0[0] = tau; pt.sa1[0] = lo - tau + z[0];
+      pt.sa0[1] = 0.0; pt.sa1[1] = z[1];
+      pt.om = rp_aff(0.0, 0.0); pt.om.c[2] = 1.0; pt.om.c[3] = -1.0;
+      pt.W = gw[ia] * gw[ib] * 0.5 * J;
+    }
+    td_touch_point(Ea, Eb, pa, pb, Va, Vb, k, pt, MG, T);
+  }
+}
+
+// H1 of touching pairs from the T moments
+GB_HD cx<double> td_h1(const double* Va, const double* Vb, const cx<double>* T, int ja, int jb) {
+  double al[3], be[3], ab[3];
+  for (int c = 0; c < 3; c++) {
+    al[c] = Va[c] - Va[3 * ja + c];
+    be[c] = Vb[c] - Vb[3 * jb + c];
+  }
+  vcross(al, be, ab);
+  cx<double> h = T[0];
+  for (int c = 0; c < 3; c++) h = h + be[c] * T[1 + c] + al[c] * T[4 + c] + ab[c] * T[7 + c];
+  return h;
 }
 
 // ---------------------------------------------------------------------------

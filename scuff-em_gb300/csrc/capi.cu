@@ -66,6 +66,7 @@ gbem_status rhs_planewave_device(Geometry* g, double wr, double wi, const double
                                  const double* nh, void* d_rhs, cudaStream_t s);
 
 static size_t esize(int dtype) { return dtype == GBEM_C128 ? 16 : (dtype == GBEM_C64 ? 8 : 8); }
+static bool omega_is_zero(double wr, double wi) { return wr == 0.0 && wi == 0.0; }
 
 static void perm_from_ipiv(const std::vector<int>& ipiv0, std::vector<int>& perm) {
   int N = (int)ipiv0.size();
@@ -181,8 +182,8 @@ gbem_status gbem_geometry_near_counts(const gbem_geometry* g, long long counts[4
 }
 
 gbem_status gbem_matrix_create(const gbem_geometry* g, int dtype, gbem_matrix** out) {
-  if (!g || !out || (dtype != GBEM_C128 && dtype != GBEM_C64)) {
-    set_error("gbem_matrix_create: bad arguments (dtype must be C128 or C64)");
+  if (!g || !out || (dtype != GBEM_C128 && dtype != GBEM_C64 && dtype != GBEM_F64)) {
+    set_error("gbem_matrix_create: bad arguments (dtype must be C128, C64 or F64)");
     return GBEM_EINVAL;
   }
   *out = nullptr;
@@ -239,14 +240,94 @@ gbem_status gbem_matrix_upload(gbem_matrix* m, const void* host, int ldh) {
   return GBEM_OK;
 }
 
+// real parts of an m x n complex128 block (the reference's real storage at
+// imaginary frequency, where the matrix is real)
+static __global__ void take_real(const double2* src, long long lds, double* dst, long long ldd, int m, int n) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)m * n) return;
+  const int i = (int)(t % m), j = (int)(t / m);
+  dst[i + j * ldd] = src[i + j * lds].x;
+}
+static __global__ void make_complex(const double* src, long long lds, double2* dst, long long ldd, int m, int n) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)m * n) return;
+  const int i = (int)(t % m), j = (int)(t / m);
+  dst[i + j * ldd] = make_double2(src[i + j * lds], 0.0);
+}
+
+static int surface_bfs(const gbem_geometry* g, int ns) { return g->S[ns].ne * (g->S[ns].pec ? 1 : 2); }
+
+// assembly of the whole matrix (sel = NULL) or of one surface block into a
+// device array; F64 goes through a complex128 block whose real part is kept
+static gbem_status assemble_into(gbem_geometry* g, double wr, double wi, const double* eps, const double* mu,
+                                 int precision, void* dst, int ld, int dtype, const BlockSel* sel) {
+  if (omega_is_zero(wr, wi)) { set_error("gbem_assemble: Omega = 0 is not supported"); return GBEM_EINVAL; }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  cudaStream_t s = g->stream;
+  if (dtype != GBEM_F64) return assemble_device(g, wr, wi, eps, mu, precision, dst, ld, dtype, s, sel);
+  if (precision != GBEM_PREC_FP64) { set_error("gbem_assemble: F64 storage needs the FP64 precision"); return GBEM_EINVAL; }
+  const int m = sel ? surface_bfs(g, sel->nsa) : g->N, n = sel ? surface_bfs(g, sel->nsb) : g->N;
+  void* tmp = nullptr;
+  CHECK_CUDA(cudaMallocAsync(&tmp, (size_t)m * n * 16, s), "F64 assembly scratch");
+  BlockSel local;
+  if (sel) { local = *sel; local.row0 = 0; local.col0 = 0; }
+  st = assemble_device(g, wr, wi, eps, mu, GBEM_PREC_FP64, tmp, m, GBEM_C128, s, sel ? &local : nullptr);
+  if (st == GBEM_OK) {
+    double* d = (double*)dst + (sel ? (size_t)sel->row0 + (size_t)sel->col0 * ld : 0);
+    take_real<<<(unsigned)(((long long)m * n + 255) / 256), 256, 0, s>>>((const double2*)tmp, m, d, ld, m, n);
+    stats_launch(ST_OTHER);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) st = cuda_status(e, "take_real");
+  }
+  cudaFreeAsync(tmp, s);
+  return st;
+}
+
 gbem_status gbem_assemble(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
                           int precision, gbem_matrix* M) {
   if (!g || !M || !eps || !mu || M->N != g->N) { set_error("gbem_assemble: bad arguments"); return GBEM_EINVAL; }
-  if (omega_re == 0.0 && omega_im == 0.0) { set_error("gbem_assemble: Omega = 0 is not supported"); return GBEM_EINVAL; }
-  gbem_status st0 = ensure_stream(g);
-  if (st0 != GBEM_OK) return st0;
   M->factored = false;
-  return assemble_device(g, omega_re, omega_im, eps, mu, precision, M->d, M->ld, M->dtype, g->stream);
+  return assemble_into(g, omega_re, omega_im, eps, mu, precision, M->d, M->ld, M->dtype, nullptr);
+}
+
+gbem_status gbem_assemble_block(gbem_geometry* g, int nsa, int nsb, double omega_re, double omega_im,
+                                const double* eps, const double* mu, int precision, void* dst, int ld, int row0,
+                                int col0, int dtype) {
+  if (!g || !dst || !eps || !mu || nsa < 0 || nsb < 0 || nsa >= (int)g->S.size() || nsb >= (int)g->S.size() ||
+      row0 < 0 || col0 < 0 || ld < row0 + surface_bfs(g, nsa) ||
+      (dtype != GBEM_C128 && dtype != GBEM_C64 && dtype != GBEM_F64)) {
+    set_error("gbem_assemble_block: bad arguments");
+    return GBEM_EINVAL;
+  }
+  BlockSel sel{nsa, nsb, row0, col0};
+  return assemble_into(g, omega_re, omega_im, eps, mu, precision, dst, ld, dtype, &sel);
+}
+
+gbem_status gbem_assemble_block_host(gbem_geometry* g, int nsa, int nsb, double omega_re, double omega_im,
+                                     const double* eps, const double* mu, void* host, int ld, int row0, int col0,
+                                     int dtype) {
+  if (!g || !host || nsa < 0 || nsb < 0 || nsa >= (int)g->S.size() || nsb >= (int)g->S.size() ||
+      (dtype != GBEM_C128 && dtype != GBEM_F64) || row0 < 0 || col0 < 0 || ld < row0 + surface_bfs(g, nsa)) {
+    set_error("gbem_assemble_block_host: bad arguments (dtype C128 or F64)");
+    return GBEM_EINVAL;
+  }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  const int m = surface_bfs(g, nsa), n = surface_bfs(g, nsb);
+  const size_t es = dtype == GBEM_C128 ? 16 : 8;
+  void* d = nullptr;
+  CHECK_CUDA(cudaMallocAsync(&d, (size_t)m * n * es, g->stream), "block scratch");
+  st = gbem_assemble_block(g, nsa, nsb, omega_re, omega_im, eps, mu, GBEM_PREC_FP64, d, m, 0, 0, dtype);
+  if (st == GBEM_OK) {
+    cudaError_t e = cudaMemcpy2DAsync((char*)host + ((size_t)row0 + (size_t)col0 * ld) * es, (size_t)ld * es, d,
+                                      (size_t)m * es, (size_t)m * es, n, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) st = cuda_status(e, "block download");
+  }
+  cudaFreeAsync(d, g->stream);
+  cudaStreamSynchronize(g->stream);
+  return st;
 }
 
 gbem_status gbem_assemble_host(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
@@ -265,7 +346,24 @@ gbem_status gbem_lu_factor(gbem_matrix* M, int* ipiv, int* info) {
   if (!M) { set_error("gbem_lu_factor: NULL matrix"); return GBEM_EINVAL; }
   CHECK_CUDA(cudaSetDevice(M->g->device), "cudaSetDevice");
   int h_info = 0;
-  gbem_status st = lu_factor_device(M->d, M->N, M->ld, M->dtype, M->d_ipiv, &h_info, M->stream, &M->ws, &M->ws_bytes);
+  gbem_status st;
+  if (M->dtype == GBEM_F64) {
+    // real matrix (dgetrf semantics): factored as complex128 with zero
+    // imaginary parts, which stay exactly zero; |Re|+|Im| is then IDAMAX's |x|
+    const int N = M->N;
+    void* tmp = nullptr;
+    CHECK_CUDA(cudaMallocAsync(&tmp, (size_t)N * N * 16, M->stream), "F64 LU scratch");
+    const unsigned nb = (unsigned)(((long long)N * N + 255) / 256);
+    make_complex<<<nb, 256, 0, M->stream>>>((const double*)M->d, M->ld, (double2*)tmp, N, N, N);
+    st = lu_factor_device(tmp, N, N, GBEM_C128, M->d_ipiv, &h_info, M->stream, &M->ws, &M->ws_bytes);
+    if (st == GBEM_OK) take_real<<<nb, 256, 0, M->stream>>>((const double2*)tmp, N, (double*)M->d, M->ld, N, N);
+    stats_launch(ST_OTHER, 2);
+    cudaFreeAsync(tmp, M->stream);
+    cudaError_t e = cudaStreamSynchronize(M->stream);
+    if (st == GBEM_OK && e != cudaSuccess) st = cuda_status(e, "F64 LU");
+  } else {
+    st = lu_factor_device(M->d, M->N, M->ld, M->dtype, M->d_ipiv, &h_info, M->stream, &M->ws, &M->ws_bytes);
+  }
   if (st != GBEM_OK) return st;
   std::vector<int> piv(M->N), perm;
   CHECK_CUDA(cudaMemcpy(piv.data(), M->d_ipiv, sizeof(int) * M->N, cudaMemcpyDeviceToHost), "ipiv");
@@ -284,6 +382,35 @@ gbem_status gbem_lu_solve(gbem_matrix* M, char trans, int nrhs, void* B, int ldb
   if (!M || !B || nrhs <= 0 || ldb < M->N) { set_error("gbem_lu_solve: bad arguments"); return GBEM_EINVAL; }
   if (!M->factored) { set_error("gbem_lu_solve: matrix is not factored"); return GBEM_EINVAL; }
   CHECK_CUDA(cudaSetDevice(M->g->device), "cudaSetDevice");
+  if (M->dtype == GBEM_F64) {
+    // real factors: solved as complex128 with zero imaginary parts
+    const int N = M->N;
+    void *tA = nullptr, *dBr = nullptr, *dB = nullptr, *dY = nullptr;
+    cudaStream_t s = M->stream;
+    CHECK_CUDA(cudaMallocAsync(&tA, (size_t)N * N * 16, s), "solve alloc");
+    CHECK_CUDA(cudaMallocAsync(&dBr, (size_t)N * nrhs * 8, s), "solve alloc");
+    CHECK_CUDA(cudaMallocAsync(&dB, (size_t)N * nrhs * 16, s), "solve alloc");
+    CHECK_CUDA(cudaMallocAsync(&dY, (size_t)N * 8 * 16, s), "solve alloc");
+    CHECK_CUDA(cudaMemcpy2DAsync(dBr, (size_t)N * 8, B, (size_t)ldb * 8, (size_t)N * 8, nrhs, cudaMemcpyHostToDevice, s),
+               "solve upload");
+    make_complex<<<(unsigned)(((long long)N * N + 255) / 256), 256, 0, s>>>((const double*)M->d, M->ld, (double2*)tA, N,
+                                                                            N, N);
+    make_complex<<<(unsigned)(((long long)N * nrhs + 255) / 256), 256, 0, s>>>((const double*)dBr, N, (double2*)dB, N,
+                                                                               N, nrhs);
+    stats_launch(ST_OTHER, 3);
+    gbem_status st = lu_solve_device(tA, N, N, GBEM_C128, M->d_perm, trans, nrhs, dB, N, dY, s);
+    if (st == GBEM_OK) {
+      take_real<<<(unsigned)(((long long)N * nrhs + 255) / 256), 256, 0, s>>>((const double2*)dB, N, (double*)dBr, N, N,
+                                                                              nrhs);
+      cudaError_t e = cudaMemcpy2DAsync(B, (size_t)ldb * 8, dBr, (size_t)N * 8, (size_t)N * 8, nrhs,
+                                        cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) st = cuda_status(e, "solve download");
+    }
+    cudaFreeAsync(tA, s); cudaFreeAsync(dBr, s); cudaFreeAsync(dB, s); cudaFreeAsync(dY, s);
+    cudaStreamSynchronize(s);
+    return st;
+  }
   size_t es = esize(M->dtype);
   void *dB = nullptr, *dY = nullptr;
   CHECK_CUDA(cudaMallocAsync(&dB, (size_t)M->N * nrhs * es, M->stream), "solve alloc");

@@ -55,6 +55,7 @@ struct Block {
   std::vector<int2> tiles;             // (row block, col block)
   std::vector<NearPair> near;          // near pairs of this surface pair
   std::vector<int> near_ptr, near_col, near_idx;  // CSR over local row panel: (pb, pair index, transpose flag in sign)
+  double rmax_touch = 0.0;             // largest panel radius over the pairs with ncv = 1, 2
 };
 
 struct DevBlock;  // defined in assemble.cu
@@ -102,8 +103,13 @@ struct Matrix {
 gbem_status build_geometry(int ns, const gbem_surface_desc* d, int nreg, Geometry* g);
 
 // assemble.cu
+// block selection: only the (nsa, nsb) surface block, placed at (row0, col0)
+struct BlockSel {
+  int nsa, nsb, row0, col0;
+};
 gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps, const double* mu,
-                            int precision, void* dM, int ld, int dtype, cudaStream_t s);
+                            int precision, void* dM, int ld, int dtype, cudaStream_t s,
+                            const BlockSel* only = nullptr);
 gbem_status upload_geometry(Geometry* g);
 void free_geometry_device(Geometry* g);
 

@@ -180,6 +180,7 @@ static void near_pairs(const Surface& A, const Surface& B, bool sym, Block& blk,
             np.ncv = rr > 2.0 ? 0 : assess(Va, Vb, rmax, np.perm_a, np.perm_b);
             if (rr > 2.0) for (int i = 0; i < 3; i++) { np.perm_a[i] = (int8_t)i; np.perm_b[i] = (int8_t)i; }
             counts[np.ncv]++;
+            if (np.ncv == 1 || np.ncv == 2) blk.rmax_touch = std::max(blk.rmax_touch, rmax);
             blk.near.push_back(np);
           }
         }

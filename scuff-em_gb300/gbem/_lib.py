@@ -24,7 +24,7 @@ EXPORTS = [
     "gbem_matrix_device_ptr", "gbem_matrix_download", "gbem_matrix_upload", "gbem_assemble", "gbem_assemble_host",
     "gbem_lu_factor", "gbem_lu_solve", "gbem_lu_factor_host", "gbem_lu_solve_host", "gbem_solve_mixed",
     "gbem_rhs_planewave", "gbem_solve_mixed_device", "gbem_stats", "gbem_geometry_set_stream",
-    "gbem_lu_solve_noalloc",
+    "gbem_lu_solve_noalloc", "gbem_assemble_block", "gbem_assemble_block_host",
 ]
 
 
@@ -65,6 +65,8 @@ def lib():
             "gbem_solve_mixed_device": ([P, D, D, P, P, I, P, I, P, I, D, I, P, P], I),
             "gbem_stats": ([I, P, P], I), "gbem_geometry_set_stream": ([P, P], I),
             "gbem_lu_solve_noalloc": ([P, ctypes.c_char, I, P, I], I),
+            "gbem_assemble_block": ([P, I, I, D, D, P, P, I, P, I, I, I, I], I),
+            "gbem_assemble_block_host": ([P, I, I, D, D, P, P, P, I, I, I, I], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

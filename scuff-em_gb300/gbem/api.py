@@ -15,7 +15,7 @@ import re
 import numpy as np
 
 from . import _lib
-from ._lib import C128, C64, PREC_FP64, PREC_MIXED, check, lib
+from ._lib import C128, C64, F64, PREC_FP64, PREC_MIXED, check, lib
 from .mesh import read_msh
 
 ZVAC = 376.73031346177
@@ -77,7 +77,7 @@ class HMatrix:
 
     @property
     def np_dtype(self):
-        return np.complex128 if self.dtype == C128 else np.complex64
+        return {C128: np.complex128, C64: np.complex64, F64: np.float64}[self.dtype]
 
     def device_ptr(self):
         p, ld = ctypes.c_void_p(), ctypes.c_int()
@@ -208,6 +208,27 @@ class RWGGeometry:
         eps, mu = self.eps_mu(Omega)
         Omega = complex(Omega)
         check(lib().gbem_assemble(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data, prec, M._h))
+        return M
+
+    def NumBFs(self, ns):
+        """Basis functions of surface ns (edges, times 2 for a dielectric)."""
+        E, _ = self.edges(ns)
+        return E.shape[0] * (1 if self.surfaces[ns]["pec"] else 2)
+
+    def AssembleBEMMatrixBlock(self, nsa, nsb, Omega, M=None, RowOffset=0, ColOffset=0, real=False):
+        """The (nsa, nsb) surface block (AssembleBEMMatrix.cc:349-391) written
+        into the host array M (complex128, or float64 with real=True for the
+        reference's real storage at imaginary frequency) at (RowOffset,
+        ColOffset); allocates an NBF(nsa) x NBF(nsb) array if M is None."""
+        dt = F64 if real else C128
+        if M is None:
+            M = np.zeros((self.NumBFs(nsa), self.NumBFs(nsb)), dtype=np.float64 if real else np.complex128, order="F")
+        if not M.flags.f_contiguous:
+            raise ValueError("M must be column-major (Fortran order)")
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        check(lib().gbem_assemble_block_host(self._h, nsa, nsb, Omega.real, Omega.imag, eps.ctypes.data,
+                                             mu.ctypes.data, M.ctypes.data, M.shape[0], RowOffset, ColOffset, dt))
         return M
 
     def AssembleRHSVector(self, Omega, E0, nHat):

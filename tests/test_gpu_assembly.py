@@ -84,11 +84,70 @@ def test_larger_dielectric_against_oracle(ora):
     assert relerr(M, Mo) < 1e-11
 
 
-def test_short_wavelength_touching_pairs_report_enotsup(golden):
-    from gbem import GbemError, RWGGeometry
+def test_short_wavelength_touching_pairs(golden, ora):
+    """eps = 4+0.1i at kR = 12: |k r| > pi on the touching pairs, which take the
+    full-kernel Taylor-Duffy branch (PanelPanelInteractions.cc:449-491)."""
+    from gbem import RWGGeometry
     d = golden("ref_diel_s1_w12.npz")
+    gs, (regs, pec, eps, mu) = fixture_surfaces(d)
+    G = RWGGeometry(gs)
+    w = omega_of(d)
+    M = G.AssembleBEMMatrix(w).numpy()
+    Mo = ora.assemble([ora.Surface(s["V"], s["P"]) for s in gs], regs, pec, w, eps, mu)
+    assert np.array_equal(M, M.T)
+    assert relerr(M, Mo) < 1e-9, relerr(M, Mo)
+    # the reference caps its touching-pair cubature at 1000 evaluations
+    # (TaylorDuffy.cc:263-272): its entries carry ~1e-6 of the largest entry
+    assert relerr(M, d["M"]) < 2e-6, relerr(M, d["M"])
+    # FP32 far field: phases k r up to ~50 rad here keep ~50 * 2^-24 relative
+    M32 = G.AssembleBEMMatrix(w, precision="mixed").numpy()
+    assert np.abs(M32 - M).max() / np.abs(M).max() < 2e-5
+
+
+def test_block_assembly_matches_full_matrix(golden):
+    """AssembleBEMMatrixBlock: the four surface blocks of two PEC spheres at
+    imaginary frequency, at offsets inside a larger array, equal the
+    corresponding blocks of the full matrix; F64 blocks are its real part."""
+    from gbem import RWGGeometry
+    d = golden("ref_pec2_s1_xi.npz")
     gs, _ = fixture_surfaces(d)
     G = RWGGeometry(gs)
-    with pytest.raises(GbemError) as e:
-        G.AssembleBEMMatrix(omega_of(d))
-    assert "ENOTSUP" in str(e.value)
+    w = omega_of(d)
+    M = G.AssembleBEMMatrix(w).numpy()
+    n0, n1 = G.NumBFs(0), G.NumBFs(1)
+    off = [0, n0]
+    assert n0 + n1 == M.shape[0]
+    assert np.abs(M.imag).max() <= 1e-14 * np.abs(M).max()  # real at imaginary frequency
+    for a in range(2):
+        for b in range(2):
+            ref = M[off[a]:off[a] + G.NumBFs(a), off[b]:off[b] + G.NumBFs(b)]
+            big = np.zeros((G.NumBFs(a) + 5, G.NumBFs(b) + 3), dtype=np.complex128, order="F")
+            G.AssembleBEMMatrixBlock(a, b, w, big, RowOffset=5, ColOffset=3)
+            assert np.array_equal(big[5:, 3:], ref)
+            assert not big[:5].any() and not big[:, :3].any()
+            R = G.AssembleBEMMatrixBlock(a, b, w, real=True)
+            assert R.dtype == np.float64 and np.array_equal(R, ref.real)
+
+
+def test_f64_matrix_and_lu(golden):
+    """Real (F64) storage at imaginary frequency: the assembled matrix is the
+    real part of the C128 one and its LU matches LAPACK dgetrf's pivots."""
+    import scipy.linalg as sl
+    from gbem import RWGGeometry
+    from gbem.api import HMatrix
+    from gbem._lib import F64
+    d = golden("ref_pec2_s1_xi.npz")
+    gs, _ = fixture_surfaces(d)
+    G = RWGGeometry(gs)
+    w = omega_of(d)
+    M = G.AssembleBEMMatrix(w).numpy()
+    R = G.AssembleBEMMatrix(w, HMatrix(G, F64))
+    A = R.numpy()
+    assert A.dtype == np.float64 and np.array_equal(A, M.real)
+    assert R.LUFactorize() == 0
+    lu, piv = sl.lu_factor(A)
+    assert np.array_equal(R.ipiv - 1, piv)
+    assert np.abs(R.numpy() - lu).max() / np.abs(lu).max() < 1e-12
+    b = np.random.default_rng(5).standard_normal((A.shape[0], 2))
+    x = R.LUSolve(b)
+    assert np.abs(A @ x - b).max() / np.abs(b).max() < 1e-10

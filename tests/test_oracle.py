@@ -105,3 +105,15 @@ def test_matrix_against_reference(golden, case):
     # entries carry the reference's near-field quadrature error (<= ~1e-7 of
     # the largest entry); far-field entries agree to rounding
     assert err < 2e-7, err
+
+
+def test_matrix_short_wavelength_against_reference(golden):
+    """kR = 12, eps = 4+0.1i: touching pairs take Taylor-Duffy with the full
+    kernel; the reference caps that cubature at 1000 evaluations
+    (TaylorDuffy.cc:263-272), so its entries carry ~1e-6 of the largest."""
+    d = golden("ref_diel_s1_w12.npz")
+    surfs, regs, pec, eps, mu = _geometry(d)
+    w = d["omega"][0] + 1j * d["omega"][1]
+    M = ora.assemble(surfs, regs, pec, w, eps, mu)
+    err = np.abs(M - d["M"]).max() / np.abs(d["M"]).max()
+    assert err < 2e-6, err
