@@ -120,11 +120,27 @@ gbem_status gbem_assemble_host(gbem_geometry *g, double omega_re, double omega_i
  * of surface nsb's, written to the device array dst (column-major, leading
  * dimension ld) at (row0, col0).  dtype C128 or F64 with GBEM_PREC_FP64 (F64:
  * real storage, the reference's LHM_REAL at imaginary frequency, where the
- * block is real), C64 with GBEM_PREC_MIXED.  This entry produces no gradient
- * (GradM) or torque (dMdT) blocks. */
+ * block is real), C64 with GBEM_PREC_MIXED.  Gradient blocks (GradM) come
+ * from gbem_assemble_block_gradient; torque blocks (dMdT) are not provided. */
 gbem_status gbem_assemble_block(gbem_geometry *g, int nsa, int nsb, double omega_re, double omega_im,
                                 const double *eps, const double *mu, int precision, void *dst, int ld,
                                 int row0, int col0, int dtype);
+/* The gradient blocks GradM[mu] = dM/dx_mu of the (nsa, nsb) block under a
+ * rigid displacement of surface nsa (AssembleBEMMatrixBlock's GradM,
+ * AssembleBEMMatrix.cc:349-391 with PanelPanelInteractions.cc:166-181):
+ * device arrays gx, gy, gz (any may be NULL to skip that component), same
+ * layout as gbem_assemble_block; FP64, dtype C128 or F64.  Far pairs use the
+ * 6x6 rule, near pairs a high-order rule without desingularisation, and
+ * pairs on the Taylor-Duffy branch contribute zero, as in the reference. */
+gbem_status gbem_assemble_block_gradient(gbem_geometry *g, int nsa, int nsb, double omega_re,
+                                         double omega_im, const double *eps, const double *mu,
+                                         void *gx, void *gy, void *gz, int ld, int row0, int col0,
+                                         int dtype);
+/* Host-buffer variant of gbem_assemble_block_gradient. */
+gbem_status gbem_assemble_block_gradient_host(gbem_geometry *g, int nsa, int nsb, double omega_re,
+                                              double omega_im, const double *eps, const double *mu,
+                                              void *gx, void *gy, void *gz, int ld, int row0, int col0,
+                                              int dtype);
 /* Host-buffer variant of gbem_assemble_block (FP64; dtype C128 or F64): fills
  * rows row0.. and columns col0.. of the host column-major array host. */
 gbem_status gbem_assemble_block_host(gbem_geometry *g, int nsa, int nsb, double omega_re, double omega_im,
@@ -202,6 +218,19 @@ gbem_status gbem_solve_mixed_device(gbem_geometry *g, double omega_re, double om
  * [7] reserved; then resets them.  enable != 0 turns event timing on for
  * subsequent calls (launch counts are always kept). */
 gbem_status gbem_stats(int enable, double ms[8], long long counts[8]);
+
+/* ---- power (EMT) ------------------------------------------------------------ */
+/* Scattered and extinguished power of nrhs solutions (the EMT method of
+ * GetPFT, EMTPFT.cc:468-700; absorbed power = extinction - scattered).  KN:
+ * host N x nrhs complex128 solution vectors in the reference's layout (K and
+ * -N/ZVAC interleaved on dielectric surfaces); rhs (optional, for pext): the
+ * matching plane-wave right-hand sides.  P_scat is a quadratic form of K, N
+ * with the exterior region's own matrix, assembled here with `precision`.
+ * Every surface must face region 0; nrhs <= 8.  Powers in the reference's
+ * units (W for |E0| = 1 V/um). */
+gbem_status gbem_power_emt(gbem_geometry *g, double omega_re, double omega_im, const double *eps,
+                           const double *mu, int precision, int nrhs, const double *KN, int ldkn,
+                           const double *rhs, int ldr, double *pscat, double *pext);
 
 /* ---- right-hand sides ----------------------------------------------------- */
 /* Plane-wave right-hand side (AssembleRHSVector.cc:145-255 with a PlaneWave

@@ -790,6 +790,23 @@ static void ora_eei(const ora_surface *Sa, int ea, const ora_surface *Sb, int eb
   GC[1] = C * (HPP[1] - HPM[1] - HMP[1] + HMM[1]);
 }
 
+/* GC[0], GC[1] (EdgeEdgeInteractions.cc:183-188) of every edge pair of one
+   surface at wavenumber k: the ingredients of the EMT power integrals
+   (EMTPFT.cc:333-352 with GetGCMatrixElements). */
+void ora_gc_matrix(const ora_surface *S, double kr, double ki, double *GC0, double *GC1)
+{
+  const int ne = S->ne;
+  const cplx k = kr + I*ki;
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int ea = 0; ea < ne; ea++)
+    for (int eb = 0; eb < ne; eb++) {
+      cplx GC[2];
+      ora_eei(S, ea, S, eb, k, GC);
+      GC0[2*(ea + (size_t)eb*ne)] = creal(GC[0]); GC0[2*(ea + (size_t)eb*ne) + 1] = cimag(GC[0]);
+      GC1[2*(ea + (size_t)eb*ne)] = creal(GC[1]); GC1[2*(ea + (size_t)eb*ne) + 1] = cimag(GC[1]);
+    }
+}
+
 static cplx csqrt2(cplx z) { cplx r = csqrt(z); return cimag(r) < 0 ? -r : r; }
 
 /* ------------------------------------------------------------------ */

@@ -59,6 +59,7 @@ def lib():
         L.ora_qifippi_c.argtypes = [P, I, I, I, P, P]
         L.ora_set_orders.argtypes = [I, I, I, I, I]
         L.ora_assemble.argtypes = [I, P, P, P, D, D, P, P, P, I]
+        L.ora_gc_matrix.argtypes = [P, D, D, P, P]
         _lib = L
     return _lib
 
@@ -93,6 +94,43 @@ class Surface:
         order = np.zeros(6, dtype=np.int32)
         ncv = lib().ora_qifippi_c(self.h, pa, pb, n, out.ctypes.data, order.ctypes.data)
         return out, ncv, order
+
+
+def gc_matrices(surface, k):
+    """GC[0], GC[1] of every edge pair of one surface at wavenumber k
+    (EdgeEdgeInteractions.cc:183-188), as two ne x ne complex arrays."""
+    k = complex(k)
+    ne = lib().ora_surface_num_edges(surface.h)
+    g0 = np.zeros((ne, ne), dtype=np.complex128, order="F")
+    g1 = np.zeros((ne, ne), dtype=np.complex128, order="F")
+    lib().ora_gc_matrix(surface.h, k.real, k.imag, g0.ctypes.data, g1.ctypes.data)
+    return g0, g1
+
+
+ZVAC = 376.73031346177
+
+
+def emt_pscat(surface, pec, omega, KN, eps0=1.0, mu0=1.0):
+    """EMT scattered power of one surface in the exterior region
+    (EMTPFT.cc:642-700, self-surface branch): with QKK = mu w GC0,
+    QNN = eps w GC0 and ikC = i k GC1 (GetScatteredPFTIntegrals,
+    EMTPFT.cc:333-352),  P = 1/2 sum_ab [ZVAC Re(K_a* K_b) Im QKK
+    + Re(N_a* N_b)/ZVAC Im QNN + Im(K_a* N_b - N_a* K_b) Im ikC],
+    K and N = -ZVAC * KN[odd] as in RWGGeometry::GetKNCoefficients."""
+    omega = complex(omega)
+    k0 = np.sqrt(complex(eps0) * complex(mu0)) * omega
+    g0, g1 = gc_matrices(surface, k0)
+    KN = np.asarray(KN)
+    if pec:
+        K, N = KN, np.zeros_like(KN)
+    else:
+        K, N = KN[0::2], -ZVAC * KN[1::2]
+    re = lambda a, b: np.real(np.conj(a)[:, None] * b[None, :])
+    im = lambda a, b: np.imag(np.conj(a)[:, None] * b[None, :])
+    p = ZVAC * np.sum(re(K, K) * np.imag(mu0 * omega * g0))
+    p += np.sum(re(N, N) * np.imag(eps0 * omega * g0)) / ZVAC
+    p += np.sum((im(K, N) - im(N, K)) * np.imag(1j * k0 * g1))
+    return 0.5 * p
 
 
 def assemble(surfaces, regions, pec, omega, eps, mu):

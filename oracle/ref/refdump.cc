@@ -11,6 +11,8 @@
 //   refdump rhs    GEO wr wi E0x E0y E0z nx ny nz OUT   plane-wave RHS (int32 N, N complex128)
 //   refdump pft    GEO wr wi E0x E0y E0z nx ny nz OUT   assemble, LU, solve, EMT power; KN vector
 //   refdump time   GEO wr wi NREP            wall time of AssembleBEMMatrix, LUFactorize, LUSolve
+//   refdump gradblock GEO wr wi nsa nsb OUT  block (nsa,nsb) and its three gradients d/dx_mu
+//                                            (per matrix: int32 NR NC, then NR*NC complex128 column-major)
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -39,6 +41,18 @@ static void write_matrix(const char *fn, HMatrix *M) {
       fwrite(d, sizeof(double), 2, f);
     }
   fclose(f);
+}
+
+static void append_rect(FILE *f, HMatrix *M) {
+  int nr = M->NR, nc = M->NC;
+  fwrite(&nr, sizeof(int), 1, f);
+  fwrite(&nc, sizeof(int), 1, f);
+  for (int c = 0; c < nc; c++)
+    for (int r = 0; r < nr; r++) {
+      cdouble z = M->GetEntry(r, c);
+      double d[2] = {real(z), imag(z)};
+      fwrite(d, sizeof(double), 2, f);
+    }
 }
 
 static void write_vector(const char *fn, HVector *V) {
@@ -185,6 +199,23 @@ int main(int argc, char **argv) {
     }
     printf("N %d threads %d assemble_cold %.6f assemble_warm %.6f lu %.6f solve1 %.6f\n", G->TotalBFs,
            omp_get_max_threads(), tcold, twarm, tlu, tsolve);
+    return 0;
+  }
+
+  if (!strcmp(cmd, "gradblock")) {
+    cdouble Omega(atof(argv[3]), atof(argv[4]));
+    int nsa = atoi(argv[5]), nsb = atoi(argv[6]);
+    int NR = G->Surfaces[nsa]->NumBFs, NC = G->Surfaces[nsb]->NumBFs;
+    HMatrix *M = new HMatrix(NR, NC, LHM_COMPLEX);
+    HMatrix *GradM[3];
+    for (int mu = 0; mu < 3; mu++) GradM[mu] = new HMatrix(NR, NC, LHM_COMPLEX);
+    M->Zero();
+    for (int mu = 0; mu < 3; mu++) GradM[mu]->Zero();
+    G->AssembleBEMMatrixBlock(nsa, nsb, Omega, 0, M, GradM, 0, 0);
+    FILE *f = fopen(argv[7], "wb");
+    append_rect(f, M);
+    for (int mu = 0; mu < 3; mu++) append_rect(f, GradM[mu]);
+    fclose(f);
     return 0;
   }
 

@@ -708,8 +708,36 @@ gbem_status compute_fippi(Geometry* g, cudaStream_t s) {
   return GBEM_OK;
 }
 
+// per-region wavenumbers and PMCHWT/EFIE prefactors of a surface block
+// (SurfaceSurfaceInteractions.cc:165-176), signs folded in
+static RegionArgs region_args(const Block& b, double wr, double wi, const double* eps, const double* mu) {
+  RegionArgs ra;
+  memset(&ra, 0, sizeof ra);
+  ra.nreg = b.nreg;
+  const cx<double> omega = cxd(wr, wi);
+  for (int r = 0; r < b.nreg; r++) {
+    int R = b.reg[r];
+    cx<double> ep = cxd(eps[2 * R], eps[2 * R + 1]), m = cxd(mu[2 * R], mu[2 * R + 1]);
+    // k = csqrt2(eps mu) omega, the root with Im >= 0 (libhrutil.cc:692-699)
+    cx<double> em = ep * m;
+    double rr = std::sqrt(std::hypot(em.re, em.im));
+    double th = 0.5 * std::atan2(em.im, em.re);
+    cx<double> rt = cxd(rr * std::cos(th), rr * std::sin(th));
+    if (rt.im < 0) rt = cxd(-rt.re, -rt.im);
+    cx<double> k = rt * omega;
+    ra.k[r] = k;
+    cx<double> I = cxd(0.0, 1.0);
+    double sg = b.sign[r];
+    ra.pf1[r] = sg * (I * m * omega);
+    cx<double> pf2 = (-sg) * (I * k);
+    ra.pfc[r] = (k.re == 0.0 && k.im == 0.0) ? cxd(0.0, 0.0) : cdiv(pf2, I * k);
+    ra.pf3[r] = (-sg) * (I * ep * omega);
+  }
+  return ra;
+}
+
 gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int precision,
-                            void* dM, int ld, int dtype, cudaStream_t s, const BlockSel* only) {
+                            void* dM, int ld, int dtype, cudaStream_t s, const BlockSel* only, int only_region) {
   if ((precision == GBEM_PREC_FP64 && dtype != GBEM_C128) || (precision == GBEM_PREC_MIXED && dtype != GBEM_C64)) {
     set_error("gbem_assemble: matrix dtype does not match the precision (C128 for FP64, C64 for MIXED)");
     return GBEM_EINVAL;
@@ -720,7 +748,7 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
     st = compute_fippi(g, s);
     if (st != GBEM_OK) return st;
   }
-  bool any_empty = false;
+  bool any_empty = only_region >= 0;  // a single region leaves blocks without it at zero
   for (const Block& b : g->blocks)
     if (!only || (b.sa == std::min(only->nsa, only->nsb) && b.sb == std::max(only->nsa, only->nsb)))
       any_empty |= (b.nreg == 0);
@@ -742,32 +770,29 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
   cudaError_t e = cudaMallocAsync((void**)&d_status, sizeof(int), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
   if (e != cudaSuccess) return cuda_status(e, "status word");
-  cx<double> omega = cxd(wr, wi);
   for (size_t bi = 0; bi < g->blocks.size(); bi++) {
     const Block& b = g->blocks[bi];
     DevBlock* db = g->dblocks[bi];
     if (b.nreg == 0) continue;
     if (only && !(b.sa == std::min(only->nsa, only->nsb) && b.sb == std::max(only->nsa, only->nsb))) continue;
-    RegionArgs ra;
-    memset(&ra, 0, sizeof ra);
-    ra.nreg = b.nreg;
-    for (int r = 0; r < b.nreg; r++) {
-      int R = b.reg[r];
-      cx<double> ep = cxd(eps[2 * R], eps[2 * R + 1]), m = cxd(mu[2 * R], mu[2 * R + 1]);
-      // k = csqrt2(eps mu) omega, the root with Im >= 0 (libhrutil.cc:692-699)
-      cx<double> em = ep * m;
-      double rr = std::sqrt(std::hypot(em.re, em.im));
-      double th = 0.5 * std::atan2(em.im, em.re);
-      cx<double> rt = cxd(rr * std::cos(th), rr * std::sin(th));
-      if (rt.im < 0) rt = cxd(-rt.re, -rt.im);
-      cx<double> k = rt * omega;
-      ra.k[r] = k;
-      cx<double> I = cxd(0.0, 1.0);
-      double sg = b.sign[r];
-      ra.pf1[r] = sg * (I * m * omega);
-      cx<double> pf2 = (-sg) * (I * k);
-      ra.pfc[r] = (k.re == 0.0 && k.im == 0.0) ? cxd(0.0, 0.0) : cdiv(pf2, I * k);
-      ra.pf3[r] = (-sg) * (I * ep * omega);
+    RegionArgs ra = region_args(b, wr, wi, eps, mu);
+    if (only_region >= 0) {
+      // one region's contribution with the sign of an exterior region:
+      // KK = i mu w GC0, KN = NK = -i k GC1, NN = -i eps w GC0
+      RegionArgs rb;
+      memset(&rb, 0, sizeof rb);
+      for (int r = 0; r < ra.nreg; r++) {
+        if (b.reg[r] != only_region) continue;
+        const int R = b.reg[r];
+        const cx<double> I = cxd(0.0, 1.0), w = cxd(wr, wi);
+        rb.k[0] = ra.k[r];
+        rb.pf1[0] = I * cxd(mu[2 * R], mu[2 * R + 1]) * w;
+        rb.pfc[0] = cxd(-1.0, 0.0);
+        rb.pf3[0] = (-1.0) * (I * cxd(eps[2 * R], eps[2 * R + 1]) * w);
+        rb.nreg = 1;
+      }
+      if (rb.nreg == 0) continue;
+      ra = rb;
     }
     {
       StatTimer tn(ST_NEAR, s);
@@ -837,6 +862,203 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
     return GBEM_ENOTSUP;
   }
   return GBEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Gradient blocks dM/dx_mu of one surface block (AssembleBEMMatrixBlock with
+// GradM, the scuff-cas3D force path): one thread per edge pair, the four
+// panel pairs integrated directly with the reference's gradient integrand
+// (PanelPanelInteractions.cc:166-181):
+//   GradH[2mu]   = int int R_mu hPlus Psi,
+//   GradH[2mu+1] = int int (R_mu hTimes Zeta + (F x F')_mu Psi),
+// hPlus = F.F' - 4/k^2, hTimes = (F x F').R, Zeta = Phi (-k^2 - 3ik/r + 3/r^2)/r^2.
+// Rules as the reference chooses them: far pairs (rRel > 4) the 6x6 rule;
+// near pairs the high-order rule without desingularisation; pairs that take
+// the Taylor-Duffy branch (ncv = 3, or ncv > 0 when |k r| > pi) contribute
+// zero (PanelPanelInteractions.cc:488).  Stamped like GC (GradGC[1] carries
+// the 1/(ik) of GC[1]).
+// ---------------------------------------------------------------------------
+struct GradArgs {
+  const double* V;   // vertices of both surfaces' panels: global panel vertex table (9 per panel)
+  const double* pc;  // centroid + radius per global panel
+  const int* Ea;     // 8 ints per edge of surface a
+  const int* Eb;
+  const double* La;  // edge lengths
+  const double* Lb;
+  int nea, neb, poff_a, poff_b;  // edges; first global panel index of each surface
+  const double* Va;  // vertex arrays of the two surfaces (for the Q vertices)
+  const double* Vb;
+  int bpe_a, bpe_b;
+  int row0, col0;
+  long long ld;
+  void* out[3];
+};
+
+__device__ void ppi_grad(const double* Pa, const double* Qa, const double* Pb, const double* Qb, cx<double> k,
+                         const double* rule, int npts, cx<double>* GH) {
+  const double inv4pi = 0.079577471545947667884;
+  const cx<double> ik = mk(-k.im, k.re), ik2 = ik * ik, m4 = cdiv(mk(4.0, 0.0), ik2);
+  double A[3], B[3], Ap[3], Bp[3];
+  for (int c = 0; c < 3; c++) {
+    A[c] = Pa[3 + c] - Pa[c]; B[c] = Pa[6 + c] - Pa[c];
+    Ap[c] = Pb[3 + c] - Pb[c]; Bp[c] = Pb[6 + c] - Pb[c];
+  }
+  for (int m = 0; m < 6; m++) GH[m] = mk(0.0, 0.0);
+  for (int i = 0; i < npts; i++) {
+    const double u = rule[3 * i], v = rule[3 * i + 1], wi = rule[3 * i + 2];
+    double x[3], F[3];
+    for (int c = 0; c < 3; c++) { x[c] = Pa[c] + u * A[c] + v * B[c]; F[c] = x[c] - Qa[c]; }
+    for (int j = 0; j < npts; j++) {
+      const double up = rule[3 * j], vp = rule[3 * j + 1], wj = rule[3 * j + 2];
+      double xp[3], Fp[3], R[3];
+      for (int c = 0; c < 3; c++) {
+        xp[c] = Pb[c] + up * Ap[c] + vp * Bp[c];
+        Fp[c] = xp[c] - Qb[c];
+        R[c] = x[c] - xp[c];
+      }
+      const double r2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2], r = sqrt(r2), ri = 1.0 / r;
+      double sn, cs;
+      sincos(k.re * r, &sn, &cs);
+      const double amp = wi * wj * inv4pi * ri * exp(-k.im * r);
+      const cx<double> Phi = mk(amp * cs, amp * sn);
+      const cx<double> Psi = Phi * mk(ik.re - ri, ik.im) * mk(ri, 0.0);
+      const cx<double> Zeta = Phi * (ik2 - mk(3.0 * ri, 0.0) * ik + mk(3.0 * ri * ri, 0.0)) * mk(ri * ri, 0.0);
+      const cx<double> hPlus = mk(F[0] * Fp[0] + F[1] * Fp[1] + F[2] * Fp[2], 0.0) + m4;
+      double X[3];
+      vcross(F, Fp, X);
+      const double hT = X[0] * R[0] + X[1] * R[1] + X[2] * R[2];
+      const cx<double> hPsi = hPlus * Psi;
+      const cx<double> hZ = hT * Zeta;
+      for (int mu = 0; mu < 3; mu++) {
+        GH[2 * mu] = GH[2 * mu] + R[mu] * hPsi;
+        GH[2 * mu + 1] = GH[2 * mu + 1] + R[mu] * hZ + X[mu] * Psi;
+      }
+    }
+  }
+}
+
+template <bool REAL>
+__global__ void __launch_bounds__(128) grad_kernel(GradArgs a, RegionArgs ra) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)a.nea * a.neb) return;
+  const int ea = (int)(t % a.nea), eb = (int)(t / a.nea);
+  const int* EA = a.Ea + 8 * ea;
+  const int* EB = a.Eb + 8 * eb;
+  const double La = a.La[ea], Lb = a.Lb[eb];
+  cx<double> acc[3][4];
+  for (int mu = 0; mu < 3; mu++)
+    for (int c = 0; c < 4; c++) acc[mu][c] = mk(0.0, 0.0);
+  for (int r = 0; r < ra.nreg; r++) {
+    const cx<double> k = ra.k[r];
+    if (k.re == 0.0 && k.im == 0.0) continue;
+    cx<double> S0[3], S1[3];
+    for (int mu = 0; mu < 3; mu++) { S0[mu] = mk(0.0, 0.0); S1[mu] = mk(0.0, 0.0); }
+    for (int sa = 0; sa < 2; sa++) {
+      const int iqa = sa == 0 ? EA[2] : EA[3];
+      const int pa = sa == 0 ? EA[4] : EA[5];
+      if (iqa < 0 || pa < 0) continue;
+      for (int sb = 0; sb < 2; sb++) {
+        const int iqb = sb == 0 ? EB[2] : EB[3];
+        const int pb = sb == 0 ? EB[4] : EB[5];
+        if (iqb < 0 || pb < 0) continue;
+        const int gpa = a.poff_a + pa, gpb = a.poff_b + pb;
+        const double* Pa = a.V + 9 * (size_t)gpa;
+        const double* Pb = a.V + 9 * (size_t)gpb;
+        const double* ca = a.pc + 4 * (size_t)gpa;
+        const double* cb = a.pc + 4 * (size_t)gpb;
+        const double rmax = fmax(ca[3], cb[3]);
+        const double dx = ca[0] - cb[0], dy = ca[1] - cb[1], dz = ca[2] - cb[2];
+        const bool far = sqrt(dx * dx + dy * dy + dz * dz) > 4.0 * rmax;
+        cx<double> GH[6];
+        if (far) {
+          ppi_grad(Pa, a.Va + 3 * iqa, Pb, a.Vb + 3 * iqb, k, c_lo64, 6, GH);
+        } else {
+          int ncv = 0;
+          for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+              const double ex = Pa[3 * i] - Pb[3 * j], ey = Pa[3 * i + 1] - Pb[3 * j + 1], ez = Pa[3 * i + 2] - Pb[3 * j + 2];
+              if (sqrt(ex * ex + ey * ey + ez * ez) < 1e-6 * rmax) ncv++;
+            }
+          const bool swr = hypot(k.re * rmax, k.im * rmax) > M_PI;
+          if (ncv == 3 || (ncv > 0 && swr)) continue;  // Taylor-Duffy pairs: zero gradient
+          ppi_grad(Pa, a.Va + 3 * iqa, Pb, a.Vb + 3 * iqb, k, c_ho, HO_N * HO_N, GH);
+        }
+        const double sg = (sa == sb) ? 1.0 : -1.0;
+        for (int mu = 0; mu < 3; mu++) {
+          S0[mu] = S0[mu] + sg * GH[2 * mu];
+          S1[mu] = S1[mu] + sg * GH[2 * mu + 1];
+        }
+      }
+    }
+    const double LL = La * Lb;
+    for (int mu = 0; mu < 3; mu++) {
+      const cx<double> g0 = LL * S0[mu], g1 = LL * S1[mu];
+      acc[mu][0] = acc[mu][0] + ra.pf1[r] * g0;
+      acc[mu][1] = acc[mu][1] + ra.pfc[r] * g1;
+      acc[mu][3] = acc[mu][3] + ra.pf3[r] * g0;
+    }
+  }
+  const long long X = a.row0 + (long long)a.bpe_a * ea, Y = a.col0 + (long long)a.bpe_b * eb;
+  for (int mu = 0; mu < 3; mu++) {
+    if (!a.out[mu]) continue;
+    // (K,K) = PF1 G0; (K,N) = (N,K) = PF2 G1 / (ik); (N,N) = PF3 G0
+    cx<double> e[2][2] = {{acc[mu][0], acc[mu][1]}, {acc[mu][1], acc[mu][3]}};
+    for (int dx = 0; dx < a.bpe_a; dx++)
+      for (int dy = 0; dy < a.bpe_b; dy++) {
+        const long long idx = (X + dx) + (Y + dy) * a.ld;
+        if (REAL) ((double*)a.out[mu])[idx] = e[dx][dy].re;
+        else ((cx<double>*)a.out[mu])[idx] = e[dx][dy];
+      }
+  }
+}
+
+gbem_status assemble_gradient_device(Geometry* g, double wr, double wi, const double* eps, const double* mu,
+                                     const BlockSel& sel, void* const out[3], int ld, int dtype, cudaStream_t s) {
+  gbem_status st = upload_geometry(g);
+  if (st != GBEM_OK) return st;
+  const int lo = std::min(sel.nsa, sel.nsb), hi = std::max(sel.nsa, sel.nsb);
+  const Block* bp = nullptr;
+  for (const Block& b : g->blocks)
+    if (b.sa == lo && b.sb == hi) bp = &b;
+  if (!bp) { set_error("gradient: no such surface block"); return GBEM_EINVAL; }
+  const Surface& A = g->S[sel.nsa];
+  const Surface& B = g->S[sel.nsb];
+  const size_t es = dtype == GBEM_F64 ? 8 : 16;
+  cudaError_t e = cudaSuccess;
+  // the block's entries are written by one thread each; a block of surfaces
+  // that share no region is zero
+  for (int m = 0; m < 3 && e == cudaSuccess; m++)
+    if (out[m])
+      e = cudaMemset2DAsync((char*)out[m] + ((size_t)sel.row0 + (size_t)sel.col0 * ld) * es, (size_t)ld * es, 0,
+                            (size_t)A.ne * (A.pec ? 1 : 2) * es, B.ne * (B.pec ? 1 : 2), s);
+  if (e != cudaSuccess) return cuda_status(e, "gradient memset");
+  if (bp->nreg == 0 || A.ne == 0 || B.ne == 0) return GBEM_OK;
+  double *dVa = nullptr, *dVb = nullptr, *dLa = nullptr, *dLb = nullptr;
+  int *dEa = nullptr, *dEb = nullptr;
+  e = dupload(&dVa, A.V.data(), A.V.size());
+  if (e == cudaSuccess) e = dupload(&dVb, B.V.data(), B.V.size());
+  if (e == cudaSuccess) e = dupload(&dEa, A.E.data(), A.E.size());
+  if (e == cudaSuccess) e = dupload(&dEb, B.E.data(), B.E.size());
+  if (e == cudaSuccess) e = dupload(&dLa, A.elen.data(), A.elen.size());
+  if (e == cudaSuccess) e = dupload(&dLb, B.elen.data(), B.elen.size());
+  if (e == cudaSuccess) {
+    GradArgs ga;
+    ga.V = g->d_pv; ga.pc = g->d_pc; ga.Ea = dEa; ga.Eb = dEb; ga.La = dLa; ga.Lb = dLb;
+    ga.nea = A.ne; ga.neb = B.ne; ga.poff_a = A.panel_offset; ga.poff_b = B.panel_offset;
+    ga.Va = dVa; ga.Vb = dVb;
+    ga.bpe_a = A.pec ? 1 : 2; ga.bpe_b = B.pec ? 1 : 2;
+    ga.row0 = sel.row0; ga.col0 = sel.col0; ga.ld = ld;
+    for (int m = 0; m < 3; m++) ga.out[m] = out[m];
+    const RegionArgs ra = region_args(*bp, wr, wi, eps, mu);
+    const long long n = (long long)A.ne * B.ne;
+    stats_launch(ST_OTHER);
+    if (dtype == GBEM_F64) grad_kernel<true><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(ga, ra);
+    else grad_kernel<false><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(ga, ra);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  cudaFree(dVa); cudaFree(dVb); cudaFree(dEa); cudaFree(dEb); cudaFree(dLa); cudaFree(dLb);
+  return cuda_status(e, "gradient block");
 }
 
 // ---------------------------------------------------------------------------

@@ -90,6 +90,54 @@ struct gbem_matrix : public Matrix {
     if (e_ != cudaSuccess) return cuda_status(e_, what); \
   } while (0)
 
+// EMT scattered power (EMTPFT.cc:642-700 for the scattered part): with M0 the
+// matrix of the exterior region alone (KK = i mu w GC0, KN = NK = -i k GC1,
+// NN = -i eps w GC0) and the physical coefficients K and N = -ZVAC * (odd
+// entries of the KN vector, RWGGeometry.cc:957-979),
+//   P_scat = 1/2 sum_ij [ ZVAC Re(K_i* K_j)(-Re M0_ij) + Re(N_i* N_j) Re(M0_ij)/ZVAC
+//                         + Im(K_i* N_j)(-Im M0_ij) + Im(N_i* K_j) Im(M0_ij) ].
+// One thread per row, columns in chunks; partial sums per (row block, chunk).
+template <typename TM>
+static __global__ void emt_quadform(const cx<TM>* M, long long ld, int N, const signed char* type, const cx<double>* X,
+                                    long long ldx, int nrhs, int cchunk, double* part) {
+  const double ZV = 376.73031346177;
+  __shared__ double red[8][128];
+  const int i = blockIdx.x * 128 + threadIdx.x;
+  const int c0 = blockIdx.y * cchunk, c1 = min(N, c0 + cchunk);
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (i < N) {
+    const int ti = type[i];
+    for (int j = c0; j < c1; j++) {
+      const cx<TM> m = M[i + (long long)j * ld];
+      const double mr = (double)m.re, mi = (double)m.im;
+      const int tj = type[j];
+      for (int r = 0; r < nrhs; r++) {
+        cx<double> ci = X[i + (long long)r * ldx], cj = X[j + (long long)r * ldx];
+        if (ti) ci = (-ZV) * ci;
+        if (tj) cj = (-ZV) * cj;
+        const double re = ci.re * cj.re + ci.im * cj.im, im = ci.re * cj.im - ci.im * cj.re;  // conj(ci) cj
+        double t;
+        if (!ti && !tj) t = -ZV * re * mr;
+        else if (ti && tj) t = re * mr / ZV;
+        else if (!ti) t = -im * mi;
+        else t = im * mi;
+        acc[r] += t;
+      }
+    }
+  }
+  for (int r = 0; r < nrhs; r++) {
+    red[r][threadIdx.x] = acc[r];
+  }
+  __syncthreads();
+  for (int o = 64; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int r = 0; r < nrhs; r++) red[r][threadIdx.x] += red[r][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int r = 0; r < nrhs; r++) part[((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 8 + r] = red[r][0];
+}
+
 extern "C" {
 
 const char* gbem_last_error(void) { return g_err; }
@@ -302,6 +350,123 @@ gbem_status gbem_assemble_block(gbem_geometry* g, int nsa, int nsb, double omega
   }
   BlockSel sel{nsa, nsb, row0, col0};
   return assemble_into(g, omega_re, omega_im, eps, mu, precision, dst, ld, dtype, &sel);
+}
+
+gbem_status gbem_power_emt(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
+                           int precision, int nrhs, const double* KN, int ldkn, const double* rhs, int ldr,
+                           double* pscat, double* pext) {
+  if (!g || !eps || !mu || !KN || !pscat || nrhs <= 0 || nrhs > 8 || ldkn < g->N || (rhs && ldr < g->N)) {
+    set_error("gbem_power_emt: bad arguments (1 <= nrhs <= 8)");
+    return GBEM_EINVAL;
+  }
+  for (const Surface& S : g->S)
+    if (S.reg_ext != 0) {
+      set_error("gbem_power_emt: every surface must face the exterior region 0 (nested bodies are not supported)");
+      return GBEM_ENOTSUP;
+    }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  const int N = g->N;
+  cudaStream_t s = g->stream;
+  const int dtype = precision == GBEM_PREC_MIXED ? GBEM_C64 : GBEM_C128;
+  std::vector<signed char> type(N);
+  for (const Surface& S : g->S)
+    for (int e = 0; e < S.ne; e++) {
+      if (S.pec) type[S.bf_offset + e] = 0;
+      else { type[S.bf_offset + 2 * e] = 0; type[S.bf_offset + 2 * e + 1] = 1; }
+    }
+  const int nsplit = 8, cchunk = (N + nsplit - 1) / nsplit, nb = (N + 127) / 128;
+  void *dM = nullptr, *dX = nullptr, *dT = nullptr, *dP = nullptr;
+  cudaError_t e = cudaMallocAsync(&dM, (size_t)N * N * (dtype == GBEM_C64 ? 8 : 16), s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dX, (size_t)N * nrhs * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dT, (size_t)N, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dP, sizeof(double) * 8 * nb * nsplit, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dX, (size_t)N * 16, KN, (size_t)ldkn * 16, (size_t)N * 16, nrhs, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dT, type.data(), N, cudaMemcpyHostToDevice, s);
+  st = cuda_status(e, "gbem_power_emt setup");
+  if (st == GBEM_OK) st = assemble_device(g, omega_re, omega_im, eps, mu, precision, dM, N, dtype, s, nullptr, 0);
+  std::vector<double> part((size_t)8 * nb * nsplit);
+  if (st == GBEM_OK) {
+    dim3 grid(nb, nsplit);
+    if (dtype == GBEM_C64)
+      emt_quadform<float><<<grid, 128, 0, s>>>((const cx<float>*)dM, N, N, (const signed char*)dT, (const cx<double>*)dX,
+                                                N, nrhs, cchunk, (double*)dP);
+    else
+      emt_quadform<double><<<grid, 128, 0, s>>>((const cx<double>*)dM, N, N, (const signed char*)dT,
+                                                 (const cx<double>*)dX, N, nrhs, cchunk, (double*)dP);
+    stats_launch(ST_OTHER);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(part.data(), dP, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    st = cuda_status(e, "gbem_power_emt");
+  }
+  cudaFreeAsync(dM, s); cudaFreeAsync(dX, s); cudaFreeAsync(dT, s); cudaFreeAsync(dP, s);
+  cudaStreamSynchronize(s);
+  if (st != GBEM_OK) return st;
+  const double ZV = 376.73031346177;
+  for (int r = 0; r < nrhs; r++) {
+    double sum = 0.0;
+    for (int b = 0; b < nb * nsplit; b++) sum += part[(size_t)b * 8 + r];
+    pscat[r] = 0.5 * sum;
+    if (pext && rhs) {
+      // extinction: -1/2 ZVAC sum Re(conj(x_i) b_i), with the opposite sign on N rows
+      double ext = 0.0;
+      for (int i = 0; i < N; i++) {
+        const double* x = KN + 2 * ((size_t)i + (size_t)r * ldkn);
+        const double* b = rhs + 2 * ((size_t)i + (size_t)r * ldr);
+        const double v = x[0] * b[0] + x[1] * b[1];
+        ext += type[i] ? -v : v;
+      }
+      pext[r] = -0.5 * ZV * ext;
+    }
+  }
+  return GBEM_OK;
+}
+
+gbem_status gbem_assemble_block_gradient(gbem_geometry* g, int nsa, int nsb, double omega_re, double omega_im,
+                                         const double* eps, const double* mu, void* gx, void* gy, void* gz, int ld,
+                                         int row0, int col0, int dtype) {
+  if (!g || !eps || !mu || nsa < 0 || nsb < 0 || nsa >= (int)g->S.size() || nsb >= (int)g->S.size() || row0 < 0 ||
+      col0 < 0 || ld < row0 + surface_bfs(g, nsa) || (dtype != GBEM_C128 && dtype != GBEM_F64)) {
+    set_error("gbem_assemble_block_gradient: bad arguments (dtype C128 or F64)");
+    return GBEM_EINVAL;
+  }
+  if (omega_is_zero(omega_re, omega_im)) { set_error("gbem_assemble_block_gradient: Omega = 0"); return GBEM_EINVAL; }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  void* const out[3] = {gx, gy, gz};
+  BlockSel sel{nsa, nsb, row0, col0};
+  return assemble_gradient_device(g, omega_re, omega_im, eps, mu, sel, out, ld, dtype, g->stream);
+}
+
+gbem_status gbem_assemble_block_gradient_host(gbem_geometry* g, int nsa, int nsb, double omega_re, double omega_im,
+                                              const double* eps, const double* mu, void* gx, void* gy, void* gz,
+                                              int ld, int row0, int col0, int dtype) {
+  if (!g || nsa < 0 || nsb < 0 || nsa >= (int)g->S.size() || nsb >= (int)g->S.size() ||
+      (dtype != GBEM_C128 && dtype != GBEM_F64) || row0 < 0 || col0 < 0 || ld < row0 + surface_bfs(g, nsa)) {
+    set_error("gbem_assemble_block_gradient_host: bad arguments (dtype C128 or F64)");
+    return GBEM_EINVAL;
+  }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  const int m = surface_bfs(g, nsa), n = surface_bfs(g, nsb);
+  const size_t es = dtype == GBEM_C128 ? 16 : 8;
+  void* host[3] = {gx, gy, gz};
+  void* d[3] = {nullptr, nullptr, nullptr};
+  for (int c = 0; c < 3; c++)
+    if (host[c]) CHECK_CUDA(cudaMallocAsync(&d[c], (size_t)m * n * es, g->stream), "gradient scratch");
+  st = gbem_assemble_block_gradient(g, nsa, nsb, omega_re, omega_im, eps, mu, d[0], d[1], d[2], m, 0, 0, dtype);
+  for (int c = 0; c < 3 && st == GBEM_OK; c++) {
+    if (!host[c]) continue;
+    cudaError_t e = cudaMemcpy2DAsync((char*)host[c] + ((size_t)row0 + (size_t)col0 * ld) * es, (size_t)ld * es, d[c],
+                                      (size_t)m * es, (size_t)m * es, n, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) st = cuda_status(e, "gradient download");
+  }
+  for (int c = 0; c < 3; c++) cudaFreeAsync(d[c], g->stream);
+  cudaStreamSynchronize(g->stream);
+  return st;
 }
 
 gbem_status gbem_assemble_block_host(gbem_geometry* g, int nsa, int nsb, double omega_re, double omega_im,

@@ -109,7 +109,9 @@ struct BlockSel {
 };
 gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps, const double* mu,
                             int precision, void* dM, int ld, int dtype, cudaStream_t s,
-                            const BlockSel* only = nullptr);
+                            const BlockSel* only = nullptr, int only_region = -1);
+gbem_status assemble_gradient_device(Geometry* g, double wr, double wi, const double* eps, const double* mu,
+                                     const BlockSel& sel, void* const out[3], int ld, int dtype, cudaStream_t s);
 gbem_status upload_geometry(Geometry* g);
 void free_geometry_device(Geometry* g);
 

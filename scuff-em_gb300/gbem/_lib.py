@@ -25,6 +25,7 @@ EXPORTS = [
     "gbem_lu_factor", "gbem_lu_solve", "gbem_lu_factor_host", "gbem_lu_solve_host", "gbem_solve_mixed",
     "gbem_rhs_planewave", "gbem_solve_mixed_device", "gbem_stats", "gbem_geometry_set_stream",
     "gbem_lu_solve_noalloc", "gbem_assemble_block", "gbem_assemble_block_host",
+    "gbem_assemble_block_gradient", "gbem_assemble_block_gradient_host", "gbem_power_emt",
 ]
 
 
@@ -67,6 +68,9 @@ def lib():
             "gbem_lu_solve_noalloc": ([P, ctypes.c_char, I, P, I], I),
             "gbem_assemble_block": ([P, I, I, D, D, P, P, I, P, I, I, I, I], I),
             "gbem_assemble_block_host": ([P, I, I, D, D, P, P, P, I, I, I, I], I),
+            "gbem_assemble_block_gradient": ([P, I, I, D, D, P, P, P, P, P, I, I, I, I], I),
+            "gbem_assemble_block_gradient_host": ([P, I, I, D, D, P, P, P, P, P, I, I, I, I], I),
+            "gbem_power_emt": ([P, D, D, P, P, I, I, P, I, P, I, P, P], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

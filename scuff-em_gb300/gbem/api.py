@@ -231,6 +231,40 @@ class RWGGeometry:
                                              mu.ctypes.data, M.ctypes.data, M.shape[0], RowOffset, ColOffset, dt))
         return M
 
+    def AssembleBEMMatrixBlockGradient(self, nsa, nsb, Omega, real=False, components=(0, 1, 2)):
+        """GradM[mu] = dM_block/dx_mu for a rigid displacement of surface nsa
+        (AssembleBEMMatrixBlock's GradM); returns a list of three host arrays
+        (None for components not requested)."""
+        dt = F64 if real else C128
+        m, n = self.NumBFs(nsa), self.NumBFs(nsb)
+        out = [np.zeros((m, n), dtype=np.float64 if real else np.complex128, order="F") if c in components else None
+               for c in range(3)]
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        ptr = [o.ctypes.data if o is not None else None for o in out]
+        check(lib().gbem_assemble_block_gradient_host(self._h, nsa, nsb, Omega.real, Omega.imag, eps.ctypes.data,
+                                                      mu.ctypes.data, ptr[0], ptr[1], ptr[2], m, 0, 0, dt))
+        return out
+
+    def GetPFT(self, Omega, KN, RHS=None, precision="fp64"):
+        """Scattered and absorbed power (the reference's EMT powers, GetPFT)
+        of one or more solution vectors KN (columns); RHS gives extinction.
+        Returns (PAbs, PScat) arrays (PAbs is None without RHS)."""
+        KN = np.asfortranarray(np.asarray(KN, dtype=np.complex128).reshape(self.TotalBFs, -1))
+        nrhs = KN.shape[1]
+        ps = np.zeros(nrhs)
+        pe = np.zeros(nrhs)
+        rp = None
+        if RHS is not None:
+            RHS = np.asfortranarray(np.asarray(RHS, dtype=np.complex128).reshape(self.TotalBFs, -1))
+            rp = RHS.ctypes.data
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        check(lib().gbem_power_emt(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data,
+                                   PREC_MIXED if precision == "mixed" else PREC_FP64, nrhs, KN.ctypes.data,
+                                   self.TotalBFs, rp, self.TotalBFs, ps.ctypes.data, pe.ctypes.data))
+        return (pe - ps if RHS is not None else None), ps
+
     def AssembleRHSVector(self, Omega, E0, nHat):
         """Plane wave E0 exp(i k nHat.x) incident from the exterior region."""
         eps, mu = self.eps_mu(Omega)

@@ -165,12 +165,58 @@ def matrix_case(tmp, name, objects, omega, pw=None, cols=None):
     np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % name), **out)
 
 
+def read_rects(path, count):
+    out = []
+    with open(path, "rb") as f:
+        for _ in range(count):
+            nr, nc = np.frombuffer(f.read(8), dtype=np.int32)
+            d = np.frombuffer(f.read(16 * nr * nc), dtype=np.float64)
+            out.append((d[0::2] + 1j * d[1::2]).reshape(nr, nc, order="F"))
+    return out
+
+
+def grad_case(tmp, name, objects, omega, blocks):
+    """Surface blocks and their gradients d/dx_mu (AssembleBEMMatrixBlock with
+    GradM, the cas3D path) for each (nsa, nsb) in blocks."""
+    geo = geo_file(tmp, name, objects)
+    out = {"omega": np.array([np.real(omega), np.imag(omega)])}
+    for i, (mname, V, P, mat, disp) in enumerate(objects):
+        out["V%d" % i] = V
+        out["P%d" % i] = P
+        out["mat%d" % i] = np.array(mat if mat is not None else "PEC")
+        out["disp%d" % i] = np.array(disp if disp is not None else (0.0, 0.0, 0.0))
+    for (a, b) in blocks:
+        fn = os.path.join(tmp, "%s_%d%d.bin" % (name, a, b))
+        run(["gradblock", os.path.basename(geo), np.real(omega), np.imag(omega), a, b, fn], tmp)
+        M, gx, gy, gz = read_rects(fn, 4)
+        out["M%d%d" % (a, b)] = M
+        out["G%d%d" % (a, b)] = np.stack([gx, gy, gz])
+    out["objects"] = np.array(len(objects))
+    np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % name), **out)
+
+
+def gradient_fixtures(tmp):
+    V1, P1 = icosphere(1)
+    # two PEC spheres, centre gap 3, imaginary frequency: every pair of the
+    # inter-sphere block is far (6x6 rule); the self block has near pairs too
+    grad_case(tmp, "pec2_s1_grad", [("a", V1, P1, None, None), ("b", V1, P1, None, (0.0, 0.0, 3.0))], 0.7j,
+              [(0, 1), (1, 0), (0, 0)])
+    # two dielectric spheres (PMCHWT 2x2 stamping), real frequency
+    grad_case(tmp, "diel2_s1_grad", [("a", V1, P1, "CONST_EPS_2.25+0.01i", None),
+                                     ("b", V1, P1, "CONST_EPS_2.25+0.01i", (0.0, 0.0, 3.0))], 1.5, [(0, 1)])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", choices=["gradients"], help="regenerate one group of fixtures only")
     a = ap.parse_args()
     if not os.path.exists(REFDUMP):
         sys.exit("build the reference first: make -C oracle/ref REF=%s" % a.ref)
+    if a.only == "gradients":
+        with tempfile.TemporaryDirectory() as tmp:
+            gradient_fixtures(tmp)
+        return
     rng = np.random.default_rng(0)
     with tempfile.TemporaryDirectory() as tmp:
         unit_ppi(a.ref, tmp)
@@ -187,6 +233,7 @@ def main():
         matrix_case(tmp, "pec2_s1_xi", [("a", V1, P1, None, None), ("b", V1, P1, None, (0.0, 0.0, 3.0))], 0.7j)
         # dielectric sphere at a frequency where high-order / Taylor-Duffy branches appear
         matrix_case(tmp, "diel_s1_w12", [("sph", V1, P1, "CONST_EPS_4+0.1i", None)], 12.0)
+        gradient_fixtures(tmp)
 
 
 if __name__ == "__main__":

@@ -38,3 +38,28 @@ def test_mixed_solve_refines_to_fp64(golden):
     M64 = G.AssembleBEMMatrix(w).numpy()
     X64 = sl.solve(M64, B)
     assert np.abs(X - X64).max() / np.abs(X64).max() < 1e-5
+
+
+@pytest.mark.parametrize("case", ["pec_s2_w1", "diel_s1_w2"])
+def test_emt_power_matches_reference(golden, case):
+    """Scattered and absorbed power (EMT, GetPFT) of the reference's own
+    solutions: the GPU quadratic form with the exterior-region matrix agrees
+    with the reference and with the oracle's restatement."""
+    from gbem import RWGGeometry
+    from oracle import oracle as ora
+    d = golden("ref_%s.npz" % case)
+    gs, (regs, pec, eps, mu) = fixture_surfaces(d)
+    G = RWGGeometry(gs)
+    w = omega_of(d)
+    j = 0
+    while "kn%d" % j in d.files:
+        kn, rhs, ref = d["kn%d" % j], d["rhs%d" % j], d["pft%d" % j]
+        pabs, pscat = G.GetPFT(w, kn, RHS=rhs)
+        po = ora.emt_pscat(ora.Surface(gs[0]["V"], gs[0]["P"]), pec[0], w, kn)
+        assert abs(pscat[0] - po) < 1e-9 * abs(po), (pscat, po)
+        assert abs(pscat[0] - ref[1]) < 2e-6 * abs(ref[1]), (pscat, ref)
+        # absorbed = extinction - scattered (zero up to quadrature for PEC)
+        assert abs(pabs[0] - ref[0]) < 2e-6 * abs(ref[1]), (pabs, ref)
+        _, p32 = G.GetPFT(w, kn, precision="mixed")
+        assert abs(p32[0] - pscat[0]) < 1e-6 * abs(pscat[0])
+        j += 1

@@ -117,3 +117,18 @@ def test_matrix_short_wavelength_against_reference(golden):
     M = ora.assemble(surfs, regs, pec, w, eps, mu)
     err = np.abs(M - d["M"]).max() / np.abs(d["M"]).max()
     assert err < 2e-6, err
+
+
+@pytest.mark.parametrize("case", ["pec_s2_w1", "diel_s1_w2"])
+def test_emt_scattered_power_against_reference(golden, case):
+    """EMT scattered power of the reference's own solutions (GetPFT): the
+    oracle's restatement from GC[0], GC[1] agrees to the reference's
+    near-field quadrature level."""
+    d = golden("ref_%s.npz" % case)
+    surfs, regs, pec, eps, mu = _geometry(d)
+    w = d["omega"][0] + 1j * d["omega"][1]
+    j = 0
+    while "kn%d" % j in d.files:
+        ps = ora.emt_pscat(surfs[0], pec[0], w, d["kn%d" % j])
+        assert abs(ps - d["pft%d" % j][1]) < 2e-6 * abs(d["pft%d" % j][1]), (j, ps, d["pft%d" % j])
+        j += 1
