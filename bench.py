@@ -306,6 +306,14 @@ def main():
         out["accuracy"] = {"rel_err_x_vs_fp64": rel_x,
                            "rel_err_extinction_power_vs_fp64": float(np.max(np.abs(pmx - p64) / np.abs(p64))),
                            "extinction_power_fp64": [float(v) for v in p64]}
+        # EMT scattered and absorbed power (GetPFT's default method) of both
+        # solutions, each with the FP64 exterior-region matrix
+        pa64, ps64 = G.GetPFT(w, X64, RHS=B)
+        pamx, psmx = G.GetPFT(w, Xmixed, RHS=B)
+        out["accuracy"]["rel_err_scattered_power_vs_fp64"] = float(np.max(np.abs(psmx - ps64) / np.abs(ps64)))
+        out["accuracy"]["rel_err_absorbed_power_vs_fp64"] = float(np.max(np.abs(pamx - pa64) / np.abs(pa64)))
+        out["accuracy"]["scattered_power_fp64"] = [float(v) for v in ps64]
+        out["accuracy"]["absorbed_power_fp64"] = [float(v) for v in pa64]
     if not args.no_cpu and rank == 0 and world == 1:
         try:
             out["cpu_baseline"] = cpu_sample(os.cpu_count())

@@ -25,6 +25,7 @@
 #include <new>
 #include <vector>
 #include "bem_math.cuh"
+#include "ffmath.cuh"
 #include "gbem_internal.h"
 
 namespace gbem {
@@ -34,7 +35,8 @@ namespace gbem {
 // ---------------------------------------------------------------------------
 // LO rule: the 13-digit values of libs/libTriInt/TCR.cc:83-91 (order 4).
 __constant__ double c_lo64[18];
-__constant__ float c_lo32[18];
+__constant__ FFRule c_ffrule;      // the LO rule as float-float (mixed far field)
+__constant__ SinCosTab c_sctab;    // cos, sin of j pi/64 as float-float
 static const double h_lo[18] = {
     0.0915762135098, 0.0915762135098, 0.0549758718276, 0.8168475729805, 0.0915762135098, 0.0549758718276,
     0.0915762135098, 0.8168475729805, 0.0549758718276, 0.1081030181681, 0.4459484909160, 0.1116907948390,
@@ -66,8 +68,6 @@ static gbem_status init_rules() {
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && done[dev]) return GBEM_OK;
-  float lo32[18];
-  for (int i = 0; i < 18; i++) lo32[i] = (float)h_lo[i];
   double x[HO_N], w[HO_N], ho[3 * HO_N * HO_N];
   gauss01(HO_N, x, w);
   int k = 0;
@@ -80,8 +80,13 @@ static gbem_status init_rules() {
   double gx16[NT_SELF], gw16[NT_SELF], gx12[N_FIP], gw12[N_FIP];
   gauss01(NT_SELF, gx16, gw16);
   gauss01(N_FIP, gx12, gw12);
+  FFRule ffr;
+  fill_ff_rule(h_lo, &ffr);
+  SinCosTab sct;
+  fill_sincos_tab(&sct);
   cudaError_t e = cudaMemcpyToSymbol(c_lo64, h_lo, sizeof h_lo);
-  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_lo32, lo32, sizeof lo32);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ffrule, &ffr, sizeof ffr);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_sctab, &sct, sizeof sct);
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_ho, ho, sizeof ho);
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gx16, gx16, sizeof gx16);
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gw16, gw16, sizeof gw16);
@@ -418,10 +423,6 @@ struct TileArgs {
   long long ld;
 };
 
-template <typename T> __device__ __forceinline__ const T* lo_rule();
-template <> __device__ __forceinline__ const float* lo_rule<float>() { return c_lo32; }
-template <> __device__ __forceinline__ const double* lo_rule<double>() { return c_lo64; }
-
 // relative distance with the reference's operation order and no FMA
 // contraction (AssessPanelPair.cc:160-166)
 __device__ __forceinline__ bool is_far(const double* ca, const double* cb, double ra, double rb) {
@@ -435,30 +436,83 @@ __device__ __forceinline__ bool is_far(const double* ca, const double* cb, doubl
   return __ddiv_rn(__dsqrt_rn(r2), rmax) > 4.0;
 }
 
-template <typename T, int NC>
+// rRel > 4 decides the 6x6 rule; an FP32 estimate settles all but the pairs
+// within 1e-4 of the threshold, which take the exact FP64 test
+__device__ __forceinline__ bool tile_pair_far(const float* ca, const float* cb, const double* da, const double* db) {
+  const float dx = ca[0] - cb[0], dy = ca[1] - cb[1], dz = ca[2] - cb[2];
+  const float d2f = dx * dx + dy * dy + dz * dz, rmf = fmaxf(ca[3], cb[3]);
+  if (d2f > 16.0008f * rmf * rmf) return true;
+  if (d2f < 15.9992f * rmf * rmf) return false;
+  return is_far(da, db, da[3], db[3]);
+}
+
+// index of the near pair (global panels gpa, gpb) in the block's near list,
+// times 2, plus 1 when it is stored transposed; -1 if absent
+__device__ __forceinline__ int near_hit(const TileArgs& a, int gpa, int gpb) {
+  const int row = gpa - a.row_panel_offset;
+  for (int e = a.nptr[row]; e < a.nptr[row + 1]; e++)
+    if (a.ncol[e] == gpb) return a.nidx[e];
+  return -1;
+}
+
+// tile entry q of a pass: pass 0 walks column-major (coalesced stores into
+// the block), pass 1 row-major (coalesced stores into its mirror).  A
+// diagonal tile of a symmetric block writes its upper triangle and mirrors
+// it, so the matrix is exactly symmetric (AssembleBEMMatrix.cc:753-758).
+__device__ __forceinline__ bool tile_entry(int pass, int q, int NR, int NCc, bool diag, int* i, int* j) {
+  if (pass == 0) { *i = q % NR; *j = q / NR; } else { *j = q % NCc; *i = q / NCc; }
+  return !(diag && (pass == 0 ? *i > *j : *i >= *j));
+}
+
+// write entry (row edge ea, column edge eb) of the block -- pass 0 -- or its
+// mirror -- pass 1 -- with the (dx, dy) sub-entries of dielectric basis
+// pairs: e00 = EE, e01 = e10 = EH/HE, e11 = HH
+template <typename C>
+__device__ __forceinline__ void store_entry(const TileArgs& a, C* out, int pass, int ea, int eb, C e00, C eoff, C e11) {
+  const long long ld = a.ld;
+  const long long X = (pass == 0 ? a.row_off : a.mcol_off) + (long long)a.bpe_a * ea;
+  const long long Y = (pass == 0 ? a.col_off : a.mrow_off) + (long long)a.bpe_b * eb;
+  if (a.bpe_a == 1 && a.bpe_b == 1) {
+    if (pass == 0) out[X + Y * ld] = e00; else out[Y + X * ld] = e00;
+  } else if (a.bpe_a == 1) {
+    if (pass == 0) { out[X + Y * ld] = e00; out[X + (Y + 1) * ld] = eoff; }
+    else { out[Y + X * ld] = e00; out[(Y + 1) + X * ld] = eoff; }
+  } else if (a.bpe_b == 1) {
+    if (pass == 0) { out[X + Y * ld] = e00; out[(X + 1) + Y * ld] = eoff; }
+    else { out[Y + X * ld] = e00; out[Y + (X + 1) * ld] = eoff; }
+  } else {
+    if (pass == 0) {
+      out[X + Y * ld] = e00; out[X + 1 + Y * ld] = eoff;
+      out[X + (Y + 1) * ld] = eoff; out[X + 1 + (Y + 1) * ld] = e11;
+    } else {
+      out[Y + X * ld] = e00; out[Y + 1 + X * ld] = eoff;
+      out[Y + (X + 1) * ld] = eoff; out[Y + 1 + (X + 1) * ld] = e11;
+    }
+  }
+}
+
+// FP64 far field: one CTA per tile of TE x TE edge pairs (upper triangle of
+// symmetric blocks).  The CTA stages its panels in shared memory, computes
+// the moments of every panel pair the tile touches once, forms the needed
+// (Qa,Qb) combinations and writes each into a per-(edge pair, P/M side) slot;
+// every slot has one writer, so the four contributions of an edge pair are
+// summed in a fixed order (deterministic, no atomics).
+template <int NC>
 __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<T>* slots = reinterpret_cast<cx<T>*>(smem_raw);  // [TE][TE][4][NC]
-  constexpr int PVN = sizeof(T) == 4 ? 1 : 9;  // the FP32 kernel keeps FP32 geometry only
-  __shared__ double s_pv[2][PMAX][PVN];
+  cx<double>* slots = reinterpret_cast<cx<double>*>(smem_raw);  // [TE][TE][4][NC]
+  __shared__ double s_pv[2][PMAX][9];
   __shared__ double s_pc[2][PMAX][4];
   __shared__ int8_t s_hl[2][3 * PMAX], s_hs[2][3 * PMAX];
   __shared__ int s_gp[2][PMAX];
-  __shared__ float s_ev[2][PMAX][6];  // FP32 edge vectors V1-V0, V2-V0
   __shared__ float s_cf[2][PMAX][4];  // FP32 centroid and radius (pre-check of rRel)
-  __shared__ float s_v0[2][PMAX][6];  // V0 as FP32 (hi, lo) pairs: D0 to FP32 relative accuracy
-  __shared__ cx<float> s_rk[2], s_rm4[2], s_rp1[2], s_rpc[2], s_rp3[2];  // per-region FP32 constants
-  __shared__ int s_live[2];
-  __shared__ T s_el[2][TE];  // edge lengths of the tile's rows and columns
 
   const int2 tile = a.tiles[blockIdx.x];
   const DevEdgeBlock* RB = a.rows + tile.x;
   const DevEdgeBlock* CB = a.cols + tile.y;
   const int PR = RB->np, PC = CB->np, NR = RB->ne, NCc = CB->ne;
-  if constexpr (sizeof(T) == 8) {
-    for (int q = threadIdx.x; q < PR * 9; q += blockDim.x) s_pv[0][q / 9][q % 9] = a.pv[9 * (size_t)RB->panels[q / 9] + q % 9];
-    for (int q = threadIdx.x; q < PC * 9; q += blockDim.x) s_pv[1][q / 9][q % 9] = a.pv[9 * (size_t)CB->panels[q / 9] + q % 9];
-  }
+  for (int q = threadIdx.x; q < PR * 9; q += blockDim.x) s_pv[0][q / 9][q % 9] = a.pv[9 * (size_t)RB->panels[q / 9] + q % 9];
+  for (int q = threadIdx.x; q < PC * 9; q += blockDim.x) s_pv[1][q / 9][q % 9] = a.pv[9 * (size_t)CB->panels[q / 9] + q % 9];
   for (int q = threadIdx.x; q < PR * 4; q += blockDim.x) s_pc[0][q / 4][q % 4] = a.pc[4 * (size_t)RB->panels[q / 4] + q % 4];
   for (int q = threadIdx.x; q < PC * 4; q += blockDim.x) s_pc[1][q / 4][q % 4] = a.pc[4 * (size_t)CB->panels[q / 4] + q % 4];
   for (int q = threadIdx.x; q < 3 * PR; q += blockDim.x) { s_hl[0][q] = RB->hl[q]; s_hs[0][q] = RB->hs[q]; }
@@ -468,36 +522,11 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
   __syncthreads();
   for (int q = threadIdx.x; q < 2 * PMAX; q += blockDim.x) {
     const int side = q / PMAX, p = q % PMAX;
-    if (p >= (side ? PC : PR)) continue;
-    const double* V = a.pv + 9 * (size_t)(side ? CB->panels[p] : RB->panels[p]);
-    for (int c = 0; c < 3; c++) { s_ev[side][p][c] = (float)(V[3 + c] - V[c]); s_ev[side][p][3 + c] = (float)(V[6 + c] - V[c]); }
-    for (int c = 0; c < 4; c++) s_cf[side][p][c] = (float)s_pc[side][p][c];
-    for (int c = 0; c < 3; c++) {
-      const float hi = (float)V[c];
-      s_v0[side][p][c] = hi;
-      s_v0[side][p][3 + c] = (float)(V[c] - (double)hi);
-    }
-  }
-  for (int q = threadIdx.x; q < 2 * TE; q += blockDim.x) {
-    const int side = q / TE, e = q % TE;
-    if (e < (side ? NCc : NR)) s_el[side][e] = (T)(side ? a.elen_b[CB->e0 + e] : a.elen_a[RB->e0 + e]);
-  }
-  if (threadIdx.x < 2) {
-    // region constants in FP32, formed once per CTA in FP64
-    const int r = threadIdx.x;
-    const cx<double> kd = r < ra.nreg ? ra.k[r] : mk(0.0, 0.0);
-    const bool live = !(kd.re == 0.0 && kd.im == 0.0);
-    s_live[r] = live;
-    const cx<double> m4d = live ? cdiv(mk(-4.0, 0.0), kd * kd) : mk(0.0, 0.0);
-    s_rk[r] = mk((float)kd.re, (float)kd.im);
-    s_rm4[r] = mk((float)m4d.re, (float)m4d.im);
-    s_rp1[r] = live ? mk((float)ra.pf1[r].re, (float)ra.pf1[r].im) : mk(0.0f, 0.0f);
-    s_rpc[r] = live ? mk((float)ra.pfc[r].re, (float)ra.pfc[r].im) : mk(0.0f, 0.0f);
-    s_rp3[r] = live ? mk((float)ra.pf3[r].re, (float)ra.pf3[r].im) : mk(0.0f, 0.0f);
+    if (p < (side ? PC : PR))
+      for (int c = 0; c < 4; c++) s_cf[side][p][c] = (float)s_pc[side][p][c];
   }
   __syncthreads();
 
-  const T* rule = lo_rule<T>();
   for (int q = threadIdx.x; q < PR * PC; q += blockDim.x) {
     const int ia = q / PC, ib = q - ia * PC;
     const double* Va = s_pv[0][ia];
@@ -507,96 +536,33 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
       la[j] = s_hl[0][3 * ia + j]; sa[j] = s_hs[0][3 * ia + j];
       lb[j] = s_hl[1][3 * ib + j]; sb[j] = s_hs[1][3 * ib + j];
     }
-    // rRel > 4 decides the 6x6 rule; an FP32 estimate settles all but the
-    // pairs within 1e-4 of the threshold, which take the exact FP64 test
-    const float dx = s_cf[0][ia][0] - s_cf[1][ib][0], dy = s_cf[0][ia][1] - s_cf[1][ib][1],
-                dz = s_cf[0][ia][2] - s_cf[1][ib][2];
-    const float d2f = dx * dx + dy * dy + dz * dz, rmf = fmaxf(s_cf[0][ia][3], s_cf[1][ib][3]);
-    bool far;
-    if (d2f > 16.0008f * rmf * rmf) far = true;
-    else if (d2f < 15.9992f * rmf * rmf) far = false;
-    else far = is_far(s_pc[0][ia], s_pc[1][ib], s_pc[0][ia][3], s_pc[1][ib][3]);
-    if (far) {
-      PairGeom<T> g;
+    if (tile_pair_far(s_cf[0][ia], s_cf[1][ib], s_pc[0][ia], s_pc[1][ib])) {
+      PairGeom<double> g;
       for (int c = 0; c < 3; c++) {
-        if constexpr (sizeof(T) == 4)
-          g.D0[c] = (s_v0[0][ia][c] - s_v0[1][ib][c]) + (s_v0[0][ia][3 + c] - s_v0[1][ib][3 + c]);
-        else
-          g.D0[c] = (T)(Va[c] - Vb[c]);
-        if constexpr (sizeof(T) == 4) {
-          g.Aa[c] = s_ev[0][ia][c]; g.Ba[c] = s_ev[0][ia][3 + c];
-          g.Ab[c] = s_ev[1][ib][c]; g.Bb[c] = s_ev[1][ib][3 + c];
-        } else {
-          g.Aa[c] = (T)(Va[3 + c] - Va[c]); g.Ba[c] = (T)(Va[6 + c] - Va[c]);
-          g.Ab[c] = (T)(Vb[3 + c] - Vb[c]); g.Bb[c] = (T)(Vb[6 + c] - Vb[c]);
-        }
+        g.D0[c] = Va[c] - Vb[c];
+        g.Aa[c] = Va[3 + c] - Va[c]; g.Ba[c] = Va[6 + c] - Va[c];
+        g.Ab[c] = Vb[3 + c] - Vb[c]; g.Bb[c] = Vb[6 + c] - Vb[c];
       }
-      if constexpr (sizeof(T) == 4) {
-        // FP32: per region, the 9+9 moments in vector form, then every needed
-        // (Qa,Qb) from them (vec_combine); the slot takes the first region's
-        // value and adds the second's (one writer per slot: deterministic)
-        constexpr int R2 = NC == 1 ? 1 : 2;
-        for (int r = 0; r < R2; r++) {
-          const bool live = s_live[r];
-          VecMoments<T> vm;
-          const cx<T> m4 = s_rm4[r], p1 = s_rp1[r], pc = s_rpc[r], p3 = s_rp3[r];
-          if (live) {
-            cx<T> MG[9], MP[9];
-            pair_moments<T, 0>(g, s_rk[r], rule, 6, MG, MP);
-            vec_moments(g, MG, MP, &vm);
-          }
-          for (int ja = 0; ja < 3; ja++) {
-            if (la[ja] < 0) continue;
-            for (int jb = 0; jb < 3; jb++) {
-              if (lb[jb] < 0) continue;
-              cx<T> v0 = mk((T)0, (T)0), v1 = v0, v2 = v0;
-              if (live) {
-                cx<T> H0, H1;
-                vec_combine(g, vm, ja, jb, m4, &H0, &H1);
-                v0 = p1 * H0;
-                v1 = pc * H1;
-                v2 = p3 * H0;
-              }
-              cx<T>* sl = slots + ((size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb]) * NC;
-              if (r == 0) {
-                sl[0] = v0;
-                if (NC > 1) sl[1] = v1;
-                if (NC > 2) sl[2] = v2;
-              } else {
-                sl[0] = sl[0] + v0;
-                if (NC > 1) sl[1] = sl[1] + v1;
-                if (NC > 2) sl[2] = sl[2] + v2;
-              }
-            }
-          }
-        }
-      } else {
       bool first = true;
       for (int r = 0; r < ra.nreg; r++) {
-        cx<double> kd = ra.k[r];
-        if (kd.re == 0.0 && kd.im == 0.0) continue;
-        cx<T> k = mk((T)kd.re, (T)kd.im);
-        cx<T> MG[9], MP[9];
-        pair_moments<T, 0>(g, k, rule, 6, MG, MP);
-        cx<double> m4ok2d = cdiv(mk(-4.0, 0.0), kd * kd);
-        cx<T> m4ok2 = mk((T)m4ok2d.re, (T)m4ok2d.im);
-        cx<T> p1 = mk((T)ra.pf1[r].re, (T)ra.pf1[r].im), pc = mk((T)ra.pfc[r].re, (T)ra.pfc[r].im),
-              p3 = mk((T)ra.pf3[r].re, (T)ra.pf3[r].im);
+        cx<double> k = ra.k[r];
+        if (k.re == 0.0 && k.im == 0.0) continue;
+        cx<double> MG[9], MP[9];
+        pair_moments<double, 0>(g, k, c_lo64, 6, MG, MP);
+        const cx<double> m4ok2 = cdiv(mk(-4.0, 0.0), k * k);
         for (int ja = 0; ja < 3; ja++) {
           if (la[ja] < 0) continue;
           for (int jb = 0; jb < 3; jb++) {
             if (lb[jb] < 0) continue;
-            double cd[9], dd[9];
-            combo_coeffs(Va, Vb, ja, jb, cd, dd);
-            T c[9], d[9];
-            for (int m = 0; m < 9; m++) { c[m] = (T)cd[m]; d[m] = (T)dd[m]; }
-            cx<T> H0, H1;
+            double c[9], d[9];
+            combo_coeffs(Va, Vb, ja, jb, c, d);
+            cx<double> H0, H1;
             combine(MG, MP, c, d, m4ok2, &H0, &H1);
-            cx<T>* s = slots + ((size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb]) * NC;
-            cx<T> v0 = p1 * H0;
-            if (first) s[0] = v0; else s[0] = s[0] + v0;
-            if (NC > 1) { cx<T> v1 = pc * H1; if (first) s[1] = v1; else s[1] = s[1] + v1; }
-            if (NC > 2) { cx<T> v2 = p3 * H0; if (first) s[2] = v2; else s[2] = s[2] + v2; }
+            cx<double>* sl = slots + ((size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb]) * NC;
+            const cx<double> v0 = ra.pf1[r] * H0;
+            if (first) sl[0] = v0; else sl[0] = sl[0] + v0;
+            if (NC > 1) { const cx<double> v1 = ra.pfc[r] * H1; if (first) sl[1] = v1; else sl[1] = sl[1] + v1; }
+            if (NC > 2) { const cx<double> v2 = ra.pf3[r] * H0; if (first) sl[2] = v2; else sl[2] = sl[2] + v2; }
           }
         }
         first = false;
@@ -605,17 +571,13 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
         for (int ja = 0; ja < 3; ja++)
           for (int jb = 0; jb < 3; jb++)
             if (la[ja] >= 0 && lb[jb] >= 0) {
-              cx<T>* s = slots + ((size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb]) * NC;
-              for (int c = 0; c < NC; c++) s[c] = mk((T)0, (T)0);
+              cx<double>* sl = slots + ((size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb]) * NC;
+              for (int c = 0; c < NC; c++) sl[c] = mk(0.0, 0.0);
             }
-      }
       }
     } else {
       // near pair: values precomputed in FP64 by self_kernel / near_kernel
-      int gpa = s_gp[0][ia], gpb = s_gp[1][ib];
-      int row = gpa - a.row_panel_offset, hit = -1;
-      for (int e = a.nptr[row]; e < a.nptr[row + 1]; e++)
-        if (a.ncol[e] == gpb) { hit = a.nidx[e]; break; }
+      const int hit = near_hit(a, s_gp[0][ia], s_gp[1][ib]);
       if (hit < 0) continue;  // cannot happen: every rRel<=4 pair is listed
       const double* nv = a.nearval + 54 * (size_t)(hit >> 1);
       const bool tr = hit & 1;
@@ -624,10 +586,10 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
         for (int jb = 0; jb < 3; jb++) {
           if (lb[jb] < 0) continue;
           const double* v = nv + 6 * (tr ? (3 * jb + ja) : (3 * ja + jb));
-          cx<T>* s = slots + ((size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb]) * NC;
-          s[0] = mk((T)v[0], (T)v[1]);
-          if (NC > 1) s[1] = mk((T)v[2], (T)v[3]);
-          if (NC > 2) s[2] = mk((T)v[4], (T)v[5]);
+          cx<double>* sl = slots + ((size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb]) * NC;
+          sl[0] = mk(v[0], v[1]);
+          if (NC > 1) sl[1] = mk(v[2], v[3]);
+          if (NC > 2) sl[2] = mk(v[4], v[5]);
         }
       }
     }
@@ -635,62 +597,266 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
   __syncthreads();
 
   // entries: sum of the four P/M contributions times La Lb
-  cx<T>* out = reinterpret_cast<cx<T>*>(a.out);
-  const long long ld = a.ld;
-  // A diagonal tile of a symmetric block writes its upper triangle and
-  // mirrors it, so the matrix is exactly symmetric (AssembleBEMMatrix.cc:753-758).
+  cx<double>* out = reinterpret_cast<cx<double>*>(a.out);
   const bool diag = a.sym && tile.x == tile.y;
   for (int pass = 0; pass < 2; pass++) {
     if (!(a.passes & (1 << pass))) continue;
     for (int q = threadIdx.x; q < NR * NCc; q += blockDim.x) {
       int i, j;
-      if (pass == 0) { i = q % NR; j = q / NR; } else { j = q % NCc; i = q / NCc; }
-      if (diag && (pass == 0 ? i > j : i >= j)) continue;
-      const cx<T>* s = slots + (size_t)(i * TE + j) * 4 * NC;
-      cx<T> v[3];
-      for (int c = 0; c < NC; c++) v[c] = (s[c] - s[NC + c]) - (s[2 * NC + c] - s[3 * NC + c]);
-      T L;
-      if constexpr (sizeof(T) == 4) L = s_el[0][i] * s_el[1][j];
-      else L = (T)(a.elen_a[RB->e0 + i] * a.elen_b[CB->e0 + j]);
-      for (int c = 0; c < NC; c++) v[c] = L * v[c];
-      // pass 0: entry (X, Y) of the block; pass 1: its mirror at (Y, X), with
-      // the mirror's own offsets (block assembly places either one anywhere)
-      long long X = (pass == 0 ? a.row_off : a.mcol_off) + (long long)a.bpe_a * (RB->e0 + i);
-      long long Y = (pass == 0 ? a.col_off : a.mrow_off) + (long long)a.bpe_b * (CB->e0 + j);
-      // block entries (dx, dy) -> value
-      cx<T> e00 = v[0], e01, e10, e11;
-      if (a.bpe_a == 1 && a.bpe_b == 1) {
-        if (pass == 0) out[X + Y * ld] = e00; else out[Y + X * ld] = e00;
-      } else if (a.bpe_a == 1) {
-        e01 = v[1];
-        if (pass == 0) { out[X + Y * ld] = e00; out[X + (Y + 1) * ld] = e01; }
-        else { out[Y + X * ld] = e00; out[(Y + 1) + X * ld] = e01; }
-      } else if (a.bpe_b == 1) {
-        e10 = v[1];
-        if (pass == 0) { out[X + Y * ld] = e00; out[(X + 1) + Y * ld] = e10; }
-        else { out[Y + X * ld] = e00; out[Y + (X + 1) * ld] = e10; }
-      } else {
-        e01 = v[1]; e10 = v[1]; e11 = v[NC > 2 ? 2 : 0];
-        if (pass == 0) {
-          out[X + Y * ld] = e00; out[X + 1 + Y * ld] = e10;
-          out[X + (Y + 1) * ld] = e01; out[X + 1 + (Y + 1) * ld] = e11;
-        } else {
-          out[Y + X * ld] = e00; out[Y + 1 + X * ld] = e01;
-          out[Y + (X + 1) * ld] = e10; out[Y + 1 + (X + 1) * ld] = e11;
+      if (!tile_entry(pass, q, NR, NCc, diag, &i, &j)) continue;
+      const cx<double>* sl = slots + (size_t)(i * TE + j) * 4 * NC;
+      const double L = a.elen_a[RB->e0 + i] * a.elen_b[CB->e0 + j];
+      cx<double> v[3];
+      for (int c = 0; c < NC; c++) v[c] = L * ((sl[c] - sl[NC + c]) - (sl[2 * NC + c] - sl[3 * NC + c]));
+      store_entry(a, out, pass, RB->e0 + i, CB->e0 + j, v[0], NC > 1 ? v[1] : v[0], NC > 2 ? v[2] : v[0]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision far field: the same tiles on the FP32 pipes in
+// float-float arithmetic (ffmath.cuh).  Node positions and pair geometry
+// are float-float offsets from the tile's origin (split from FP64), the
+// moments and the H0/H1 combinations are float-float, and the slots of the
+// H0 channels keep hi + lo, so the four P/M contributions of an edge pair
+// cancel without loss; each entry is rounded to complex64 once, at the
+// store.  The H1 channel (no cancellation between the four contributions)
+// is rounded to FP32 in its slot.
+// ---------------------------------------------------------------------------
+constexpr int NODE_STRIDE = 37;  // floats per panel: 6 nodes x (3 hi + 3 lo), + 1 (bank spread)
+constexpr int GEO_STRIDE = 19;   // floats per panel: V0 - O, A, B as float-float, + 1
+
+template <int NC> constexpr int ff_channels() { return NC == 3 ? 2 : 1; }
+template <int NC> constexpr size_t tile_ff_smem() {
+  return (size_t)TE * TE * 4 * (NC + ff_channels<NC>()) * sizeof(cx<float>) +
+         (size_t)2 * PMAX * (NODE_STRIDE + GEO_STRIDE) * sizeof(float) + sizeof(SinCosTab);
+}
+
+GB_HD cff cff_at(const cx<float>& hi, const cx<float>& lo) { return cffv(ffv(hi.re, lo.re), ffv(hi.im, lo.im)); }
+
+template <int NC>
+__global__ void __launch_bounds__(256) tile_kernel_ff(TileArgs a, RegionArgs ra) {
+  constexpr int NH = ff_channels<NC>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<float>* slots = reinterpret_cast<cx<float>*>(smem_raw);  // [TE][TE][4][NC] (hi)
+  cx<float>* slots_lo = slots + (size_t)TE * TE * 4 * NC;      // [TE][TE][4][NH]: lo of the H0 channels
+  float* s_node = reinterpret_cast<float*>(slots_lo + (size_t)TE * TE * 4 * NH);  // [2][PMAX][NODE_STRIDE]
+  float* s_geo = s_node + 2 * PMAX * NODE_STRIDE;                                   // [2][PMAX][GEO_STRIDE]
+  SinCosTab* s_tab = reinterpret_cast<SinCosTab*>(s_geo + 2 * PMAX * GEO_STRIDE);
+  __shared__ double s_pc[2][PMAX][4];
+  __shared__ int8_t s_hl[2][3 * PMAX], s_hs[2][3 * PMAX];
+  __shared__ int s_gp[2][PMAX];
+  __shared__ float s_cf[2][PMAX][4];
+  __shared__ float s_el[2][2][TE];  // edge lengths as float-float: [side][hi, lo][edge]
+  __shared__ FFRule s_rule;
+  __shared__ cff s_k[2], s_m4[2], s_p1[2], s_p3[2];  // s_k[r] = (Re k, Im k) as float-float
+  __shared__ cx<float> s_pcf[2];
+  __shared__ int s_live[2];
+
+  const int2 tile = a.tiles[blockIdx.x];
+  const DevEdgeBlock* RB = a.rows + tile.x;
+  const DevEdgeBlock* CB = a.cols + tile.y;
+  const int PR = RB->np, PC = CB->np, NR = RB->ne, NCc = CB->ne;
+  for (int q = threadIdx.x; q < PR * 4; q += blockDim.x) s_pc[0][q / 4][q % 4] = a.pc[4 * (size_t)RB->panels[q / 4] + q % 4];
+  for (int q = threadIdx.x; q < PC * 4; q += blockDim.x) s_pc[1][q / 4][q % 4] = a.pc[4 * (size_t)CB->panels[q / 4] + q % 4];
+  for (int q = threadIdx.x; q < 3 * PR; q += blockDim.x) { s_hl[0][q] = RB->hl[q]; s_hs[0][q] = RB->hs[q]; }
+  for (int q = threadIdx.x; q < 3 * PC; q += blockDim.x) { s_hl[1][q] = CB->hl[q]; s_hs[1][q] = CB->hs[q]; }
+  for (int q = threadIdx.x; q < PR; q += blockDim.x) s_gp[0][q] = RB->panels[q];
+  for (int q = threadIdx.x; q < PC; q += blockDim.x) s_gp[1][q] = CB->panels[q];
+  for (int q = threadIdx.x; q < (int)(sizeof(SinCosTab) / 4); q += blockDim.x)
+    reinterpret_cast<float*>(s_tab)[q] = reinterpret_cast<const float*>(&c_sctab)[q];
+  for (int q = threadIdx.x; q < (int)(sizeof(FFRule) / 4); q += blockDim.x)
+    reinterpret_cast<float*>(&s_rule)[q] = reinterpret_cast<const float*>(&c_ffrule)[q];
+  // per panel: float-float geometry and quadrature nodes relative to the
+  // tile's origin O (V0 of its first row panel), formed in FP64
+  const double* O = a.pv + 9 * (size_t)RB->panels[0];
+  for (int q = threadIdx.x; q < 2 * PMAX; q += blockDim.x) {
+    const int side = q / PMAX, p = q % PMAX;
+    if (p >= (side ? PC : PR)) continue;
+    const size_t gp = side ? CB->panels[p] : RB->panels[p];
+    const double* V = a.pv + 9 * gp;
+    float* G = s_geo + (side * PMAX + p) * GEO_STRIDE;
+    float* X = s_node + (side * PMAX + p) * NODE_STRIDE;
+    double v0[3], A[3], B[3];
+    for (int c = 0; c < 3; c++) { v0[c] = V[c] - O[c]; A[c] = V[3 + c] - V[c]; B[c] = V[6 + c] - V[c]; }
+    for (int c = 0; c < 3; c++) {
+      ff t = ff_of(v0[c]);
+      G[c] = t.hi; G[3 + c] = t.lo;
+      t = ff_of(A[c]);
+      G[6 + c] = t.hi; G[9 + c] = t.lo;
+      t = ff_of(B[c]);
+      G[12 + c] = t.hi; G[15 + c] = t.lo;
+    }
+    for (int i = 0; i < 6; i++) {
+      const double u = c_lo64[3 * i], v = c_lo64[3 * i + 1];
+      for (int c = 0; c < 3; c++) {
+        const ff t = ff_of(v0[c] + u * A[c] + v * B[c]);
+        X[6 * i + c] = t.hi; X[6 * i + 3 + c] = t.lo;
+      }
+    }
+    for (int c = 0; c < 4; c++) s_cf[side][p][c] = (float)a.pc[4 * gp + c];
+  }
+  for (int q = threadIdx.x; q < 2 * TE; q += blockDim.x) {
+    const int side = q / TE, e = q % TE;
+    if (e < (side ? NCc : NR)) {
+      const ff l = ff_of(side ? a.elen_b[CB->e0 + e] : a.elen_a[RB->e0 + e]);
+      s_el[side][0][e] = l.hi;
+      s_el[side][1][e] = l.lo;
+    }
+  }
+  if (threadIdx.x < 2) {
+    // region constants, formed once per CTA in FP64
+    const int r = threadIdx.x;
+    const cx<double> kd = r < ra.nreg ? ra.k[r] : mk(0.0, 0.0);
+    const bool live = !(kd.re == 0.0 && kd.im == 0.0);
+    s_live[r] = live;
+    s_k[r] = cff_of(kd);
+    s_m4[r] = live ? cff_of(cdiv(mk(-4.0, 0.0), kd * kd)) : cff_zero();
+    s_p1[r] = live ? cff_of(ra.pf1[r]) : cff_zero();
+    s_p3[r] = live ? cff_of(ra.pf3[r]) : cff_zero();
+    s_pcf[r] = live ? mk((float)ra.pfc[r].re, (float)ra.pfc[r].im) : mk(0.0f, 0.0f);
+  }
+  __syncthreads();
+
+  constexpr int R2 = NC == 1 ? 1 : 2;
+  for (int q = threadIdx.x; q < PR * PC; q += blockDim.x) {
+    const int ia = q / PC, ib = q - ia * PC;
+    int la[3], lb[3], sa[3], sb[3];
+    for (int j = 0; j < 3; j++) {
+      la[j] = s_hl[0][3 * ia + j]; sa[j] = s_hs[0][3 * ia + j];
+      lb[j] = s_hl[1][3 * ib + j]; sb[j] = s_hs[1][3 * ib + j];
+    }
+    if (tile_pair_far(s_cf[0][ia], s_cf[1][ib], s_pc[0][ia], s_pc[1][ib])) {
+      const float* Ga = s_geo + ia * GEO_STRIDE;
+      const float* Gb = s_geo + (PMAX + ib) * GEO_STRIDE;
+      FFGeom g;
+      for (int c = 0; c < 3; c++) {
+        g.Aa[c] = ffv(Ga[6 + c], Ga[9 + c]); g.Ba[c] = ffv(Ga[12 + c], Ga[15 + c]);
+        g.Ab[c] = ffv(Gb[6 + c], Gb[9 + c]); g.Bb[c] = ffv(Gb[12 + c], Gb[15 + c]);
+        g.D0[c] = ff_sub(ffv(Ga[c], Ga[3 + c]), ffv(Gb[c], Gb[3 + c]));
+      }
+      ff D[2][2];
+      h0_dots(g, D);
+      H1Pre p1;
+      if (NC > 1) h1_prepare(g, &p1);
+      for (int r = 0; r < R2; r++) {
+        const bool live = s_live[r];
+        cff MP[9];
+        H0Pre p0;
+        if (live) {
+          cff MG[9];
+          pair_moments_ff<6>(s_node + ia * NODE_STRIDE, s_node + (PMAX + ib) * NODE_STRIDE, s_k[r].re, s_k[r].im,
+                             &s_rule, s_tab, MG, MP);
+          h0_prepare(D, MG, &p0);
+        }
+#pragma unroll 1
+        for (int ja = 0; ja < 3; ja++) {
+          if (la[ja] < 0) continue;
+#pragma unroll 1
+          for (int jb = 0; jb < 3; jb++) {
+            if (lb[jb] < 0) continue;
+            cff v0 = cff_zero(), v2 = cff_zero();
+            cx<float> v1 = mk(0.0f, 0.0f);
+            if (live) {
+              const cff H0 = h0_combo(p0, ja, jb, s_m4[r]);
+              v0 = cff_mul(s_p1[r], H0);
+              if (NC > 2) v2 = cff_mul(s_p3[r], H0);
+              if (NC > 1) {
+                const cff H1 = h1_combo(p1, ja, jb, MP);
+                v1 = s_pcf[r] * mk(H1.re.hi + H1.re.lo, H1.im.hi + H1.im.lo);
+              }
+            }
+            const size_t slot = (size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb];
+            cx<float>* hi = slots + slot * NC;
+            cx<float>* lo = slots_lo + slot * NH;
+            if (r > 0) {
+              v0 = cff_add(v0, cff_at(hi[0], lo[0]));
+              if (NC > 1) v1 = v1 + hi[1];
+              if (NC > 2) v2 = cff_add(v2, cff_at(hi[2], lo[1]));
+            }
+            hi[0] = cff_hi(v0); lo[0] = cff_lo(v0);
+            if (NC > 1) hi[1] = v1;
+            if (NC > 2) { hi[2] = cff_hi(v2); lo[1] = cff_lo(v2); }
+          }
         }
       }
+    } else {
+      // near pair: values precomputed in FP64 by self_kernel / near_kernel
+      const int hit = near_hit(a, s_gp[0][ia], s_gp[1][ib]);
+      if (hit < 0) continue;  // cannot happen: every rRel<=4 pair is listed
+      const double* nv = a.nearval + 54 * (size_t)(hit >> 1);
+      const bool tr = hit & 1;
+      for (int ja = 0; ja < 3; ja++) {
+        if (la[ja] < 0) continue;
+        for (int jb = 0; jb < 3; jb++) {
+          if (lb[jb] < 0) continue;
+          const double* v = nv + 6 * (tr ? (3 * jb + ja) : (3 * ja + jb));
+          const size_t slot = (size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb];
+          cx<float>* hi = slots + slot * NC;
+          cx<float>* lo = slots_lo + slot * NH;
+          const cff v0 = cff_of(mk(v[0], v[1]));
+          hi[0] = cff_hi(v0); lo[0] = cff_lo(v0);
+          if (NC > 1) hi[1] = mk((float)v[2], (float)v[3]);
+          if (NC > 2) {
+            const cff v2 = cff_of(mk(v[4], v[5]));
+            hi[2] = cff_hi(v2); lo[1] = cff_lo(v2);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // entries: the four P/M contributions combined in float-float (H0
+  // channels), times La Lb, rounded to complex64
+  cx<float>* out = reinterpret_cast<cx<float>*>(a.out);
+  const bool diag = a.sym && tile.x == tile.y;
+  for (int pass = 0; pass < 2; pass++) {
+    if (!(a.passes & (1 << pass))) continue;
+    for (int q = threadIdx.x; q < NR * NCc; q += blockDim.x) {
+      int i, j;
+      if (!tile_entry(pass, q, NR, NCc, diag, &i, &j)) continue;
+      const cx<float>* hi = slots + (size_t)(i * TE + j) * 4 * NC;
+      const cx<float>* lo = slots_lo + (size_t)(i * TE + j) * 4 * NH;
+      // La Lb as float-float: an FP32 product would scale every row and
+      // column of an edge by its own rounding, which the right-hand side and
+      // the power integrals do not share
+      const ff L = ff_mul(ffv(s_el[0][0][i], s_el[0][1][i]), ffv(s_el[1][0][j], s_el[1][1][j]));
+      cx<float> v[3];
+      for (int c = 0; c < NC; c++) {
+        if (c == 1) {
+          const cx<float> x = (hi[1] - hi[NC + 1]) - (hi[2 * NC + 1] - hi[3 * NC + 1]);
+          v[1] = mk(fmaf(L.hi, x.re, L.lo * x.re), fmaf(L.hi, x.im, L.lo * x.im));
+        } else {
+          const int h = c == 0 ? 0 : 1;
+          const cff x = cff_sub(cff_sub(cff_at(hi[c], lo[h]), cff_at(hi[NC + c], lo[NH + h])),
+                                cff_sub(cff_at(hi[2 * NC + c], lo[2 * NH + h]), cff_at(hi[3 * NC + c], lo[3 * NH + h])));
+          const cff y = cff_mul_ff(x, L);
+          v[c] = mk(y.re.hi + y.re.lo, y.im.hi + y.im.lo);
+        }
+      }
+      store_entry(a, out, pass, RB->e0 + i, CB->e0 + j, v[0], NC > 1 ? v[1] : v[0], NC > 2 ? v[2] : v[0]);
     }
   }
 }
 
 static inline cx<double> cxd(double r, double i) { return mk(r, i); }
 
-template <typename T, int NC>
-static cudaError_t launch_tiles(const TileArgs& ta, const RegionArgs& ra, int ntiles, cudaStream_t s) {
-  size_t smem = (size_t)TE * TE * 4 * NC * sizeof(cx<T>);
-  cudaError_t e = cudaFuncSetAttribute(tile_kernel<T, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int NC>
+static cudaError_t launch_tiles64(const TileArgs& ta, const RegionArgs& ra, int ntiles, cudaStream_t s) {
+  const size_t smem = (size_t)TE * TE * 4 * NC * sizeof(cx<double>);
+  cudaError_t e = cudaFuncSetAttribute(tile_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  tile_kernel<T, NC><<<ntiles, 256, smem, s>>>(ta, ra);
+  tile_kernel<NC><<<ntiles, 256, smem, s>>>(ta, ra);
+  return cudaGetLastError();
+}
+
+template <int NC>
+static cudaError_t launch_tiles_ff(const TileArgs& ta, const RegionArgs& ra, int ntiles, cudaStream_t s) {
+  const size_t smem = tile_ff_smem<NC>();
+  cudaError_t e = cudaFuncSetAttribute(tile_kernel_ff<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  tile_kernel_ff<NC><<<ntiles, 256, smem, s>>>(ta, ra);
   return cudaGetLastError();
 }
 
@@ -843,11 +1009,11 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
     StatTimer tf(ST_FAR, s);
     stats_launch(ST_FAR);
     if (precision == GBEM_PREC_MIXED) {
-      e = nc == 1 ? launch_tiles<float, 1>(ta, ra, db->ntiles, s)
-                  : nc == 2 ? launch_tiles<float, 2>(ta, ra, db->ntiles, s) : launch_tiles<float, 3>(ta, ra, db->ntiles, s);
+      e = nc == 1 ? launch_tiles_ff<1>(ta, ra, db->ntiles, s)
+                  : nc == 2 ? launch_tiles_ff<2>(ta, ra, db->ntiles, s) : launch_tiles_ff<3>(ta, ra, db->ntiles, s);
     } else {
-      e = nc == 1 ? launch_tiles<double, 1>(ta, ra, db->ntiles, s)
-                  : nc == 2 ? launch_tiles<double, 2>(ta, ra, db->ntiles, s) : launch_tiles<double, 3>(ta, ra, db->ntiles, s);
+      e = nc == 1 ? launch_tiles64<1>(ta, ra, db->ntiles, s)
+                  : nc == 2 ? launch_tiles64<2>(ta, ra, db->ntiles, s) : launch_tiles64<3>(ta, ra, db->ntiles, s);
     }
     if (e != cudaSuccess) return cuda_status(e, "tile_kernel");
   }

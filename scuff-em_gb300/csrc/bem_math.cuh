@@ -210,32 +210,6 @@ GB_HD void combo_coeffs(const double* Va, const double* Vb, int ja, int jb, doub
     }
 }
 
-// The same coefficients from a pair's relative geometry in precision T
-// (the far-field tile kernel's arithmetic): with Q the ja-th vertex,
-// V0a - Qa is 0, -Aa or -Ba, and Qa - Qb = D0 - a0 + b0.
-template <typename T>
-GB_HD void combo_coeffs_t(const PairGeom<T>& g, int ja, int jb, T* c, T* d) {
-  T a0[3], b0[3], q[3];
-  for (int i = 0; i < 3; i++) {
-    a0[i] = ja == 0 ? (T)0 : (ja == 1 ? -g.Aa[i] : -g.Ba[i]);
-    b0[i] = jb == 0 ? (T)0 : (jb == 1 ? -g.Ab[i] : -g.Bb[i]);
-    q[i] = g.D0[i] - a0[i] + b0[i];
-  }
-#define GB_DOT(x, y) (x[0] * y[0] + x[1] * y[1] + x[2] * y[2])
-#define GB_DET(x, y) ((x[1] * y[2] - x[2] * y[1]) * q[0] + (x[2] * y[0] - x[0] * y[2]) * q[1] + (x[0] * y[1] - x[1] * y[0]) * q[2])
-  c[0] = GB_DOT(a0, b0);     d[0] = GB_DET(a0, b0);
-  c[1] = GB_DOT(a0, g.Ab);   d[1] = GB_DET(a0, g.Ab);
-  c[2] = GB_DOT(a0, g.Bb);   d[2] = GB_DET(a0, g.Bb);
-  c[3] = GB_DOT(g.Aa, b0);   d[3] = GB_DET(g.Aa, b0);
-  c[4] = GB_DOT(g.Aa, g.Ab); d[4] = GB_DET(g.Aa, g.Ab);
-  c[5] = GB_DOT(g.Aa, g.Bb); d[5] = GB_DET(g.Aa, g.Bb);
-  c[6] = GB_DOT(g.Ba, b0);   d[6] = GB_DET(g.Ba, b0);
-  c[7] = GB_DOT(g.Ba, g.Ab); d[7] = GB_DET(g.Ba, g.Ab);
-  c[8] = GB_DOT(g.Ba, g.Bb); d[8] = GB_DET(g.Ba, g.Bb);
-#undef GB_DOT
-#undef GB_DET
-}
-
 // Vector form of a pair's moments.  With u = x - V0a = u Aa + v Ba and
 // v = x' - V0b = u' Ab + v' Bb:
 //   W0 = int G,  Wx = int u G,  Wy = int v G,  Wxy = int u.v G,

@@ -413,21 +413,21 @@ __device__ __forceinline__ void warp_cand(unsigned vb, int row, unsigned& wvb, i
   wrow = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
 }
 
-template <int RT>
-__global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
+template <int RT, int NT>
+__global__ void __launch_bounds__(NT, 1) leaf_kernel_reg(LeafArgs a) {
   cg::cluster_group cl = cg::this_cluster();
   __shared__ Cand pub[2];
   __shared__ __align__(16) cx<float> prow[2][LEAF_W];
   __shared__ __align__(16) cx<float> drow[2][LEAF_W];
-  __shared__ __align__(16) cx<float> wrow[16][LEAF_W];
-  __shared__ unsigned w_vb[16];
-  __shared__ int w_row[16];
+  constexpr int NW = NT / 32;
+  __shared__ __align__(16) cx<float> wrow[NW][LEAF_W];
+  __shared__ unsigned w_vb[NW];
+  __shared__ int w_row[NW];
   __shared__ __align__(16) cx<float> allrows[16][LEAF_W];  // every CTA's candidate row
   __shared__ __align__(16) cx<float> dcopy[LEAF_W];        // the diagonal row before the interchange
   __shared__ int s_p, s_own;
   const int rank = (int)cl.block_rank(), CL = (int)cl.num_blocks();
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  constexpr int NT = 512;
   const int w = a.w;
   const int m0 = a.c0 + rank * a.Rr;
   const int nr = max(0, min(a.Rr, a.N - m0));
@@ -488,8 +488,8 @@ __global__ void __launch_bounds__(512, 1) leaf_kernel_reg(LeafArgs a) {
     }
     __syncthreads();
     if (warp == 0) {
-      const unsigned vb = lane < 16 ? w_vb[lane] : 0u;
-      const int rw = lane < 16 ? w_row[lane] : 0x7fffffff;
+      const unsigned vb = lane < NW ? w_vb[lane] : 0u;
+      const int rw = lane < NW ? w_row[lane] : 0x7fffffff;
       const unsigned mx = __reduce_max_sync(0xffffffffu, rw != 0x7fffffff ? vb : 0u);
       const int cand = (rw != 0x7fffffff && vb == mx) ? rw : 0x7fffffff;
       const int best = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
@@ -726,9 +726,11 @@ static int leaf_cluster_size(int N, int smem_optin) {
     if (smem + 2048 > (size_t)smem_optin) continue;
     if (cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) continue;
     if (CL > 8 && (cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
-                   cudaFuncSetAttribute(leaf_kernel_reg<1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                   cudaFuncSetAttribute(leaf_kernel_reg<1, 1024>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                        cudaSuccess ||
-                   cudaFuncSetAttribute(leaf_kernel_reg<2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                   cudaFuncSetAttribute(leaf_kernel_reg<1, 512>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                       cudaSuccess ||
+                   cudaFuncSetAttribute(leaf_kernel_reg<2, 512>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                        cudaSuccess))
       continue;
     cudaLaunchConfig_t cfg = {};
@@ -763,8 +765,20 @@ static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w,
   cfg.attrs = at;
   cfg.numAttrs = 1;
   // rows in registers when each thread holds at most two, else in shared memory
-  if (la.Rr <= 512) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<1>, la);
-  if (la.Rr <= 1024) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<2>, la);
+  // 512-thread CTAs holding up to two rows per thread measured faster than
+  // 1024-thread CTAs with one row each (45.7 vs 49.8 us per 16-column leaf
+  // at 960 rows per CTA); GBEM_LU_LEAF_THREADS=1024 selects the latter
+  static int threads = -1;
+  if (threads < 0) {
+    const char* e = getenv("GBEM_LU_LEAF_THREADS");
+    threads = (e && atoi(e) == 1024) ? 1024 : 512;
+  }
+  if (la.Rr <= 1024 && threads == 1024) {
+    cfg.blockDim = dim3(1024);
+    return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<1, 1024>, la);
+  }
+  if (la.Rr <= 512) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<1, 512>, la);
+  if (la.Rr <= 1024) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<2, 512>, la);
   cfg.dynamicSmemBytes = (size_t)la.Rr * LEAF_STRIDE * sizeof(cx<float>);
   return cudaLaunchKernelEx(&cfg, leaf_kernel, la);
 }
