@@ -129,6 +129,16 @@ struct DevBlock {
   int* other_list = nullptr;
   Fippi* fippi = nullptr;     // per near pair (unused slots for self pairs)
   double* nearval = nullptr;  // 27 complex per near pair
+  // column stripes of the mixed far field
+  struct DevStripe {
+    int nrow = 0, ncp = 0, ntiles = 0;
+    int* cpan = nullptr;
+    int2* tiles = nullptr;
+  };
+  std::vector<DevStripe> stripes;
+  int4* edge_a = nullptr;  // per row edge: P panel, its Q index, M panel, its Q index
+  int4* edge_b = nullptr;  // per column edge, likewise
+  int2* ecol = nullptr;    // per column edge: stripe-local P, M panel index
 };
 
 template <typename Tp>
@@ -199,8 +209,50 @@ gbem_status upload_geometry(Geometry* g) {
     if (e == cudaSuccess) e = dupload(&db->other_list, others.data(), others.size());
     if (e == cudaSuccess && db->nnear) e = cudaMalloc((void**)&db->fippi, sizeof(Fippi) * db->nnear);
     if (e == cudaSuccess && db->nnear) e = cudaMalloc((void**)&db->nearval, sizeof(double) * 54 * db->nnear);
+    // edge tables and column stripes of the mixed far field
+    auto edge4 = [](const Surface& S) {
+      std::vector<int4> t(S.ne);
+      for (int i = 0; i < S.ne; i++) t[i] = make_int4(S.E[8 * i + 4], S.E[8 * i + 6], S.E[8 * i + 5], S.E[8 * i + 7]);
+      return t;
+    };
+    const std::vector<int4> ea = edge4(g->S[b.sa]), eb = edge4(g->S[b.sb]);
+    if (e == cudaSuccess) e = dupload(&db->edge_a, ea.data(), ea.size());
+    if (e == cudaSuccess) e = dupload(&db->edge_b, eb.data(), eb.size());
+    if (e == cudaSuccess) e = dupload(&db->ecol, b.ecol.data(), b.ecol.size());
+    for (const Stripe& st : b.stripes) {
+      DevBlock::DevStripe ds;
+      ds.nrow = st.nrow; ds.ncp = (int)st.cpan.size(); ds.ntiles = (int)st.tiles.size();
+      if (e == cudaSuccess) e = dupload(&ds.cpan, st.cpan.data(), st.cpan.size());
+      if (e == cudaSuccess) e = dupload(&ds.tiles, st.tiles.data(), st.tiles.size());
+      db->stripes.push_back(ds);
+    }
     if (e != cudaSuccess) return cuda_status(e, "upload blocks");
   }
+  // float-float rule nodes and geometry of every panel, relative to the mean
+  // vertex (the mixed far field's positions: ~48 bits relative to that origin)
+  double O[3] = {0.0, 0.0, 0.0};
+  for (size_t gp = 0; gp < (size_t)g->np_total; gp++)
+    for (int c = 0; c < 3; c++) O[c] += (pv[9 * gp + c] + pv[9 * gp + 3 + c] + pv[9 * gp + 6 + c]) / (3.0 * g->np_total);
+  std::vector<float> node(36 * (size_t)g->np_total), geo(18 * (size_t)g->np_total);
+  for (size_t gp = 0; gp < (size_t)g->np_total; gp++) {
+    const double* V = pv.data() + 9 * gp;
+    double v0[3], A[3], B[3];
+    for (int c = 0; c < 3; c++) { v0[c] = V[c] - O[c]; A[c] = V[3 + c] - V[c]; B[c] = V[6 + c] - V[c]; }
+    for (int c = 0; c < 3; c++) {
+      const ff x = ff_of(v0[c]), y = ff_of(A[c]), z = ff_of(B[c]);
+      geo[18 * gp + c] = x.hi; geo[18 * gp + 3 + c] = x.lo;
+      geo[18 * gp + 6 + c] = y.hi; geo[18 * gp + 9 + c] = y.lo;
+      geo[18 * gp + 12 + c] = z.hi; geo[18 * gp + 15 + c] = z.lo;
+    }
+    for (int i = 0; i < 6; i++)
+      for (int c = 0; c < 3; c++) {
+        const ff x = ff_of(v0[c] + h_lo[3 * i] * A[c] + h_lo[3 * i + 1] * B[c]);
+        node[36 * gp + 6 * i + c] = x.hi; node[36 * gp + 6 * i + 3 + c] = x.lo;
+      }
+  }
+  e = dupload(&g->d_ffnode, node.data(), node.size());
+  if (e == cudaSuccess) e = dupload(&g->d_ffgeo, geo.data(), geo.size());
+  if (e != cudaSuccess) return cuda_status(e, "upload float-float panels");
   return GBEM_OK;
 }
 
@@ -211,9 +263,15 @@ void free_geometry_device(Geometry* g) {
     cudaFree(db->rows); cudaFree(db->cols); cudaFree(db->tiles); cudaFree(db->elen_a); cudaFree(db->elen_b);
     cudaFree(db->nptr); cudaFree(db->ncol); cudaFree(db->nidx); cudaFree(db->near); cudaFree(db->self_list);
     cudaFree(db->other_list); cudaFree(db->fippi); cudaFree(db->nearval);
+    cudaFree(db->edge_a); cudaFree(db->edge_b); cudaFree(db->ecol);
+    for (auto& st : db->stripes) { cudaFree(st.cpan); cudaFree(st.tiles); }
     delete db;
   }
   g->dblocks.clear();
+  cudaFree(g->d_ffnode); cudaFree(g->d_ffgeo); cudaFree(g->ppv);
+  g->d_ffnode = g->d_ffgeo = nullptr;
+  g->ppv = nullptr;
+  g->ppv_bytes = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -614,99 +672,74 @@ __global__ void __launch_bounds__(256) tile_kernel(TileArgs a, RegionArgs ra) {
 }
 
 // ---------------------------------------------------------------------------
-// Mixed-precision far field: the same tiles on the FP32 pipes in
-// float-float arithmetic (ffmath.cuh).  Node positions and pair geometry
-// are float-float offsets from the tile's origin (split from FP64), the
-// moments and the H0/H1 combinations are float-float, and the slots of the
-// H0 channels keep hi + lo, so the four P/M contributions of an edge pair
-// cancel without loss; each entry is rounded to complex64 once, at the
-// store.  The H1 channel (no cancellation between the four contributions)
-// is rounded to FP32 in its slot.
+// Mixed-precision far field, on the FP32 pipes in float-float arithmetic
+// (ffmath.cuh), in two passes per column stripe of a block:
+//  1. ppair_kernel: every far panel pair (row panel, stripe column panel)
+//     once -- moments for each common region, then the slot values of all 9
+//     (Qa, Qb) choices, EE/HH channels as float-float and the EH channel in
+//     FP32 -- into a scratch buffer; near pairs get a NaN marker.
+//  2. stamp_kernel: per edge tile, each entry sums its four (P/M, P/M)
+//     values (from the buffer, or from the FP64 near table) in float-float,
+//     applies La Lb, rounds to complex64 once, and is written with its mirror.
+// Computing each panel pair once (the tile kernel recomputes a panel pair in
+// every tile that touches it, ~2.4x over on an icosphere) and without the
+// 190 KB of float-float slots per CTA is what makes the float-float form
+// affordable.
 // ---------------------------------------------------------------------------
-constexpr int NODE_STRIDE = 37;  // floats per panel: 6 nodes x (3 hi + 3 lo), + 1 (bank spread)
-constexpr int GEO_STRIDE = 19;   // floats per panel: V0 - O, A, B as float-float, + 1
+constexpr int NODE_STRIDE = 37;  // floats per panel in shared memory: 6 nodes x (3 hi + 3 lo), + 1 (bank spread)
+constexpr int GEO_STRIDE = 19;   // floats per panel in shared memory: V0 - O, A, B as float-float, + 1
 
-template <int NC> constexpr int ff_channels() { return NC == 3 ? 2 : 1; }
-template <int NC> constexpr size_t tile_ff_smem() {
-  return (size_t)TE * TE * 4 * (NC + ff_channels<NC>()) * sizeof(cx<float>) +
-         (size_t)2 * PMAX * (NODE_STRIDE + GEO_STRIDE) * sizeof(float) + sizeof(SinCosTab);
-}
+template <int NC> constexpr int ppair_fields() { return NC == 1 ? 4 : (NC == 2 ? 6 : 10); }
 
-GB_HD cff cff_at(const cx<float>& hi, const cx<float>& lo) { return cffv(ffv(hi.re, lo.re), ffv(hi.im, lo.im)); }
+struct PPairArgs {
+  const float* node;  // per global panel: 36 floats (float-float rule nodes)
+  const float* geo;   // per global panel: 18 floats (float-float V0 - O, A, B)
+  const double* pc;   // per global panel: centroid, radius
+  const int* cpan;    // the stripe's column panels (surface-local)
+  int offa, offb;     // global index of the first panel of each surface
+  int nrow, ncp;
+  float* out;         // [NF][9][ncp][nrow]
+};
 
+// pass 1: block (32, 8) = 32 row panels x 8 column panels, one pair per thread
 template <int NC>
-__global__ void __launch_bounds__(256) tile_kernel_ff(TileArgs a, RegionArgs ra) {
-  constexpr int NH = ff_channels<NC>();
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<float>* slots = reinterpret_cast<cx<float>*>(smem_raw);  // [TE][TE][4][NC] (hi)
-  cx<float>* slots_lo = slots + (size_t)TE * TE * 4 * NC;      // [TE][TE][4][NH]: lo of the H0 channels
-  float* s_node = reinterpret_cast<float*>(slots_lo + (size_t)TE * TE * 4 * NH);  // [2][PMAX][NODE_STRIDE]
-  float* s_geo = s_node + 2 * PMAX * NODE_STRIDE;                                   // [2][PMAX][GEO_STRIDE]
-  SinCosTab* s_tab = reinterpret_cast<SinCosTab*>(s_geo + 2 * PMAX * GEO_STRIDE);
-  __shared__ double s_pc[2][PMAX][4];
-  __shared__ int8_t s_hl[2][3 * PMAX], s_hs[2][3 * PMAX];
-  __shared__ int s_gp[2][PMAX];
-  __shared__ float s_cf[2][PMAX][4];
-  __shared__ float s_el[2][2][TE];  // edge lengths as float-float: [side][hi, lo][edge]
+__global__ void __launch_bounds__(256) ppair_kernel(PPairArgs p, RegionArgs ra) {
+  constexpr int NF = ppair_fields<NC>();
+  __shared__ float s_node[40][NODE_STRIDE];
+  __shared__ float s_geo[40][GEO_STRIDE];
+  __shared__ double s_pcd[40][4];
+  __shared__ float s_cf[40][4];
+  __shared__ SinCosTab s_tab;
   __shared__ FFRule s_rule;
   __shared__ cff s_k[2], s_m4[2], s_p1[2], s_p3[2];  // s_k[r] = (Re k, Im k) as float-float
   __shared__ cx<float> s_pcf[2];
   __shared__ int s_live[2];
-
-  const int2 tile = a.tiles[blockIdx.x];
-  const DevEdgeBlock* RB = a.rows + tile.x;
-  const DevEdgeBlock* CB = a.cols + tile.y;
-  const int PR = RB->np, PC = CB->np, NR = RB->ne, NCc = CB->ne;
-  for (int q = threadIdx.x; q < PR * 4; q += blockDim.x) s_pc[0][q / 4][q % 4] = a.pc[4 * (size_t)RB->panels[q / 4] + q % 4];
-  for (int q = threadIdx.x; q < PC * 4; q += blockDim.x) s_pc[1][q / 4][q % 4] = a.pc[4 * (size_t)CB->panels[q / 4] + q % 4];
-  for (int q = threadIdx.x; q < 3 * PR; q += blockDim.x) { s_hl[0][q] = RB->hl[q]; s_hs[0][q] = RB->hs[q]; }
-  for (int q = threadIdx.x; q < 3 * PC; q += blockDim.x) { s_hl[1][q] = CB->hl[q]; s_hs[1][q] = CB->hs[q]; }
-  for (int q = threadIdx.x; q < PR; q += blockDim.x) s_gp[0][q] = RB->panels[q];
-  for (int q = threadIdx.x; q < PC; q += blockDim.x) s_gp[1][q] = CB->panels[q];
-  for (int q = threadIdx.x; q < (int)(sizeof(SinCosTab) / 4); q += blockDim.x)
-    reinterpret_cast<float*>(s_tab)[q] = reinterpret_cast<const float*>(&c_sctab)[q];
-  for (int q = threadIdx.x; q < (int)(sizeof(FFRule) / 4); q += blockDim.x)
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 8;
+  // the CTA's 32 row and 8 column panels (global index, -1 past the end)
+  auto panel_of = [&](int sl) -> int {
+    if (sl < 32) return r0 + sl < p.nrow ? p.offa + r0 + sl : -1;
+    return c0 + sl - 32 < p.ncp ? p.offb + p.cpan[c0 + sl - 32] : -1;
+  };
+  for (int q = tid; q < 40 * 36; q += 256) {
+    const int sl = q / 36, f = q - sl * 36, gp = panel_of(sl);
+    if (gp >= 0) s_node[sl][f] = p.node[36 * (size_t)gp + f];
+  }
+  for (int q = tid; q < 40 * 18; q += 256) {
+    const int sl = q / 18, f = q - sl * 18, gp = panel_of(sl);
+    if (gp >= 0) s_geo[sl][f] = p.geo[18 * (size_t)gp + f];
+  }
+  for (int q = tid; q < 40 * 4; q += 256) {
+    const int sl = q / 4, f = q - sl * 4, gp = panel_of(sl);
+    if (gp >= 0) { s_pcd[sl][f] = p.pc[4 * (size_t)gp + f]; s_cf[sl][f] = (float)p.pc[4 * (size_t)gp + f]; }
+  }
+  for (int q = tid; q < (int)(sizeof(SinCosTab) / 4); q += 256)
+    reinterpret_cast<float*>(&s_tab)[q] = reinterpret_cast<const float*>(&c_sctab)[q];
+  for (int q = tid; q < (int)(sizeof(FFRule) / 4); q += 256)
     reinterpret_cast<float*>(&s_rule)[q] = reinterpret_cast<const float*>(&c_ffrule)[q];
-  // per panel: float-float geometry and quadrature nodes relative to the
-  // tile's origin O (V0 of its first row panel), formed in FP64
-  const double* O = a.pv + 9 * (size_t)RB->panels[0];
-  for (int q = threadIdx.x; q < 2 * PMAX; q += blockDim.x) {
-    const int side = q / PMAX, p = q % PMAX;
-    if (p >= (side ? PC : PR)) continue;
-    const size_t gp = side ? CB->panels[p] : RB->panels[p];
-    const double* V = a.pv + 9 * gp;
-    float* G = s_geo + (side * PMAX + p) * GEO_STRIDE;
-    float* X = s_node + (side * PMAX + p) * NODE_STRIDE;
-    double v0[3], A[3], B[3];
-    for (int c = 0; c < 3; c++) { v0[c] = V[c] - O[c]; A[c] = V[3 + c] - V[c]; B[c] = V[6 + c] - V[c]; }
-    for (int c = 0; c < 3; c++) {
-      ff t = ff_of(v0[c]);
-      G[c] = t.hi; G[3 + c] = t.lo;
-      t = ff_of(A[c]);
-      G[6 + c] = t.hi; G[9 + c] = t.lo;
-      t = ff_of(B[c]);
-      G[12 + c] = t.hi; G[15 + c] = t.lo;
-    }
-    for (int i = 0; i < 6; i++) {
-      const double u = c_lo64[3 * i], v = c_lo64[3 * i + 1];
-      for (int c = 0; c < 3; c++) {
-        const ff t = ff_of(v0[c] + u * A[c] + v * B[c]);
-        X[6 * i + c] = t.hi; X[6 * i + 3 + c] = t.lo;
-      }
-    }
-    for (int c = 0; c < 4; c++) s_cf[side][p][c] = (float)a.pc[4 * gp + c];
-  }
-  for (int q = threadIdx.x; q < 2 * TE; q += blockDim.x) {
-    const int side = q / TE, e = q % TE;
-    if (e < (side ? NCc : NR)) {
-      const ff l = ff_of(side ? a.elen_b[CB->e0 + e] : a.elen_a[RB->e0 + e]);
-      s_el[side][0][e] = l.hi;
-      s_el[side][1][e] = l.lo;
-    }
-  }
-  if (threadIdx.x < 2) {
+  if (tid < 2) {
     // region constants, formed once per CTA in FP64
-    const int r = threadIdx.x;
+    const int r = tid;
     const cx<double> kd = r < ra.nreg ? ra.k[r] : mk(0.0, 0.0);
     const bool live = !(kd.re == 0.0 && kd.im == 0.0);
     s_live[r] = live;
@@ -718,123 +751,150 @@ __global__ void __launch_bounds__(256) tile_kernel_ff(TileArgs a, RegionArgs ra)
   }
   __syncthreads();
 
+  const int pa = r0 + threadIdx.x, cl = c0 + threadIdx.y;
+  if (pa >= p.nrow || cl >= p.ncp) return;
+  const int ia = threadIdx.x, ib = 32 + threadIdx.y;
+  const size_t cs = (size_t)p.ncp * p.nrow;  // stride of one (field, combination) plane
+  float* out = p.out + (size_t)cl * p.nrow + pa;
+  if (!tile_pair_far(s_cf[ia], s_cf[ib], s_pcd[ia], s_pcd[ib])) {
+    const float marker = __int_as_float(0x7fc00000);  // quiet NaN: a near pair
+    for (int c = 0; c < 9; c++) out[c * cs] = marker;
+    return;
+  }
+  FFGeom g;
+  for (int c = 0; c < 3; c++) {
+    g.Aa[c] = ffv(s_geo[ia][6 + c], s_geo[ia][9 + c]); g.Ba[c] = ffv(s_geo[ia][12 + c], s_geo[ia][15 + c]);
+    g.Ab[c] = ffv(s_geo[ib][6 + c], s_geo[ib][9 + c]); g.Bb[c] = ffv(s_geo[ib][12 + c], s_geo[ib][15 + c]);
+    g.D0[c] = ff_sub(ffv(s_geo[ia][c], s_geo[ia][3 + c]), ffv(s_geo[ib][c], s_geo[ib][3 + c]));
+  }
+  ff D[2][2];
+  h0_dots(g, D);
+  H1Pre p1;
+  if (NC > 1) h1_prepare(g, &p1);
   constexpr int R2 = NC == 1 ? 1 : 2;
-  for (int q = threadIdx.x; q < PR * PC; q += blockDim.x) {
-    const int ia = q / PC, ib = q - ia * PC;
-    int la[3], lb[3], sa[3], sb[3];
-    for (int j = 0; j < 3; j++) {
-      la[j] = s_hl[0][3 * ia + j]; sa[j] = s_hs[0][3 * ia + j];
-      lb[j] = s_hl[1][3 * ib + j]; sb[j] = s_hs[1][3 * ib + j];
+  for (int r = 0; r < R2; r++) {
+    const bool live = s_live[r];
+    if (r > 0 && !live) break;
+    cff MP[9];
+    H0Pre p0;
+    if (live) {
+      cff MG[9];
+      pair_moments_ff<6>(s_node[ia], s_node[ib], s_k[r].re, s_k[r].im, &s_rule, &s_tab, MG, MP);
+      h0_prepare(D, MG, &p0);
     }
-    if (tile_pair_far(s_cf[0][ia], s_cf[1][ib], s_pc[0][ia], s_pc[1][ib])) {
-      const float* Ga = s_geo + ia * GEO_STRIDE;
-      const float* Gb = s_geo + (PMAX + ib) * GEO_STRIDE;
-      FFGeom g;
-      for (int c = 0; c < 3; c++) {
-        g.Aa[c] = ffv(Ga[6 + c], Ga[9 + c]); g.Ba[c] = ffv(Ga[12 + c], Ga[15 + c]);
-        g.Ab[c] = ffv(Gb[6 + c], Gb[9 + c]); g.Bb[c] = ffv(Gb[12 + c], Gb[15 + c]);
-        g.D0[c] = ff_sub(ffv(Ga[c], Ga[3 + c]), ffv(Gb[c], Gb[3 + c]));
-      }
-      ff D[2][2];
-      h0_dots(g, D);
-      H1Pre p1;
-      if (NC > 1) h1_prepare(g, &p1);
-      for (int r = 0; r < R2; r++) {
-        const bool live = s_live[r];
-        cff MP[9];
-        H0Pre p0;
-        if (live) {
-          cff MG[9];
-          pair_moments_ff<6>(s_node + ia * NODE_STRIDE, s_node + (PMAX + ib) * NODE_STRIDE, s_k[r].re, s_k[r].im,
-                             &s_rule, s_tab, MG, MP);
-          h0_prepare(D, MG, &p0);
-        }
 #pragma unroll 1
-        for (int ja = 0; ja < 3; ja++) {
-          if (la[ja] < 0) continue;
-#pragma unroll 1
-          for (int jb = 0; jb < 3; jb++) {
-            if (lb[jb] < 0) continue;
-            cff v0 = cff_zero(), v2 = cff_zero();
-            cx<float> v1 = mk(0.0f, 0.0f);
-            if (live) {
-              const cff H0 = h0_combo(p0, ja, jb, s_m4[r]);
-              v0 = cff_mul(s_p1[r], H0);
-              if (NC > 2) v2 = cff_mul(s_p3[r], H0);
-              if (NC > 1) {
-                const cff H1 = h1_combo(p1, ja, jb, MP);
-                v1 = s_pcf[r] * mk(H1.re.hi + H1.re.lo, H1.im.hi + H1.im.lo);
-              }
-            }
-            const size_t slot = (size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb];
-            cx<float>* hi = slots + slot * NC;
-            cx<float>* lo = slots_lo + slot * NH;
-            if (r > 0) {
-              v0 = cff_add(v0, cff_at(hi[0], lo[0]));
-              if (NC > 1) v1 = v1 + hi[1];
-              if (NC > 2) v2 = cff_add(v2, cff_at(hi[2], lo[1]));
-            }
-            hi[0] = cff_hi(v0); lo[0] = cff_lo(v0);
-            if (NC > 1) hi[1] = v1;
-            if (NC > 2) { hi[2] = cff_hi(v2); lo[1] = cff_lo(v2); }
-          }
+    for (int c = 0; c < 9; c++) {
+      const int ja = c / 3, jb = c - 3 * ja;
+      cff v0 = cff_zero(), v2 = cff_zero();
+      cx<float> v1 = mk(0.0f, 0.0f);
+      if (live) {
+        const cff H0 = h0_combo(p0, ja, jb, s_m4[r]);
+        v0 = cff_mul(s_p1[r], H0);
+        if (NC > 2) v2 = cff_mul(s_p3[r], H0);
+        if (NC > 1) {
+          const cff H1 = h1_combo(p1, ja, jb, MP);
+          v1 = s_pcf[r] * mk(H1.re.hi + H1.re.lo, H1.im.hi + H1.im.lo);
         }
       }
-    } else {
-      // near pair: values precomputed in FP64 by self_kernel / near_kernel
-      const int hit = near_hit(a, s_gp[0][ia], s_gp[1][ib]);
-      if (hit < 0) continue;  // cannot happen: every rRel<=4 pair is listed
-      const double* nv = a.nearval + 54 * (size_t)(hit >> 1);
-      const bool tr = hit & 1;
-      for (int ja = 0; ja < 3; ja++) {
-        if (la[ja] < 0) continue;
-        for (int jb = 0; jb < 3; jb++) {
-          if (lb[jb] < 0) continue;
-          const double* v = nv + 6 * (tr ? (3 * jb + ja) : (3 * ja + jb));
-          const size_t slot = (size_t)(la[ja] * TE + lb[jb]) * 4 + sa[ja] * 2 + sb[jb];
-          cx<float>* hi = slots + slot * NC;
-          cx<float>* lo = slots_lo + slot * NH;
-          const cff v0 = cff_of(mk(v[0], v[1]));
-          hi[0] = cff_hi(v0); lo[0] = cff_lo(v0);
-          if (NC > 1) hi[1] = mk((float)v[2], (float)v[3]);
-          if (NC > 2) {
-            const cff v2 = cff_of(mk(v[4], v[5]));
-            hi[2] = cff_hi(v2); lo[1] = cff_lo(v2);
-          }
+      float* o = out + c * cs;
+      const size_t fs = 9 * cs;  // stride of one field
+      if (r > 0) {
+        // the second region adds to the first (same thread: no ordering issue)
+        v0 = cff_add(v0, cffv(ffv(o[0], o[fs]), ffv(o[2 * fs], o[3 * fs])));
+        if (NC > 1) v1 = v1 + mk(o[4 * fs], o[5 * fs]);
+        if (NC > 2) v2 = cff_add(v2, cffv(ffv(o[6 * fs], o[7 * fs]), ffv(o[8 * fs], o[9 * fs])));
+      }
+      o[0] = v0.re.hi; o[fs] = v0.re.lo; o[2 * fs] = v0.im.hi; o[3 * fs] = v0.im.lo;
+      if (NC > 1) { o[4 * fs] = v1.re; o[5 * fs] = v1.im; }
+      if (NC > 2) { o[6 * fs] = v2.re.hi; o[7 * fs] = v2.re.lo; o[8 * fs] = v2.im.hi; o[9 * fs] = v2.im.lo; }
+    }
+  }
+  (void)NF;
+}
+
+struct StampArgs {
+  TileArgs ta;            // output placement, near table, edge blocks
+  const int2* tiles;      // the stripe's tiles
+  const int4* edge_a;     // per row edge: P panel, its Q index, M panel, its Q index (surface-local; -1: none)
+  const int4* edge_b;     // per column edge, likewise
+  const int2* ecol;       // per column edge: stripe-local index of its P, M panel
+  int offb;               // global index of the first column-surface panel
+  const float* ppv;       // pass-1 values [NF][9][ncp][nrow]
+  int nrow, ncp;
+};
+
+// pass 2: one CTA per edge tile; the entries are formed once into shared
+// memory, then written column-major (block) and row-major (mirror) so both
+// stores are coalesced
+template <int NC>
+__global__ void __launch_bounds__(256) stamp_kernel(StampArgs sp) {
+  __shared__ cx<float> s_val[TE * TE * NC];
+  const TileArgs& a = sp.ta;
+  const int2 tile = sp.tiles[blockIdx.x];
+  const DevEdgeBlock* RB = a.rows + tile.x;
+  const DevEdgeBlock* CB = a.cols + tile.y;
+  const int NR = RB->ne, NCc = CB->ne;
+  const bool diag = a.sym && tile.x == tile.y;
+  const size_t cs = (size_t)sp.ncp * sp.nrow, fs = 9 * cs;
+  for (int q = threadIdx.x; q < NR * NCc; q += blockDim.x) {
+    const int i = q % NR, j = q / NR;
+    if (diag && i > j) continue;
+    const int ea = RB->e0 + i, eb = CB->e0 + j;
+    const int4 A = sp.edge_a[ea], B = sp.edge_b[eb];
+    const int2 C = sp.ecol[eb];
+    cff s0 = cff_zero(), s2 = cff_zero();
+    cx<float> s1 = mk(0.0f, 0.0f);
+    for (int u = 0; u < 2; u++) {
+      const int pa = u ? A.z : A.x, ja = u ? A.w : A.y;
+      if (pa < 0) continue;
+      for (int w = 0; w < 2; w++) {
+        const int pb = w ? B.z : B.x, jb = w ? B.w : B.y, cl = w ? C.y : C.x;
+        if (pb < 0) continue;
+        const float* src = sp.ppv + (size_t)(3 * ja + jb) * cs + (size_t)cl * sp.nrow + pa;
+        cff v0, v2 = cff_zero();
+        cx<float> v1 = mk(0.0f, 0.0f);
+        const float f0 = src[0];
+        if (!isnan(f0)) {
+          v0 = cffv(ffv(f0, src[fs]), ffv(src[2 * fs], src[3 * fs]));
+          if (NC > 1) v1 = mk(src[4 * fs], src[5 * fs]);
+          if (NC > 2) v2 = cffv(ffv(src[6 * fs], src[7 * fs]), ffv(src[8 * fs], src[9 * fs]));
+        } else {
+          // near pair: FP64 values of near_kernel / self_kernel
+          const int hit = near_hit(a, a.row_panel_offset + pa, sp.offb + pb);
+          if (hit < 0) continue;  // cannot happen: every rRel<=4 pair is listed
+          const double* v = a.nearval + 54 * (size_t)(hit >> 1) + 6 * ((hit & 1) ? (3 * jb + ja) : (3 * ja + jb));
+          v0 = cff_of(mk(v[0], v[1]));
+          if (NC > 1) v1 = mk((float)v[2], (float)v[3]);
+          if (NC > 2) v2 = cff_of(mk(v[4], v[5]));
+        }
+        if (u == w) {
+          s0 = cff_add(s0, v0); s1 = s1 + v1; s2 = cff_add(s2, v2);
+        } else {
+          s0 = cff_sub(s0, v0); s1 = s1 - v1; s2 = cff_sub(s2, v2);
         }
       }
+    }
+    // La Lb in FP64, then float-float: an FP32 product would scale every row
+    // and column of an edge by its own rounding, which the right-hand side
+    // and the power integrals do not share
+    const ff L = ff_of(a.elen_a[ea] * a.elen_b[eb]);
+    cx<float>* o = s_val + (size_t)(i * TE + j) * NC;
+    const cff y0 = cff_mul_ff(s0, L);
+    o[0] = mk(y0.re.hi + y0.re.lo, y0.im.hi + y0.im.lo);
+    if (NC > 1) o[1] = mk(fmaf(L.hi, s1.re, L.lo * s1.re), fmaf(L.hi, s1.im, L.lo * s1.im));
+    if (NC > 2) {
+      const cff y2 = cff_mul_ff(s2, L);
+      o[2] = mk(y2.re.hi + y2.re.lo, y2.im.hi + y2.im.lo);
     }
   }
   __syncthreads();
-
-  // entries: the four P/M contributions combined in float-float (H0
-  // channels), times La Lb, rounded to complex64
   cx<float>* out = reinterpret_cast<cx<float>*>(a.out);
-  const bool diag = a.sym && tile.x == tile.y;
   for (int pass = 0; pass < 2; pass++) {
     if (!(a.passes & (1 << pass))) continue;
     for (int q = threadIdx.x; q < NR * NCc; q += blockDim.x) {
       int i, j;
       if (!tile_entry(pass, q, NR, NCc, diag, &i, &j)) continue;
-      const cx<float>* hi = slots + (size_t)(i * TE + j) * 4 * NC;
-      const cx<float>* lo = slots_lo + (size_t)(i * TE + j) * 4 * NH;
-      // La Lb as float-float: an FP32 product would scale every row and
-      // column of an edge by its own rounding, which the right-hand side and
-      // the power integrals do not share
-      const ff L = ff_mul(ffv(s_el[0][0][i], s_el[0][1][i]), ffv(s_el[1][0][j], s_el[1][1][j]));
-      cx<float> v[3];
-      for (int c = 0; c < NC; c++) {
-        if (c == 1) {
-          const cx<float> x = (hi[1] - hi[NC + 1]) - (hi[2 * NC + 1] - hi[3 * NC + 1]);
-          v[1] = mk(fmaf(L.hi, x.re, L.lo * x.re), fmaf(L.hi, x.im, L.lo * x.im));
-        } else {
-          const int h = c == 0 ? 0 : 1;
-          const cff x = cff_sub(cff_sub(cff_at(hi[c], lo[h]), cff_at(hi[NC + c], lo[NH + h])),
-                                cff_sub(cff_at(hi[2 * NC + c], lo[2 * NH + h]), cff_at(hi[3 * NC + c], lo[3 * NH + h])));
-          const cff y = cff_mul_ff(x, L);
-          v[c] = mk(y.re.hi + y.re.lo, y.im.hi + y.im.lo);
-        }
-      }
+      const cx<float>* v = s_val + (size_t)(i * TE + j) * NC;
       store_entry(a, out, pass, RB->e0 + i, CB->e0 + j, v[0], NC > 1 ? v[1] : v[0], NC > 2 ? v[2] : v[0]);
     }
   }
@@ -851,13 +911,41 @@ static cudaError_t launch_tiles64(const TileArgs& ta, const RegionArgs& ra, int 
   return cudaGetLastError();
 }
 
+// the two passes of the mixed far field over a block's column stripes
 template <int NC>
-static cudaError_t launch_tiles_ff(const TileArgs& ta, const RegionArgs& ra, int ntiles, cudaStream_t s) {
-  const size_t smem = tile_ff_smem<NC>();
-  cudaError_t e = cudaFuncSetAttribute(tile_kernel_ff<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  tile_kernel_ff<NC><<<ntiles, 256, smem, s>>>(ta, ra);
-  return cudaGetLastError();
+static cudaError_t far_mixed(Geometry* g, const Block& b, DevBlock* db, const TileArgs& ta, const RegionArgs& ra,
+                             cudaStream_t s) {
+  const size_t need = b.max_stripe_pairs * 9 * ppair_fields<NC>() * sizeof(float);
+  cudaError_t e = cudaSuccess;
+  if (need > g->ppv_bytes) {
+    // grow the scratch (kept on the geometry; the old one may still be read
+    // by earlier launches, so wait for the device before freeing it)
+    if (g->ppv) {
+      e = cudaDeviceSynchronize();
+      cudaFree(g->ppv);
+    }
+    g->ppv = nullptr;
+    g->ppv_bytes = 0;
+    if (e == cudaSuccess) e = cudaMalloc(&g->ppv, need);
+    if (e != cudaSuccess) return e;
+    g->ppv_bytes = need;
+  }
+  for (const DevBlock::DevStripe& st : db->stripes) {
+    if (st.ntiles == 0 || st.ncp == 0) continue;
+    PPairArgs pp;
+    pp.node = g->d_ffnode; pp.geo = g->d_ffgeo; pp.pc = g->d_pc; pp.cpan = st.cpan;
+    pp.offa = g->S[b.sa].panel_offset; pp.offb = g->S[b.sb].panel_offset;
+    pp.nrow = st.nrow; pp.ncp = st.ncp; pp.out = (float*)g->ppv;
+    ppair_kernel<NC><<<dim3((st.nrow + 31) / 32, (st.ncp + 7) / 8), dim3(32, 8), 0, s>>>(pp, ra);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    StampArgs sp;
+    sp.ta = ta; sp.tiles = st.tiles; sp.edge_a = db->edge_a; sp.edge_b = db->edge_b; sp.ecol = db->ecol;
+    sp.offb = pp.offb; sp.ppv = pp.out; sp.nrow = st.nrow; sp.ncp = st.ncp;
+    stamp_kernel<NC><<<st.ntiles, 256, 0, s>>>(sp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    stats_launch(ST_FAR, 2);
+  }
+  return cudaSuccess;
 }
 
 gbem_status compute_fippi(Geometry* g, cudaStream_t s) {
@@ -1007,10 +1095,9 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
     ta.out = dM; ta.ld = ld;
     int nc = (b.bpe_a == 2 && b.bpe_b == 2) ? 3 : ((b.bpe_a == 1 && b.bpe_b == 1) ? 1 : 2);
     StatTimer tf(ST_FAR, s);
-    stats_launch(ST_FAR);
+    if (precision != GBEM_PREC_MIXED) stats_launch(ST_FAR);
     if (precision == GBEM_PREC_MIXED) {
-      e = nc == 1 ? launch_tiles_ff<1>(ta, ra, db->ntiles, s)
-                  : nc == 2 ? launch_tiles_ff<2>(ta, ra, db->ntiles, s) : launch_tiles_ff<3>(ta, ra, db->ntiles, s);
+      e = nc == 1 ? far_mixed<1>(g, b, db, ta, ra, s) : nc == 2 ? far_mixed<2>(g, b, db, ta, ra, s) : far_mixed<3>(g, b, db, ta, ra, s);
     } else {
       e = nc == 1 ? launch_tiles64<1>(ta, ra, db->ntiles, s)
                   : nc == 2 ? launch_tiles64<2>(ta, ra, db->ntiles, s) : launch_tiles64<3>(ta, ra, db->ntiles, s);

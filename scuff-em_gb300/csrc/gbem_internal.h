@@ -44,6 +44,16 @@ struct NearPair {
   double rmax;     // larger panel radius
 };
 
+// A column stripe of a block for the mixed-precision far field, which runs
+// in two passes: every far panel pair of the stripe once (pair values into a
+// scratch buffer), then the stripe's edge tiles from those values.
+struct Stripe {
+  int cb0 = 0, cb1 = 0;     // column edge blocks [cb0, cb1)
+  int nrow = 0;             // row panels [0, nrow) (surface-local) the stripe's entries touch
+  std::vector<int> cpan;    // column panels (surface-local, ascending) of the stripe's edges
+  std::vector<int2> tiles;  // the stripe's tiles (row block, column block)
+};
+
 struct Block {
   int sa = 0, sb = 0;
   bool sym = false;
@@ -56,6 +66,9 @@ struct Block {
   std::vector<NearPair> near;          // near pairs of this surface pair
   std::vector<int> near_ptr, near_col, near_idx;  // CSR over local row panel: (pb, pair index, transpose flag in sign)
   double rmax_touch = 0.0;             // largest panel radius over the pairs with ncv = 1, 2
+  std::vector<Stripe> stripes;         // column stripes (mixed far field)
+  std::vector<int2> ecol;              // per column edge: stripe-local index of its P, M panel (-1: none)
+  size_t max_stripe_pairs = 0;         // largest nrow * cpan.size() over the stripes
 };
 
 struct DevBlock;  // defined in assemble.cu
@@ -80,6 +93,10 @@ struct Geometry {
   // geometry while matrices exist defers the release to the last of them
   int refs = 0;
   bool dead = false;
+  float* d_ffnode = nullptr;  // per global panel: 6 rule nodes, float-float offsets from ff_origin (36 floats)
+  float* d_ffgeo = nullptr;   // per global panel: V0 - ff_origin, V1 - V0, V2 - V0 as float-float (18 floats)
+  void* ppv = nullptr;        // pair-value scratch of the mixed far field
+  size_t ppv_bytes = 0;
   // cached buffers of the mixed-precision solve
   void* mixedM = nullptr;
   void* mixedF = nullptr;

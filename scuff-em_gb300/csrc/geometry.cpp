@@ -115,6 +115,66 @@ static std::vector<EdgeBlock> edge_blocks(const Surface& s) {
   return out;
 }
 
+// Column stripes of a block (mixed far field): consecutive column edge blocks
+// while the stripe's column panels times the row panels stay within a
+// pair-value budget of STRIPE_PAIRS panel pairs (~0.5 GB of scratch at the
+// largest field count); the row panels a stripe needs are those of the row
+// edges up to its last column edge (a symmetric block keeps i <= j), or all.
+constexpr size_t STRIPE_PAIRS = (size_t)3 << 20;
+
+static void build_stripes(const Surface& sa, const Surface& sb, Block& blk) {
+  blk.ecol.assign(sb.ne, make_int2(-1, -1));
+  const int ncb = (int)blk.cols.size();
+  // running maximum of the row panel index over the row edges
+  std::vector<int> rowmax(sa.ne);
+  int m = -1;
+  for (int e = 0; e < sa.ne; e++) {
+    m = std::max(m, std::max(sa.E[8 * e + 4], sa.E[8 * e + 5]));
+    rowmax[e] = m;
+  }
+  int cb = 0;
+  while (cb < ncb) {
+    Stripe st;
+    st.cb0 = cb;
+    std::vector<char> in(sb.np, 0);
+    size_t ncp = 0;
+    while (cb < ncb) {
+      const EdgeBlock& c = blk.cols[cb];
+      size_t add = 0;
+      std::vector<int> newp;
+      for (int e = c.e0; e < c.e0 + c.ne; e++)
+        for (int s = 0; s < 2; s++) {
+          const int p = sb.E[8 * e + 4 + s];
+          if (p >= 0 && !in[p]) { in[p] = 1; newp.push_back(p); add++; }
+        }
+      const int last = c.e0 + c.ne - 1;
+      const size_t nrow = blk.sym ? (size_t)rowmax[std::min(last, sa.ne - 1)] + 1 : (size_t)sa.np;
+      if (cb > st.cb0 && (ncp + add) * nrow > STRIPE_PAIRS) {
+        for (int p : newp) in[p] = 0;
+        break;
+      }
+      ncp += add;
+      st.nrow = (int)nrow;
+      cb++;
+    }
+    st.cb1 = cb;
+    for (int p = 0; p < sb.np; p++)
+      if (in[p]) st.cpan.push_back(p);
+    std::vector<int> loc(sb.np, -1);
+    for (size_t i = 0; i < st.cpan.size(); i++) loc[st.cpan[i]] = (int)i;
+    for (int j = st.cb0; j < st.cb1; j++) {
+      const EdgeBlock& c = blk.cols[j];
+      for (int e = c.e0; e < c.e0 + c.ne; e++) {
+        const int pp = sb.E[8 * e + 4], pm = sb.E[8 * e + 5];
+        blk.ecol[e] = make_int2(pp >= 0 ? loc[pp] : -1, pm >= 0 ? loc[pm] : -1);
+      }
+      for (int i = 0; i < (int)blk.rows.size() && (!blk.sym || i <= j); i++) st.tiles.push_back(make_int2(i, j));
+    }
+    blk.max_stripe_pairs = std::max(blk.max_stripe_pairs, (size_t)st.nrow * st.cpan.size());
+    blk.stripes.push_back(std::move(st));
+  }
+}
+
 // Common-vertex count and common-vertices-first ordering
 // (AssessPanelPair.cc:52-103; vertices within 1e-6 r_max count as common,
 // VecClose of libs/libhrutil/Vector.cc:294-297).
@@ -261,6 +321,7 @@ gbem_status build_geometry(int ns, const gbem_surface_desc* d, int nreg, Geometr
       blk.cols = blk.sym ? blk.rows : edge_blocks(g->S[b]);
       for (int i = 0; i < (int)blk.rows.size(); i++)
         for (int j = blk.sym ? i : 0; j < (int)blk.cols.size(); j++) blk.tiles.push_back(make_int2(i, j));
+      build_stripes(g->S[a], g->S[b], blk);
       if (blk.nreg > 0) near_pairs(g->S[a], g->S[b], blk.sym, blk, g->near_counts);
       g->blocks.push_back(std::move(blk));
     }
