@@ -19,6 +19,10 @@ Fixtures:
   ref_fippi_s2.npz reference Q-independent FIPPI data for near pairs.
   ref_<case>.npz   reference BEM matrices (full or a column sample), plane-wave
                    right-hand sides, solutions and EMT powers for small geometries.
+  mie_pft_tables.json  the reference's tables of sphere powers (R = 1 um, PEC,
+                   SiO2, gold at omega = 0.01, 0.1, 1; unitTests/unit-test-PFT.cc:
+                   77-130), read from the test source as text: they pin the Mie
+                   oracle (oracle/mie.py).
 """
 import argparse
 import os
@@ -206,11 +210,30 @@ def gradient_fixtures(tmp):
                                      ("b", V1, P1, "CONST_EPS_2.25+0.01i", (0.0, 0.0, 3.0))], 1.5, [(0, 1)])
 
 
+def mie_tables(ref):
+    """Parse the PFTData tables of unitTests/unit-test-PFT.cc (omega, Re eps,
+    Im eps, absorbed power, scattered power, z-force, z-torque per row)."""
+    import json
+    src = open(os.path.join(ref, "unitTests", "unit-test-PFT.cc")).read()
+    out = {}
+    for name in ("PECPFTData", "SIO2PFTData", "GoldPFTData"):
+        body = re.search(name + r"\s*=\s*\{(.*?)\};", src, re.S).group(1)
+        nums = [float(x) for x in re.findall(r"[-+]?\d+\.?\d*(?:[eE][-+]?\d+)?", body)]
+        out[name] = [nums[i:i + 7] for i in range(0, len(nums), 7)]
+    with open(os.path.join(HERE, "mie_pft_tables.json"), "w") as f:
+        json.dump({"source": "unitTests/unit-test-PFT.cc:77-130", "columns":
+                   ["omega", "eps_re", "eps_im", "p_abs_W", "p_scat_W", "f_z_nN", "tau_z_nN_um"], "tables": out}, f,
+                  indent=1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["gradients"], help="regenerate one group of fixtures only")
+    ap.add_argument("--only", choices=["gradients", "mie"], help="regenerate one group of fixtures only")
     a = ap.parse_args()
+    if a.only == "mie":
+        mie_tables(a.ref)
+        return
     if not os.path.exists(REFDUMP):
         sys.exit("build the reference first: make -C oracle/ref REF=%s" % a.ref)
     if a.only == "gradients":
@@ -234,6 +257,7 @@ def main():
         # dielectric sphere at a frequency where high-order / Taylor-Duffy branches appear
         matrix_case(tmp, "diel_s1_w12", [("sph", V1, P1, "CONST_EPS_4+0.1i", None)], 12.0)
         gradient_fixtures(tmp)
+    mie_tables(a.ref)
 
 
 if __name__ == "__main__":

@@ -87,8 +87,15 @@ def test_complex64_lu_tensor_core_update():
     A = M.numpy().astype(np.complex128)
     assert M.LUFactorize() == 0
     lu_ref, piv_ref = sl.lu_factor(A)
-    # pivots agree with LAPACK except where FP32 rounding reorders near-ties
-    assert np.mean((M.ipiv - 1) == piv_ref) > 0.98
+    # backward error of P A = L U (FP32 rounding may reorder near-tied
+    # pivots, so the pivots themselves are not compared with LAPACK's)
+    N = A.shape[0]
+    LU = M.numpy().astype(np.complex128)
+    perm = np.arange(N)
+    for i, p in enumerate(M.ipiv - 1):
+        perm[[i, p]] = perm[[p, i]]
+    be = np.linalg.norm(A[perm] - (np.tril(LU, -1) + np.eye(N)) @ np.triu(LU)) / np.linalg.norm(A)
+    assert be < 2e-4
     rng = np.random.default_rng(3)
     b = rng.standard_normal(A.shape[0]) + 1j * rng.standard_normal(A.shape[0])
     x = M.LUSolve(b.astype(np.complex64)).astype(np.complex128)
@@ -128,3 +135,4 @@ def test_complex64_lu_random_matrix(subdiv, pec, tol):
     x = M.LUSolve(b.astype(np.complex64)).astype(np.complex128)
     xr = sl.solve(A, b)
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 500 * tol
+

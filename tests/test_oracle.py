@@ -132,3 +132,23 @@ def test_emt_scattered_power_against_reference(golden, case):
         ps = ora.emt_pscat(surfs[0], pec[0], w, d["kn%d" % j])
         assert abs(ps - d["pft%d" % j][1]) < 2e-6 * abs(d["pft%d" % j][1]), (j, ps, d["pft%d" % j])
         j += 1
+
+
+def test_mie_oracle_against_reference_tables():
+    """The Mie oracle (oracle/mie.py) reproduces the reference's sphere power
+    tables (unitTests/unit-test-PFT.cc:77-130: R = 1 um, PEC, SiO2 and gold
+    at omega = 0.01, 0.1, 1) to their 7 printed digits."""
+    import json
+    import os
+    from oracle import mie
+    with open(os.path.join(os.path.dirname(__file__), "golden", "mie_pft_tables.json")) as f:
+        tables = json.load(f)["tables"]
+    for name, rows in tables.items():
+        for w, er, ei, pabs, pscat, _, _ in rows:
+            pec = name.startswith("PEC")
+            a, s = mie.powers(w, eps=None if pec else complex(er, ei), pec=pec)
+            assert abs(s - pscat) < 1e-6 * pscat, (name, w, s, pscat)
+            if pec:
+                assert abs(a) < 1e-20
+            else:
+                assert abs(a - pabs) < 1e-6 * pabs, (name, w, a, pabs)
