@@ -121,7 +121,8 @@ gbem_status gbem_assemble_host(gbem_geometry *g, double omega_re, double omega_i
  * dimension ld) at (row0, col0).  dtype C128 or F64 with GBEM_PREC_FP64 (F64:
  * real storage, the reference's LHM_REAL at imaginary frequency, where the
  * block is real), C64 with GBEM_PREC_MIXED.  Gradient blocks (GradM) come
- * from gbem_assemble_block_gradient; torque blocks (dMdT) are not provided. */
+ * from gbem_assemble_block_gradient, torque blocks (dMdT) from
+ * gbem_assemble_block_dmdt. */
 gbem_status gbem_assemble_block(gbem_geometry *g, int nsa, int nsb, double omega_re, double omega_im,
                                 const double *eps, const double *mu, int precision, void *dst, int ld,
                                 int row0, int col0, int dtype);
@@ -136,6 +137,21 @@ gbem_status gbem_assemble_block_gradient(gbem_geometry *g, int nsa, int nsb, dou
                                          double omega_im, const double *eps, const double *mu,
                                          void *gx, void *gy, void *gz, int ld, int row0, int col0,
                                          int dtype);
+/* The torque blocks dMdT[a] = dM/dtheta_a of the (nsa, nsb) block under a
+ * rotation of surface nsa generated by gamma + 9a (dX = Gamma X, with
+ * gamma[9a + mu + 3 nu] = Gamma_{mu nu}; the GammaMatrix of
+ * AssembleBEMMatrixBlock(..., NumTorqueAxes, dMdT, GammaMatrix),
+ * AssembleBEMMatrix.cc:341-400, integrand PanelPanelInteractions.cc:183-199):
+ * naxes (1..3) device arrays out[a], same layout, rules and branches as
+ * gbem_assemble_block_gradient; dtype C128 or F64. */
+gbem_status gbem_assemble_block_dmdt(gbem_geometry *g, int nsa, int nsb, double omega_re, double omega_im,
+                                     const double *eps, const double *mu, int naxes, const double *gamma,
+                                     void *const *out, int ld, int row0, int col0, int dtype);
+/* Host-buffer variant of gbem_assemble_block_dmdt. */
+gbem_status gbem_assemble_block_dmdt_host(gbem_geometry *g, int nsa, int nsb, double omega_re,
+                                          double omega_im, const double *eps, const double *mu, int naxes,
+                                          const double *gamma, void *const *out, int ld, int row0, int col0,
+                                          int dtype);
 /* Host-buffer variant of gbem_assemble_block_gradient. */
 gbem_status gbem_assemble_block_gradient_host(gbem_geometry *g, int nsa, int nsb, double omega_re,
                                               double omega_im, const double *eps, const double *mu,
@@ -160,6 +176,16 @@ gbem_status gbem_lu_factor(gbem_matrix *M, int *ipiv, int *info);
  * column-major array B (N x nrhs, ldb) of the factor's type (C128, C64, or
  * real F64); trans is 'N' or 'T'. */
 gbem_status gbem_lu_solve(gbem_matrix *M, char trans, int nrhs, void *B, int ldb);
+
+/* Trace of M^-1 B over the first ncols diagonal entries, for a factored M
+ * (gbem_lu_factor) and B of M's size and element type (F64, C128 or C64)
+ * whose first ncols columns hold the derivative blocks of the BEM matrix:
+ * trace[0] = Re, trace[1] = Im.  Replaces the M->LUSolve(dM) + diagonal sum
+ * of GetTraceMInvdM (applications/scuff-cas3D/CasimirIntegrand.cc:100-146),
+ * whose force is -2 Re(trace) / (2 pi).  B on the device (a gbem_matrix) or
+ * on the host (leading dimension ldb >= N). */
+gbem_status gbem_lu_trace(gbem_matrix *M, const gbem_matrix *B, int ncols, double *trace);
+gbem_status gbem_lu_trace_host(gbem_matrix *M, const void *B, int ldb, int ncols, double *trace);
 
 /* gbem_lu_solve without any device allocation.  No counterpart in the
  * reference (HMatrix::LUSolve runs LAPACK on host memory).  Same arguments

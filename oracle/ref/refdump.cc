@@ -13,6 +13,9 @@
 //   refdump time   GEO wr wi NREP            wall time of AssembleBEMMatrix, LUFactorize, LUSolve
 //   refdump gradblock GEO wr wi nsa nsb OUT  block (nsa,nsb) and its three gradients d/dx_mu
 //                                            (per matrix: int32 NR NC, then NR*NC complex128 column-major)
+//   refdump torqueblock GEO wr wi nsa nsb OUT  block (nsa,nsb) and its derivatives dM/dtheta for
+//                                            rotations about the x, y and z axes through the origin
+//                                            (GammaMatrix = the cross-product matrix of each axis)
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -215,6 +218,33 @@ int main(int argc, char **argv) {
     FILE *f = fopen(argv[7], "wb");
     append_rect(f, M);
     for (int mu = 0; mu < 3; mu++) append_rect(f, GradM[mu]);
+    fclose(f);
+    return 0;
+  }
+
+  if (!strcmp(cmd, "torqueblock")) {
+    cdouble Omega(atof(argv[3]), atof(argv[4]));
+    int nsa = atoi(argv[5]), nsb = atoi(argv[6]);
+    int NR = G->Surfaces[nsa]->NumBFs, NC = G->Surfaces[nsb]->NumBFs;
+    HMatrix *M = new HMatrix(NR, NC, LHM_COMPLEX);
+    HMatrix *dMdT[3];
+    for (int a = 0; a < 3; a++) dMdT[a] = new HMatrix(NR, NC, LHM_COMPLEX);
+    M->Zero();
+    for (int a = 0; a < 3; a++) dMdT[a]->Zero();
+    // dX = n x X for axis n: Gamma[9 a + Mu + 3 Nu] = (n x e_Nu)_Mu
+    double Gamma[27];
+    memset(Gamma, 0, sizeof Gamma);
+    for (int a = 0; a < 3; a++)
+      for (int nu = 0; nu < 3; nu++) {
+        double n[3] = {0, 0, 0}, e[3] = {0, 0, 0}, c[3];
+        n[a] = 1.0; e[nu] = 1.0;
+        c[0] = n[1] * e[2] - n[2] * e[1]; c[1] = n[2] * e[0] - n[0] * e[2]; c[2] = n[0] * e[1] - n[1] * e[0];
+        for (int mu = 0; mu < 3; mu++) Gamma[9 * a + mu + 3 * nu] = c[mu];
+      }
+    G->AssembleBEMMatrixBlock(nsa, nsb, Omega, 0, M, 0, 0, 0, 0, false, 3, dMdT, Gamma);
+    FILE *f = fopen(argv[7], "wb");
+    append_rect(f, M);
+    for (int a = 0; a < 3; a++) append_rect(f, dMdT[a]);
     fclose(f);
     return 0;
   }

@@ -1144,11 +1144,19 @@ struct GradArgs {
   int bpe_a, bpe_b;
   int row0, col0;
   long long ld;
-  void* out[3];
+  void* out[3];      // dM/dx_mu (null: not wanted)
+  int nta;           // rotation axes (0..3)
+  double gamma[27];  // per axis: dX = Gamma X, Gamma[9 a + mu + 3 nu] (GammaMatrix of AssembleBEMMatrixBlock)
+  void* outT[3];     // dM/dtheta_a
 };
 
+// TH (2 per axis, may be null): the angular derivatives of the reference
+// (PanelPanelInteractions.cc:183-199): with dX = Gamma x, dF = Gamma F,
+//   dHdT[2a]   = int int hPlus (R.dX) Psi + (dF.F') Phi,
+//   dHdT[2a+1] = int int hTimes (R.dX) Zeta + ((dF x F').R + (F x F').dX) Psi.
 __device__ void ppi_grad(const double* Pa, const double* Qa, const double* Pb, const double* Qb, cx<double> k,
-                         const double* rule, int npts, cx<double>* GH) {
+                         const double* rule, int npts, cx<double>* GH, int nta = 0, const double* gamma = nullptr,
+                         cx<double>* TH = nullptr) {
   const double inv4pi = 0.079577471545947667884;
   const cx<double> ik = mk(-k.im, k.re), ik2 = ik * ik, m4 = cdiv(mk(4.0, 0.0), ik2);
   double A[3], B[3], Ap[3], Bp[3];
@@ -1157,6 +1165,7 @@ __device__ void ppi_grad(const double* Pa, const double* Qa, const double* Pb, c
     Ap[c] = Pb[3 + c] - Pb[c]; Bp[c] = Pb[6 + c] - Pb[c];
   }
   for (int m = 0; m < 6; m++) GH[m] = mk(0.0, 0.0);
+  for (int m = 0; m < 2 * nta; m++) TH[m] = mk(0.0, 0.0);
   for (int i = 0; i < npts; i++) {
     const double u = rule[3 * i], v = rule[3 * i + 1], wi = rule[3 * i + 2];
     double x[3], F[3];
@@ -1186,6 +1195,20 @@ __device__ void ppi_grad(const double* Pa, const double* Qa, const double* Pb, c
         GH[2 * mu] = GH[2 * mu] + R[mu] * hPsi;
         GH[2 * mu + 1] = GH[2 * mu + 1] + R[mu] * hZ + X[mu] * Psi;
       }
+      for (int a = 0; a < nta; a++) {
+        const double* Gm = gamma + 9 * a;
+        double dX[3], dF[3], dFxFp[3];
+        for (int mu = 0; mu < 3; mu++) {
+          dX[mu] = Gm[mu] * x[0] + Gm[mu + 3] * x[1] + Gm[mu + 6] * x[2];
+          dF[mu] = Gm[mu] * F[0] + Gm[mu + 3] * F[1] + Gm[mu + 6] * F[2];
+        }
+        vcross(dF, Fp, dFxFp);
+        const double Puv = R[0] * dX[0] + R[1] * dX[1] + R[2] * dX[2];
+        const double dFFp = dF[0] * Fp[0] + dF[1] * Fp[1] + dF[2] * Fp[2];
+        const double cr = dFxFp[0] * R[0] + dFxFp[1] * R[1] + dFxFp[2] * R[2] + X[0] * dX[0] + X[1] * dX[1] + X[2] * dX[2];
+        TH[2 * a] = TH[2 * a] + Puv * hPsi + dFFp * Phi;
+        TH[2 * a + 1] = TH[2 * a + 1] + Puv * hZ + cr * Psi;
+      }
     }
   }
 }
@@ -1198,14 +1221,14 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs a, RegionArgs ra) {
   const int* EA = a.Ea + 8 * ea;
   const int* EB = a.Eb + 8 * eb;
   const double La = a.La[ea], Lb = a.Lb[eb];
-  cx<double> acc[3][4];
+  cx<double> acc[3][4], accT[3][4];
   for (int mu = 0; mu < 3; mu++)
-    for (int c = 0; c < 4; c++) acc[mu][c] = mk(0.0, 0.0);
+    for (int c = 0; c < 4; c++) acc[mu][c] = accT[mu][c] = mk(0.0, 0.0);
   for (int r = 0; r < ra.nreg; r++) {
     const cx<double> k = ra.k[r];
     if (k.re == 0.0 && k.im == 0.0) continue;
-    cx<double> S0[3], S1[3];
-    for (int mu = 0; mu < 3; mu++) { S0[mu] = mk(0.0, 0.0); S1[mu] = mk(0.0, 0.0); }
+    cx<double> S0[3], S1[3], T0[3], T1[3];
+    for (int mu = 0; mu < 3; mu++) S0[mu] = S1[mu] = T0[mu] = T1[mu] = mk(0.0, 0.0);
     for (int sa = 0; sa < 2; sa++) {
       const int iqa = sa == 0 ? EA[2] : EA[3];
       const int pa = sa == 0 ? EA[4] : EA[5];
@@ -1222,9 +1245,9 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs a, RegionArgs ra) {
         const double rmax = fmax(ca[3], cb[3]);
         const double dx = ca[0] - cb[0], dy = ca[1] - cb[1], dz = ca[2] - cb[2];
         const bool far = sqrt(dx * dx + dy * dy + dz * dz) > 4.0 * rmax;
-        cx<double> GH[6];
+        cx<double> GH[6], TH[6];
         if (far) {
-          ppi_grad(Pa, a.Va + 3 * iqa, Pb, a.Vb + 3 * iqb, k, c_lo64, 6, GH);
+          ppi_grad(Pa, a.Va + 3 * iqa, Pb, a.Vb + 3 * iqb, k, c_lo64, 6, GH, a.nta, a.gamma, TH);
         } else {
           int ncv = 0;
           for (int i = 0; i < 3; i++)
@@ -1234,12 +1257,16 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs a, RegionArgs ra) {
             }
           const bool swr = hypot(k.re * rmax, k.im * rmax) > M_PI;
           if (ncv == 3 || (ncv > 0 && swr)) continue;  // Taylor-Duffy pairs: zero gradient
-          ppi_grad(Pa, a.Va + 3 * iqa, Pb, a.Vb + 3 * iqb, k, c_ho, HO_N * HO_N, GH);
+          ppi_grad(Pa, a.Va + 3 * iqa, Pb, a.Vb + 3 * iqb, k, c_ho, HO_N * HO_N, GH, a.nta, a.gamma, TH);
         }
         const double sg = (sa == sb) ? 1.0 : -1.0;
         for (int mu = 0; mu < 3; mu++) {
           S0[mu] = S0[mu] + sg * GH[2 * mu];
           S1[mu] = S1[mu] + sg * GH[2 * mu + 1];
+        }
+        for (int t = 0; t < a.nta; t++) {
+          T0[t] = T0[t] + sg * TH[2 * t];
+          T1[t] = T1[t] + sg * TH[2 * t + 1];
         }
       }
     }
@@ -1250,23 +1277,33 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs a, RegionArgs ra) {
       acc[mu][1] = acc[mu][1] + ra.pfc[r] * g1;
       acc[mu][3] = acc[mu][3] + ra.pf3[r] * g0;
     }
+    for (int t = 0; t < a.nta; t++) {  // stamped like the gradient (SurfaceSurfaceInteractions.cc:216-325)
+      const cx<double> g0 = LL * T0[t], g1 = LL * T1[t];
+      accT[t][0] = accT[t][0] + ra.pf1[r] * g0;
+      accT[t][1] = accT[t][1] + ra.pfc[r] * g1;
+      accT[t][3] = accT[t][3] + ra.pf3[r] * g0;
+    }
   }
   const long long X = a.row0 + (long long)a.bpe_a * ea, Y = a.col0 + (long long)a.bpe_b * eb;
-  for (int mu = 0; mu < 3; mu++) {
-    if (!a.out[mu]) continue;
+  for (int m = 0; m < 6; m++) {
+    const int mu = m % 3;
+    void* dst = m < 3 ? a.out[mu] : (mu < a.nta ? a.outT[mu] : nullptr);
+    if (!dst) continue;
+    const cx<double>* v = m < 3 ? acc[mu] : accT[mu];
     // (K,K) = PF1 G0; (K,N) = (N,K) = PF2 G1 / (ik); (N,N) = PF3 G0
-    cx<double> e[2][2] = {{acc[mu][0], acc[mu][1]}, {acc[mu][1], acc[mu][3]}};
+    cx<double> e[2][2] = {{v[0], v[1]}, {v[1], v[3]}};
     for (int dx = 0; dx < a.bpe_a; dx++)
       for (int dy = 0; dy < a.bpe_b; dy++) {
         const long long idx = (X + dx) + (Y + dy) * a.ld;
-        if (REAL) ((double*)a.out[mu])[idx] = e[dx][dy].re;
-        else ((cx<double>*)a.out[mu])[idx] = e[dx][dy];
+        if (REAL) ((double*)dst)[idx] = e[dx][dy].re;
+        else ((cx<double>*)dst)[idx] = e[dx][dy];
       }
   }
 }
 
 gbem_status assemble_gradient_device(Geometry* g, double wr, double wi, const double* eps, const double* mu,
-                                     const BlockSel& sel, void* const out[3], int ld, int dtype, cudaStream_t s) {
+                                     const BlockSel& sel, void* const out[3], int ld, int dtype, cudaStream_t s,
+                                     int nta, const double* gamma, void* const* outT) {
   gbem_status st = upload_geometry(g);
   if (st != GBEM_OK) return st;
   const int lo = std::min(sel.nsa, sel.nsb), hi = std::max(sel.nsa, sel.nsb);
@@ -1280,10 +1317,12 @@ gbem_status assemble_gradient_device(Geometry* g, double wr, double wi, const do
   cudaError_t e = cudaSuccess;
   // the block's entries are written by one thread each; a block of surfaces
   // that share no region is zero
-  for (int m = 0; m < 3 && e == cudaSuccess; m++)
-    if (out[m])
-      e = cudaMemset2DAsync((char*)out[m] + ((size_t)sel.row0 + (size_t)sel.col0 * ld) * es, (size_t)ld * es, 0,
+  for (int m = 0; m < 6 && e == cudaSuccess; m++) {
+    void* dst = m < 3 ? out[m] : (m - 3 < nta ? outT[m - 3] : nullptr);
+    if (dst)
+      e = cudaMemset2DAsync((char*)dst + ((size_t)sel.row0 + (size_t)sel.col0 * ld) * es, (size_t)ld * es, 0,
                             (size_t)A.ne * (A.pec ? 1 : 2) * es, B.ne * (B.pec ? 1 : 2), s);
+  }
   if (e != cudaSuccess) return cuda_status(e, "gradient memset");
   if (bp->nreg == 0 || A.ne == 0 || B.ne == 0) return GBEM_OK;
   double *dVa = nullptr, *dVb = nullptr, *dLa = nullptr, *dLb = nullptr;
@@ -1302,6 +1341,9 @@ gbem_status assemble_gradient_device(Geometry* g, double wr, double wi, const do
     ga.bpe_a = A.pec ? 1 : 2; ga.bpe_b = B.pec ? 1 : 2;
     ga.row0 = sel.row0; ga.col0 = sel.col0; ga.ld = ld;
     for (int m = 0; m < 3; m++) ga.out[m] = out[m];
+    ga.nta = nta;
+    for (int m = 0; m < 27; m++) ga.gamma[m] = m < 9 * nta ? gamma[m] : 0.0;
+    for (int m = 0; m < 3; m++) ga.outT[m] = m < nta ? outT[m] : nullptr;
     const RegionArgs ra = region_args(*bp, wr, wi, eps, mu);
     const long long n = (long long)A.ne * B.ne;
     stats_launch(ST_OTHER);

@@ -138,6 +138,28 @@ static __global__ void emt_quadform(const cx<TM>* M, long long ld, int N, const 
     for (int r = 0; r < nrhs; r++) part[((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 8 + r] = red[r][0];
 }
 
+namespace gbem {
+template <typename T>
+static __global__ void trace_diag(const cx<T>* X, long long ldx, int n, double* out) {
+  __shared__ double sr[1024], si[1024];
+  double ar = 0.0, ai = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const cx<T> v = X[i + (long long)i * ldx];
+    ar += (double)v.re;
+    ai += (double)v.im;
+  }
+  sr[threadIdx.x] = ar;
+  si[threadIdx.x] = ai;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) { sr[threadIdx.x] += sr[threadIdx.x + o]; si[threadIdx.x] += si[threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { out[0] = sr[0]; out[1] = si[0]; }
+}
+
+}  // namespace gbem
+
 extern "C" {
 
 const char* gbem_last_error(void) { return g_err; }
@@ -469,6 +491,55 @@ gbem_status gbem_assemble_block_gradient_host(gbem_geometry* g, int nsa, int nsb
   return st;
 }
 
+gbem_status gbem_assemble_block_dmdt(gbem_geometry* g, int nsa, int nsb, double omega_re, double omega_im,
+                                     const double* eps, const double* mu, int naxes, const double* gamma,
+                                     void* const* out, int ld, int row0, int col0, int dtype) {
+  if (!g || !eps || !mu || !gamma || !out || naxes < 1 || naxes > 3 || nsa < 0 || nsb < 0 ||
+      nsa >= (int)g->S.size() || nsb >= (int)g->S.size() || row0 < 0 || col0 < 0 || ld < row0 + surface_bfs(g, nsa) ||
+      (dtype != GBEM_C128 && dtype != GBEM_F64)) {
+    set_error("gbem_assemble_block_dmdt: bad arguments (1 <= naxes <= 3, dtype C128 or F64)");
+    return GBEM_EINVAL;
+  }
+  if (omega_is_zero(omega_re, omega_im)) { set_error("gbem_assemble_block_dmdt: Omega = 0"); return GBEM_EINVAL; }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  void* const none[3] = {nullptr, nullptr, nullptr};
+  BlockSel sel{nsa, nsb, row0, col0};
+  return assemble_gradient_device(g, omega_re, omega_im, eps, mu, sel, none, ld, dtype, g->stream, naxes, gamma, out);
+}
+
+gbem_status gbem_assemble_block_dmdt_host(gbem_geometry* g, int nsa, int nsb, double omega_re, double omega_im,
+                                          const double* eps, const double* mu, int naxes, const double* gamma,
+                                          void* const* out, int ld, int row0, int col0, int dtype) {
+  if (!g || !out || naxes < 1 || naxes > 3 || nsa < 0 || nsb < 0 || nsa >= (int)g->S.size() ||
+      nsb >= (int)g->S.size() || (dtype != GBEM_C128 && dtype != GBEM_F64) || row0 < 0 || col0 < 0 ||
+      ld < row0 + surface_bfs(g, nsa)) {
+    set_error("gbem_assemble_block_dmdt_host: bad arguments (1 <= naxes <= 3, dtype C128 or F64)");
+    return GBEM_EINVAL;
+  }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  const int m = surface_bfs(g, nsa), n = surface_bfs(g, nsb);
+  const size_t es = dtype == GBEM_C128 ? 16 : 8;
+  void* d[3] = {nullptr, nullptr, nullptr};
+  for (int c = 0; c < naxes; c++) {
+    if (!out[c]) { set_error("gbem_assemble_block_dmdt_host: NULL output"); st = GBEM_EINVAL; break; }
+    cudaError_t e = cudaMallocAsync(&d[c], (size_t)m * n * es, g->stream);
+    if (e != cudaSuccess) { st = cuda_status(e, "dMdT scratch"); break; }
+  }
+  if (st == GBEM_OK) st = gbem_assemble_block_dmdt(g, nsa, nsb, omega_re, omega_im, eps, mu, naxes, gamma, d, m, 0, 0, dtype);
+  for (int c = 0; c < naxes && st == GBEM_OK; c++) {
+    cudaError_t e = cudaMemcpy2DAsync((char*)out[c] + ((size_t)row0 + (size_t)col0 * ld) * es, (size_t)ld * es, d[c],
+                                      (size_t)m * es, (size_t)m * es, n, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) st = cuda_status(e, "dMdT download");
+  }
+  for (int c = 0; c < 3; c++)
+    if (d[c]) cudaFreeAsync(d[c], g->stream);
+  cudaStreamSynchronize(g->stream);
+  return st;
+}
+
 gbem_status gbem_assemble_block_host(gbem_geometry* g, int nsa, int nsb, double omega_re, double omega_im,
                                      const double* eps, const double* mu, void* host, int ld, int row0, int col0,
                                      int dtype) {
@@ -593,6 +664,82 @@ gbem_status gbem_lu_solve(gbem_matrix* M, char trans, int nrhs, void* B, int ldb
   cudaFreeAsync(dY, M->stream);
   cudaStreamSynchronize(M->stream);
   return st;
+}
+
+// Tr over the first ncols diagonal entries of M^-1 B (GetTraceMInvdM,
+// applications/scuff-cas3D/CasimirIntegrand.cc:100-146): B holds the
+// derivative blocks of the BEM matrix in its first ncols columns.
+static gbem_status trace_impl(gbem_matrix* M, const void* B, int ldb, int ncols, bool host, double* trace) {
+  if (!M || !B || !trace || ncols <= 0 || ncols > M->N || ldb < M->N) {
+    set_error("gbem_lu_trace: bad arguments");
+    return GBEM_EINVAL;
+  }
+  if (!M->factored) { set_error("gbem_lu_trace: matrix is not factored"); return GBEM_EINVAL; }
+  CHECK_CUDA(cudaSetDevice(M->g->device), "cudaSetDevice");
+  const int N = M->N;
+  cudaStream_t s = M->stream;
+  const bool real = M->dtype == GBEM_F64;
+  const int dt = real ? GBEM_C128 : M->dtype;           // element type of the solve
+  const size_t es = dt == GBEM_C64 ? 8 : 16, ein = real ? 8 : es;
+  void *A = M->d, *tA = nullptr, *X = nullptr, *tB = nullptr;
+  double* d_out = nullptr;
+  int lda = M->ld;
+  gbem_status st = GBEM_OK;
+  cudaError_t e = cudaMallocAsync(&X, (size_t)N * ncols * es, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_out, 2 * sizeof(double), s);
+  if (e == cudaSuccess && real) e = cudaMallocAsync(&tA, (size_t)N * N * 16, s);
+  if (e == cudaSuccess && real && host) e = cudaMallocAsync(&tB, (size_t)N * ncols * 8, s);
+  if (e == cudaSuccess) {
+    const void* src = B;
+    long long lds = ldb;
+    if (host) {
+      // the host B goes through a device buffer: the real one, or X itself
+      void* dst = real ? tB : X;
+      e = cudaMemcpy2DAsync(dst, (size_t)N * ein, B, (size_t)ldb * ein, (size_t)N * ein, ncols, cudaMemcpyHostToDevice, s);
+      src = dst;
+      lds = N;
+    } else if (!real) {
+      e = cudaMemcpy2DAsync(X, (size_t)N * es, B, (size_t)ldb * es, (size_t)N * es, ncols, cudaMemcpyDeviceToDevice, s);
+    }
+    if (e == cudaSuccess && real) {
+      // real factors and B: solved as complex128 with zero imaginary parts
+      make_complex<<<(unsigned)(((long long)N * N + 255) / 256), 256, 0, s>>>((const double*)M->d, M->ld, (double2*)tA,
+                                                                              N, N, N);
+      make_complex<<<(unsigned)(((long long)N * ncols + 255) / 256), 256, 0, s>>>((const double*)src, lds, (double2*)X,
+                                                                                  N, N, ncols);
+      stats_launch(ST_OTHER, 2);
+      A = tA;
+      lda = N;
+      e = cudaGetLastError();
+    }
+  }
+  if (e != cudaSuccess) st = cuda_status(e, "gbem_lu_trace setup");
+  if (st == GBEM_OK) st = lu_solve_many_device(A, N, lda, dt, M->d_perm, ncols, X, N, s);
+  if (st == GBEM_OK) {
+    if (dt == GBEM_C64) trace_diag<float><<<1, 1024, 0, s>>>((const cx<float>*)X, N, ncols, d_out);
+    else trace_diag<double><<<1, 1024, 0, s>>>((const cx<double>*)X, N, ncols, d_out);
+    stats_launch(ST_OTHER);
+    e = cudaMemcpyAsync(trace, d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "gbem_lu_trace");
+  }
+  cudaFreeAsync(X, s); cudaFreeAsync(d_out, s);
+  if (tA) cudaFreeAsync(tA, s);
+  if (tB) cudaFreeAsync(tB, s);
+  cudaStreamSynchronize(s);
+  return st;
+}
+
+gbem_status gbem_lu_trace(gbem_matrix* M, const gbem_matrix* B, int ncols, double* trace) {
+  if (!M || !B || B->N != M->N || B->dtype != M->dtype) {
+    set_error("gbem_lu_trace: B must be a matrix of the same size and type as M");
+    return GBEM_EINVAL;
+  }
+  return trace_impl(M, B->d, B->ld, ncols, false, trace);
+}
+
+gbem_status gbem_lu_trace_host(gbem_matrix* M, const void* B, int ldb, int ncols, double* trace) {
+  return trace_impl(M, B, ldb, ncols, true, trace);
 }
 
 gbem_status gbem_lu_solve_noalloc(gbem_matrix* M, char trans, int nrhs, void* B, int ldb) {

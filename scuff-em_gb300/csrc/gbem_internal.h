@@ -127,8 +127,11 @@ struct BlockSel {
 gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps, const double* mu,
                             int precision, void* dM, int ld, int dtype, cudaStream_t s,
                             const BlockSel* only = nullptr, int only_region = -1);
+// gradients dM/dx_mu (out[mu], null to skip) and, for nta rotation axes with
+// generators gamma (9 per axis), dM/dtheta (outT[a])
 gbem_status assemble_gradient_device(Geometry* g, double wr, double wi, const double* eps, const double* mu,
-                                     const BlockSel& sel, void* const out[3], int ld, int dtype, cudaStream_t s);
+                                     const BlockSel& sel, void* const out[3], int ld, int dtype, cudaStream_t s,
+                                     int nta = 0, const double* gamma = nullptr, void* const* outT = nullptr);
 gbem_status upload_geometry(Geometry* g);
 void free_geometry_device(Geometry* g);
 
@@ -137,6 +140,9 @@ gbem_status lu_factor_device(void* dA, int N, int ld, int dtype, int* d_ipiv, in
                              void** ws, size_t* ws_bytes);
 gbem_status lu_solve_device(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs,
                             void* dB, int ldb, void* dY, cudaStream_t s);
+// X = A^-1 B for many right-hand sides (blocked: block inverses + GEMM updates)
+gbem_status lu_solve_many_device(const void* dA, int N, int ld, int dtype, const int* d_perm, int nrhs, void* dB, int ldb,
+                                 cudaStream_t s);
 gbem_status residual_device(const void* dA, int lda, int dtype, int N, const double* dX, int ldx, const double* dB,
                             int ldb, int nrhs, double* dR, int ldr, void* part, cudaStream_t s);
 // LU solve on a host B whose device workspace is a static array of lu.cu

@@ -606,15 +606,23 @@ __global__ void laswp_kernel(cx<T>* A, long long ld, const int* ipiv, int r0, in
 // U12 = L11^{-1} A12: rows [c0, c0+w), columns [cb, ce), 32 columns per CTA.
 // L11 is walked in 32 x 32 tiles (each diagonal tile, then the tiles below it)
 // through two shared-memory buffers: the next tile's cp.async copy is in
-// flight while the current one is used.  A diagonal tile is a short
-// sequential solve, a tile below it a small GEMM update.
+// flight while the current one is used.  A tile below the diagonal is a
+// small GEMM update.  A diagonal tile is, with dinv set (w a multiple of 32,
+// c0 of 32), one product with the tile's inverse: the unit-lower inverses of
+// the 32 x 32 diagonal blocks live in dinv (1024 elements per block, slot
+// row/32, column-major); a block whose bit is set in make is inverted here
+// first (31 barriers, every CTA, CTA 0 stores it) -- otherwise 31 barriers
+// per tile for every CTA of every solve.  Without dinv, the short
+// sequential solve.
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 template <typename T>
-__global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int ce) {
+__global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int ce,
+                                                   cx<T>* dinv = nullptr, unsigned make = 0u) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][33]
+  cx<T>* Dt = B + w * 33;                          // [32][33]: the diagonal tile's inverse (dinv mode)
   __shared__ __align__(16) cx<T> Lt[2][32][33];    // cp.async targets: element-aligned
   const int j0 = cb + blockIdx.x * 32;
   const int nc = min(32, ce - j0);
@@ -642,7 +650,41 @@ __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c
       cp_async_commit();
       cp_async_wait_1();
       __syncthreads();
-      if (ib == kb) {
+      if (ib == kb && dinv) {
+        // diagonal tile: x = D^-1 y with D^-1 from dinv, or inverted here
+        cx<T>* slot = dinv + (size_t)((c0 + kb) / 32) * 1024;
+        if ((make >> (kb / 32)) & 1u) {
+          for (int q = tid; q < 32 * 32; q += blockDim.x) Dt[(q % 32) * 33 + q / 32] = mk((T)(q % 32 == q / 32), (T)0);
+          __syncthreads();
+          for (int k = 0; k < 31; k++) {
+            for (int q = tid; q < (31 - k) * (k + 1); q += blockDim.x) {
+              const int i = k + 1 + q % (31 - k), j = q / (31 - k);
+              Dt[i * 33 + j] = Dt[i * 33 + j] - Lt[buf][i][k] * Dt[k * 33 + j];
+            }
+            __syncthreads();
+          }
+          if (blockIdx.x == 0)
+            for (int q = tid; q < 1024; q += blockDim.x) slot[q] = Dt[(q % 32) * 33 + q / 32];
+        } else {
+          for (int q = tid; q < 1024; q += blockDim.x) Dt[(q % 32) * 33 + q / 32] = slot[q];
+          __syncthreads();
+        }
+        cx<T> xv[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const int q = tid + t * 256, i = q % 32, j = q / 32;
+          cx<T> acc = mk((T)0, (T)0);
+          if (j < nc)
+            for (int k = 0; k <= i; k++) acc = acc + Dt[i * 33 + k] * B[(kb + k) * 33 + j];
+          xv[t] = acc;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const int q = tid + t * 256, i = q % 32, j = q / 32;
+          if (j < nc) B[(kb + i) * 33 + j] = xv[t];
+        }
+      } else if (ib == kb) {
         // diagonal tile: unit lower solve, columns in parallel
         for (int k = 0; k < kn - 1; k++) {
           for (int q = tid; q < (kn - k - 1) * nc; q += blockDim.x) {
@@ -669,6 +711,29 @@ __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c
     const int i = q % w, j = q / w;
     A[(c0 + i) + (long long)(j0 + j) * ld] = B[i * 33 + j];
   }
+}
+
+// unit-lower inverses of the 32 x 32 diagonal blocks of columns [c0, c0+w)
+// (w a multiple of 32), one CTA per block, into dinv's slots (see trsm_kernel)
+template <typename T>
+__global__ void __launch_bounds__(256) tri_inv_blocks(const cx<T>* A, long long ld, int c0, cx<T>* dinv) {
+  __shared__ cx<T> L[32][33], X[32][33];
+  const int r0 = c0 + 32 * blockIdx.x, tid = threadIdx.x;
+  for (int q = tid; q < 1024; q += blockDim.x) {
+    const int i = q % 32, k = q / 32;
+    L[i][k] = A[(r0 + i) + (long long)(r0 + k) * ld];
+    X[i][k] = mk((T)(i == k), (T)0);
+  }
+  __syncthreads();
+  for (int k = 0; k < 31; k++) {
+    for (int q = tid; q < (31 - k) * (k + 1); q += blockDim.x) {
+      const int i = k + 1 + q % (31 - k), j = q / (31 - k);
+      X[i][j] = X[i][j] - L[i][k] * X[k][j];
+    }
+    __syncthreads();
+  }
+  cx<T>* slot = dinv + (size_t)(r0 / 32) * 1024;
+  for (int q = tid; q < 1024; q += blockDim.x) slot[q] = X[q % 32][q / 32];
 }
 
 // C -= A B (complex, column-major), 64x64 tiles, 4x4 outputs per thread
@@ -786,17 +851,37 @@ static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w,
 // factor columns [c, c+w) of rows [c, N) inside the panel [pc0, pc1): left
 // half, U12 = L11^{-1} A12, A22 -= L21 U12, right half.  The leaves apply
 // their row interchanges to every column of the panel themselves.
+// The U12 solves use the inverted 32 x 32 diagonal blocks of L (dinv, see
+// trsm_kernel) wherever L11 is made of whole 32-blocks: the first solve that
+// needs a block inverts it (made[] marks the blocks already in dinv).
+struct DinvState {
+  cx<float>* dinv = nullptr;
+  std::vector<char> made;
+};
+
+static unsigned dinv_make_mask(DinvState* ds, int c, int h) {
+  unsigned make = 0u;
+  for (int b = 0; b < h / 32; b++) {
+    char& m = ds->made[(c + 32 * b) / 32];
+    if (!m) { make |= 1u << b; m = 1; }
+  }
+  return make;
+}
+
 static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, int pc0, int pc1, int* ipiv, int* info,
-                             int CL, void* tcws, size_t tcb, cudaStream_t s, int* launches) {
+                             int CL, void* tcws, size_t tcb, DinvState* ds, cudaStream_t s, int* launches) {
   if (w <= LEAF_W) {
     ++*launches;
     return leaf_launch(A, ld, N, c, w, pc0, pc1, ipiv, info, CL, s);
   }
   const int h = ((w / 2 + LEAF_W - 1) / LEAF_W) * LEAF_W;
-  cudaError_t e = rec_panel(A, ld, N, c, h, pc0, pc1, ipiv, info, CL, tcws, tcb, s, launches);
+  cudaError_t e = rec_panel(A, ld, N, c, h, pc0, pc1, ipiv, info, CL, tcws, tcb, ds, s, launches);
   if (e != cudaSuccess) return e;
   const int wr = w - h, m2 = N - c - h;
-  trsm_kernel<float><<<(wr + 31) / 32, 256, (size_t)h * 33 * sizeof(cx<float>), s>>>(A, ld, c, h, c + h, c + w);
+  const bool dm = ds && h % 32 == 0 && c % 32 == 0;
+  const unsigned make = dm ? dinv_make_mask(ds, c, h) : 0u;
+  trsm_kernel<float><<<(wr + 31) / 32, 256, (size_t)(h + (dm ? 32 : 0)) * 33 * sizeof(cx<float>), s>>>(
+      A, ld, c, h, c + h, c + w, dm ? ds->dinv : nullptr, make);
   ++*launches;
   if (m2 > 0) {
     cx<float>* C = A + (c + h) + (long long)(c + h) * ld;
@@ -815,7 +900,7 @@ static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, in
     }
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  return rec_panel(A, ld, N, c + h, wr, pc0, pc1, ipiv, info, CL, tcws, tcb, s, launches);
+  return rec_panel(A, ld, N, c + h, wr, pc0, pc1, ipiv, info, CL, tcws, tcb, ds, s, launches);
 }
 
 template <typename T>
@@ -850,7 +935,8 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   size_t need = (size_t)2 * Gmax * w * esz + 2 * (size_t)w * esz + 2 * Gmax * sizeof(Cand) + 256;
   size_t tcb = 0;
   if (sizeof(T) == 4) tcb = tc_gemm_ws_bytes(N, N, w);
-  size_t total = need + tcb + 1024;
+  const size_t dinv_bytes = (size_t)((N + 31) / 32) * 1024 * esz;
+  size_t total = need + tcb + 1024 + dinv_bytes + 256;
   if (*ws_bytes < total) {
     if (*ws) cudaFree(*ws);
     *ws = nullptr;
@@ -866,10 +952,16 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   st.cand = (Cand*)(((uintptr_t)wp + 15) & ~(uintptr_t)15); wp = (unsigned char*)(st.cand + 2 * Gmax);
   int* d_info = (int*)(((uintptr_t)wp + 15) & ~(uintptr_t)15); wp = (unsigned char*)(d_info + 4);
   void* tcws = (void*)(((uintptr_t)wp + 1023) & ~(uintptr_t)1023);
+  cx<T>* dinv = (cx<T>*)(((uintptr_t)tcws + tcb + 255) & ~(uintptr_t)255);
+  DinvState ds;
+  ds.dinv = (cx<float>*)dinv;
+  ds.made.assign((N + 31) / 32, 0);
   e = cudaMemsetAsync(d_info, 0, sizeof(int), s);
   if (e != cudaSuccess) return cuda_status(e, "info");
   // the U12 solves (outer and inside recursive panels) stage at most w rows
-  e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)((size_t)w * 33 * esz));
+  // plus one inverted diagonal tile
+  e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)((size_t)(w + 32) * 33 * esz));
   if (e != cudaSuccess) return cuda_status(e, "trsm smem");
   for (int c0 = 0; c0 < N; c0 += w) {
     const int wc = std::min(w, N - c0);
@@ -885,7 +977,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
       StatTimer tp(ST_PANEL, s);
       if (leaf_cl) {
         int nl = 0;
-        e = rec_panel((cx<float>*)A, ld, N, c0, wc, c0, c0 + wc, d_ipiv, d_info, leaf_cl, tcws, tcb, s, &nl);
+        e = rec_panel((cx<float>*)A, ld, N, c0, wc, c0, c0 + wc, d_ipiv, d_info, leaf_cl, tcws, tcb, &ds, s, &nl);
         stats_launch(ST_PANEL, nl + 1);
         if (e != cudaSuccess) return cuda_status(e, "recursive panel");
       } else {
@@ -900,11 +992,20 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     const int cb = c0 + wc;
     if (cb >= N) break;
     const int nrest = N - cb;
-    size_t tsm = (size_t)wc * 33 * esz;
+    const bool dm = wc % 32 == 0 && c0 % 32 == 0;
+    size_t tsm = (size_t)(wc + (dm ? 32 : 0)) * 33 * esz;
     {
       StatTimer tt(ST_PANEL, s);
+      unsigned make = 0u;
+      if (dm && leaf_cl) {
+        make = dinv_make_mask(&ds, c0, wc);  // blocks no recursive solve inverted yet
+      } else if (dm) {
+        // the grid panel has no recursive solves: invert the panel's blocks first
+        tri_inv_blocks<T><<<wc / 32, 256, 0, s>>>(A, ld, c0, dinv);
+        stats_launch(ST_PANEL);
+      }
       stats_launch(ST_PANEL);
-      trsm_kernel<T><<<(nrest + 31) / 32, 256, tsm, s>>>(A, ld, c0, wc, cb, N);
+      trsm_kernel<T><<<(nrest + 31) / 32, 256, tsm, s>>>(A, ld, c0, wc, cb, N, dm ? dinv : nullptr, make);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
     }
     StatTimer tg(ST_GEMM, s);
@@ -1239,6 +1340,83 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "solve");
   }
   return GBEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Solve with many right-hand sides (X = A^-1 B, trans 'N', nrhs ~ N): the
+// permutation, then per diagonal block the block inverse applied from
+// shared memory and a GEMM update of the rows still to be solved.  Used for
+// Tr[M^-1 dM] (the force and torque integrand of scuff-cas3D), where the
+// right-hand side is a whole block column of dM.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) block_apply(const cx<T>* Dinv, int bs, int n, cx<T>* Y, long long ldy, int i0,
+                                                   int nrhs) {
+  __shared__ cx<T> y[64][17];
+  const int c0 = blockIdx.x * 16;
+  for (int q = threadIdx.x; q < n * 16; q += blockDim.x) {
+    const int r = q % n, c = q / n;
+    y[r][c] = c0 + c < nrhs ? Y[i0 + r + (long long)(c0 + c) * ldy] : mk((T)0, (T)0);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < n * 16; q += blockDim.x) {
+    const int r = q % n, c = q / n;
+    if (c0 + c >= nrhs) continue;
+    cx<T> acc = mk((T)0, (T)0);
+    for (int kk = 0; kk < n; kk++) acc = acc + Dinv[r + (size_t)kk * bs] * y[kk][c];
+    Y[i0 + r + (long long)(c0 + c) * ldy] = acc;
+  }
+}
+
+template <typename T>
+static gbem_status solve_many_impl(const cx<T>* A, int N, int ld, const int* d_perm, int nrhs, cx<T>* B, int ldb,
+                                   cudaStream_t s) {
+  const int bs = sizeof(T) == 4 ? 64 : 32;
+  const int nb = (N + bs - 1) / bs;
+  cx<T>* Y = nullptr;
+  cx<T>* Dinv = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&Y, sizeof(cx<T>) * (size_t)N * nrhs, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&Dinv, sizeof(cx<T>) * (size_t)nb * bs * bs * 2, s);
+  if (e != cudaSuccess) return cuda_status(e, "solve workspace");
+  cx<T>* DinvU = Dinv + (size_t)nb * bs * bs;
+  gather_rows<T><<<(N + 255) / 256, 256, 0, s>>>(B, ldb, Y, N, d_perm, N, nrhs);
+  const size_t ism = sizeof(cx<T>) * 2 * bs * (bs + 1);
+  cudaFuncSetAttribute(diag_inverse<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+  cudaFuncSetAttribute(diag_inverse<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+  diag_inverse<T, true><<<nb, 256, ism, s>>>(A, ld, N, bs, Dinv);
+  diag_inverse<T, false><<<nb, 256, ism, s>>>(A, ld, N, bs, DinvU);
+  const dim3 ga((nrhs + 15) / 16);
+  for (int b = 0; b < nb; b++) {  // forward: unit L
+    const int i0 = b * bs, n = std::min(bs, N - i0), m = N - i0 - n;
+    block_apply<T><<<ga, 256, 0, s>>>(Dinv + (size_t)b * bs * bs, bs, n, Y, N, i0, nrhs);
+    if (m > 0)
+      gemm_simt<T><<<dim3((m + 63) / 64, (nrhs + 63) / 64), 256, 0, s>>>(Y + i0 + n, N, A + (i0 + n) + (long long)i0 * ld,
+                                                                        ld, Y + i0, N, m, nrhs, n);
+  }
+  for (int b = nb - 1; b >= 0; b--) {  // backward: U
+    const int i0 = b * bs, n = std::min(bs, N - i0);
+    block_apply<T><<<ga, 256, 0, s>>>(DinvU + (size_t)b * bs * bs, bs, n, Y, N, i0, nrhs);
+    if (i0 > 0)
+      gemm_simt<T><<<dim3((i0 + 63) / 64, (nrhs + 63) / 64), 256, 0, s>>>(Y, N, A + (long long)i0 * ld, ld, Y + i0, N,
+                                                                         i0, nrhs, n);
+  }
+  stats_launch(ST_SOLVE, 3 + 4 * nb);
+  e = cudaMemcpy2DAsync(B, (size_t)ldb * sizeof(cx<T>), Y, (size_t)N * sizeof(cx<T>), (size_t)N * sizeof(cx<T>), nrhs,
+                        cudaMemcpyDeviceToDevice, s);
+  cudaFreeAsync(Dinv, s);
+  cudaFreeAsync(Y, s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return e == cudaSuccess ? GBEM_OK : cuda_status(e, "solve (many right-hand sides)");
+}
+
+gbem_status lu_solve_many_device(const void* dA, int N, int ld, int dtype, const int* d_perm, int nrhs, void* dB, int ldb,
+                                 cudaStream_t s) {
+  if (dtype == GBEM_C128)
+    return solve_many_impl<double>((const cx<double>*)dA, N, ld, d_perm, nrhs, (cx<double>*)dB, ldb, s);
+  if (dtype == GBEM_C64)
+    return solve_many_impl<float>((const cx<float>*)dA, N, ld, d_perm, nrhs, (cx<float>*)dB, ldb, s);
+  set_error("lu_solve: dtype must be C128 or C64");
+  return GBEM_EINVAL;
 }
 
 gbem_status lu_solve_device(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs, void* dB,

@@ -26,6 +26,7 @@ EXPORTS = [
     "gbem_rhs_planewave", "gbem_solve_mixed_device", "gbem_stats", "gbem_geometry_set_stream",
     "gbem_lu_solve_noalloc", "gbem_assemble_block", "gbem_assemble_block_host",
     "gbem_assemble_block_gradient", "gbem_assemble_block_gradient_host", "gbem_power_emt",
+    "gbem_lu_trace", "gbem_lu_trace_host", "gbem_assemble_block_dmdt", "gbem_assemble_block_dmdt_host",
 ]
 
 
@@ -71,6 +72,10 @@ def lib():
             "gbem_assemble_block_gradient": ([P, I, I, D, D, P, P, P, P, P, I, I, I, I], I),
             "gbem_assemble_block_gradient_host": ([P, I, I, D, D, P, P, P, P, P, I, I, I, I], I),
             "gbem_power_emt": ([P, D, D, P, P, I, I, P, I, P, I, P, P], I),
+            "gbem_lu_trace": ([P, P, I, P], I),
+            "gbem_assemble_block_dmdt": ([P, I, I, D, D, P, P, I, P, P, I, I, I, I], I),
+            "gbem_assemble_block_dmdt_host": ([P, I, I, D, D, P, P, I, P, P, I, I, I, I], I),
+            "gbem_lu_trace_host": ([P, P, I, I, P], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

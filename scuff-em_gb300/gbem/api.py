@@ -104,6 +104,19 @@ class HMatrix:
         self.ipiv, self.info = ipiv, info.value
         return info.value
 
+    def TraceMInvdM(self, dM, ncols=None):
+        """Tr over the first ncols diagonal entries of M^-1 dM for this
+        factored matrix and dM (an HMatrix of the same size and type, or an
+        N x ncols array), the scuff-cas3D force/torque integrand
+        (GetTraceMInvdM, CasimirIntegrand.cc:100-146: force = -2 Re/(2 pi))."""
+        tr = np.zeros(2)
+        if isinstance(dM, HMatrix):
+            check(lib().gbem_lu_trace(self._h, dM._h, ncols or self.N, tr.ctypes.data))
+        else:
+            B = np.asfortranarray(np.asarray(dM, dtype=self.np_dtype).reshape(self.N, -1))
+            check(lib().gbem_lu_trace_host(self._h, B.ctypes.data, self.N, ncols or B.shape[1], tr.ctypes.data))
+        return complex(tr[0], tr[1])
+
     def LUSolve(self, B, Trans="N"):
         """Solve op(M) X = B for a vector or an N x nrhs array; returns X."""
         B = np.asarray(B)
@@ -244,6 +257,28 @@ class RWGGeometry:
         ptr = [o.ctypes.data if o is not None else None for o in out]
         check(lib().gbem_assemble_block_gradient_host(self._h, nsa, nsb, Omega.real, Omega.imag, eps.ctypes.data,
                                                       mu.ctypes.data, ptr[0], ptr[1], ptr[2], m, 0, 0, dt))
+        return out
+
+    def AssembleBEMMatrixBlockTorque(self, nsa, nsb, Omega, axes, real=False):
+        """dMdT[a] = dM_block/dtheta_a for rotations of surface nsa about the
+        given axes through the origin (unit vectors; AssembleBEMMatrixBlock's
+        dMdT with GammaMatrix = the cross-product matrix of each axis).
+        Returns a list of host arrays, one per axis."""
+        axes = [np.asarray(a, dtype=np.float64) for a in axes]
+        gam = np.zeros(9 * len(axes))
+        for a, n in enumerate(axes):
+            for nu in range(3):
+                e = np.zeros(3)
+                e[nu] = 1.0
+                gam[9 * a + 3 * nu:9 * a + 3 * nu + 3] = np.cross(n, e)  # Gamma[mu + 3 nu] = (n x e_nu)_mu
+        dt = F64 if real else C128
+        m, n = self.NumBFs(nsa), self.NumBFs(nsb)
+        out = [np.zeros((m, n), dtype=np.float64 if real else np.complex128, order="F") for _ in axes]
+        ptrs = (ctypes.c_void_p * len(out))(*[o.ctypes.data for o in out])
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        check(lib().gbem_assemble_block_dmdt_host(self._h, nsa, nsb, Omega.real, Omega.imag, eps.ctypes.data,
+                                                  mu.ctypes.data, len(axes), gam.ctypes.data, ptrs, m, 0, 0, dt))
         return out
 
     def GetPFT(self, Omega, KN, RHS=None, precision="fp64"):

@@ -19,6 +19,8 @@ Fixtures:
   ref_fippi_s2.npz reference Q-independent FIPPI data for near pairs.
   ref_<case>.npz   reference BEM matrices (full or a column sample), plane-wave
                    right-hand sides, solutions and EMT powers for small geometries.
+  ref_<case>_grad.npz, ref_<case>_torque.npz  surface blocks with their
+                   derivatives for displacements (GradM) and rotations (dMdT).
   mie_pft_tables.json  the reference's tables of sphere powers (R = 1 um, PEC,
                    SiO2, gold at omega = 0.01, 0.1, 1; unitTests/unit-test-PFT.cc:
                    77-130), read from the test source as text: they pin the Mie
@@ -199,6 +201,35 @@ def grad_case(tmp, name, objects, omega, blocks):
     np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % name), **out)
 
 
+def torque_case(tmp, name, objects, omega, blocks):
+    """Surface blocks and their derivatives dM/dtheta for rotations of the
+    row surface about the x, y, z axes through the origin
+    (AssembleBEMMatrixBlock with NumTorqueAxes = 3, dMdT, GammaMatrix)."""
+    geo = geo_file(tmp, name, objects)
+    out = {"omega": np.array([np.real(omega), np.imag(omega)])}
+    for i, (mname, V, P, mat, disp) in enumerate(objects):
+        out["V%d" % i] = V
+        out["P%d" % i] = P
+        out["mat%d" % i] = np.array(mat if mat is not None else "PEC")
+        out["disp%d" % i] = np.array(disp if disp is not None else (0.0, 0.0, 0.0))
+    for (a, b) in blocks:
+        fn = os.path.join(tmp, "%s_%d%d.bin" % (name, a, b))
+        run(["torqueblock", os.path.basename(geo), np.real(omega), np.imag(omega), a, b, fn], tmp)
+        M, tx, ty, tz = read_rects(fn, 4)
+        out["M%d%d" % (a, b)] = M
+        out["T%d%d" % (a, b)] = np.stack([tx, ty, tz])
+    out["objects"] = np.array(len(objects))
+    np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % name), **out)
+
+
+def torque_fixtures(tmp):
+    V1, P1 = icosphere(1)
+    torque_case(tmp, "pec2_s1_torque", [("a", V1, P1, None, None), ("b", V1, P1, None, (0.0, 0.0, 3.0))], 0.7j,
+                [(0, 1), (1, 0)])
+    torque_case(tmp, "diel2_s1_torque", [("a", V1, P1, "CONST_EPS_2.25+0.01i", None),
+                                         ("b", V1, P1, "CONST_EPS_2.25+0.01i", (0.0, 0.0, 3.0))], 1.5, [(0, 1)])
+
+
 def gradient_fixtures(tmp):
     V1, P1 = icosphere(1)
     # two PEC spheres, centre gap 3, imaginary frequency: every pair of the
@@ -229,16 +260,16 @@ def mie_tables(ref):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["gradients", "mie"], help="regenerate one group of fixtures only")
+    ap.add_argument("--only", choices=["gradients", "torque", "mie"], help="regenerate one group of fixtures only")
     a = ap.parse_args()
     if a.only == "mie":
         mie_tables(a.ref)
         return
     if not os.path.exists(REFDUMP):
         sys.exit("build the reference first: make -C oracle/ref REF=%s" % a.ref)
-    if a.only == "gradients":
+    if a.only in ("gradients", "torque"):
         with tempfile.TemporaryDirectory() as tmp:
-            gradient_fixtures(tmp)
+            (gradient_fixtures if a.only == "gradients" else torque_fixtures)(tmp)
         return
     rng = np.random.default_rng(0)
     with tempfile.TemporaryDirectory() as tmp:
@@ -257,6 +288,7 @@ def main():
         # dielectric sphere at a frequency where high-order / Taylor-Duffy branches appear
         matrix_case(tmp, "diel_s1_w12", [("sph", V1, P1, "CONST_EPS_4+0.1i", None)], 12.0)
         gradient_fixtures(tmp)
+        torque_fixtures(tmp)
     mie_tables(a.ref)
 
 
