@@ -606,23 +606,16 @@ __global__ void laswp_kernel(cx<T>* A, long long ld, const int* ipiv, int r0, in
 // U12 = L11^{-1} A12: rows [c0, c0+w), columns [cb, ce), 32 columns per CTA.
 // L11 is walked in 32 x 32 tiles (each diagonal tile, then the tiles below it)
 // through two shared-memory buffers: the next tile's cp.async copy is in
-// flight while the current one is used.  A tile below the diagonal is a
-// small GEMM update.  A diagonal tile is, with dinv set (w a multiple of 32,
-// c0 of 32), one product with the tile's inverse: the unit-lower inverses of
-// the 32 x 32 diagonal blocks live in dinv (1024 elements per block, slot
-// row/32, column-major); a block whose bit is set in make is inverted here
-// first (31 barriers, every CTA, CTA 0 stores it) -- otherwise 31 barriers
-// per tile for every CTA of every solve.  Without dinv, the short
-// sequential solve.
+// flight while the current one is used.  A diagonal tile is a short
+// sequential solve, a tile below it a small GEMM update.  Used where L11 is
+// not made of whole 32-row blocks (trsm_blocked otherwise).
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 template <typename T>
-__global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int ce,
-                                                   cx<T>* dinv = nullptr, unsigned make = 0u) {
+__global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int ce) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][33]
-  cx<T>* Dt = B + w * 33;                          // [32][33]: the diagonal tile's inverse (dinv mode)
   __shared__ __align__(16) cx<T> Lt[2][32][33];    // cp.async targets: element-aligned
   const int j0 = cb + blockIdx.x * 32;
   const int nc = min(32, ce - j0);
@@ -650,41 +643,7 @@ __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c
       cp_async_commit();
       cp_async_wait_1();
       __syncthreads();
-      if (ib == kb && dinv) {
-        // diagonal tile: x = D^-1 y with D^-1 from dinv, or inverted here
-        cx<T>* slot = dinv + (size_t)((c0 + kb) / 32) * 1024;
-        if ((make >> (kb / 32)) & 1u) {
-          for (int q = tid; q < 32 * 32; q += blockDim.x) Dt[(q % 32) * 33 + q / 32] = mk((T)(q % 32 == q / 32), (T)0);
-          __syncthreads();
-          for (int k = 0; k < 31; k++) {
-            for (int q = tid; q < (31 - k) * (k + 1); q += blockDim.x) {
-              const int i = k + 1 + q % (31 - k), j = q / (31 - k);
-              Dt[i * 33 + j] = Dt[i * 33 + j] - Lt[buf][i][k] * Dt[k * 33 + j];
-            }
-            __syncthreads();
-          }
-          if (blockIdx.x == 0)
-            for (int q = tid; q < 1024; q += blockDim.x) slot[q] = Dt[(q % 32) * 33 + q / 32];
-        } else {
-          for (int q = tid; q < 1024; q += blockDim.x) Dt[(q % 32) * 33 + q / 32] = slot[q];
-          __syncthreads();
-        }
-        cx<T> xv[4];
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-          const int q = tid + t * 256, i = q % 32, j = q / 32;
-          cx<T> acc = mk((T)0, (T)0);
-          if (j < nc)
-            for (int k = 0; k <= i; k++) acc = acc + Dt[i * 33 + k] * B[(kb + k) * 33 + j];
-          xv[t] = acc;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-          const int q = tid + t * 256, i = q % 32, j = q / 32;
-          if (j < nc) B[(kb + i) * 33 + j] = xv[t];
-        }
-      } else if (ib == kb) {
+      if (ib == kb) {
         // diagonal tile: unit lower solve, columns in parallel
         for (int k = 0; k < kn - 1; k++) {
           for (int q = tid; q < (kn - k - 1) * nc; q += blockDim.x) {
@@ -713,8 +672,89 @@ __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c
   }
 }
 
+// U12 = L11^{-1} A12 with the inverted diagonal blocks (w a multiple of 32,
+// c0 of 32): the unit-lower inverses of the 32 x 32 diagonal blocks of L live
+// in dinv (1024 elements per block, slot row/32, column-major); a block whose
+// bit is set in make is inverted here first (31 barriers, every CTA; CTA 0
+// stores it), every later solve reads it.  32 columns per CTA, one 32-row
+// block step at a time: x_b = D_b^-1 y_b, then every row below the block at
+// once, y -= L(rows below, b) x_b, from a column block of L staged in shared
+// memory.  Thread (lane j, warp g) owns column j: rows 4g..4g+3 of x_b and
+// rows g, g+8, ... below, so the L operands of a warp are broadcasts and each
+// column element of x is loaded once per k.  Three barriers per block step.
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_blocked(cx<T>* A, long long ld, int c0, int w, int cb, int ce, cx<T>* dinv,
+                                                    unsigned make) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][33]
+  cx<T>* Lc = B + w * 33;                          // [w][33]: the column block of L at and below the diagonal
+  cx<T>* Dt = Lc + w * 33;                         // [32][33]
+  const int j0 = cb + blockIdx.x * 32;
+  const int nc = min(32, ce - j0);
+  const int tid = threadIdx.x, lane = tid & 31, g = tid >> 5;
+  for (int q = tid; q < w * 32; q += blockDim.x) {
+    const int i = q % w, j = q / w;
+    if (j < nc) cp_async_cx(&B[i * 33 + j], &A[(c0 + i) + (long long)(j0 + j) * ld]);
+  }
+  cp_async_commit();
+  for (int kb = 0; kb < w; kb += 32) {
+    // L(kb.., kb..kb+32): the diagonal tile and everything below it
+    const int R = w - kb;
+    for (int q = tid; q < R * 32; q += blockDim.x) {
+      const int i = q % R, k = q / R;
+      cp_async_cx(&Lc[i * 33 + k], &A[(c0 + kb + i) + (long long)(c0 + kb + k) * ld]);
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    cx<T>* slot = dinv + (size_t)((c0 + kb) / 32) * 1024;
+    if ((make >> (kb / 32)) & 1u) {
+      for (int q = tid; q < 1024; q += blockDim.x) Dt[(q % 32) * 33 + q / 32] = mk((T)(q % 32 == q / 32), (T)0);
+      __syncthreads();
+      for (int k = 0; k < 31; k++) {
+        for (int q = tid; q < (31 - k) * (k + 1); q += blockDim.x) {
+          const int i = k + 1 + q % (31 - k), jj = q / (31 - k);
+          Dt[i * 33 + jj] = Dt[i * 33 + jj] - Lc[i * 33 + k] * Dt[k * 33 + jj];
+        }
+        __syncthreads();
+      }
+      if (blockIdx.x == 0)
+        for (int q = tid; q < 1024; q += blockDim.x) slot[q] = Dt[(q % 32) * 33 + q / 32];
+    } else {
+      for (int q = tid; q < 1024; q += blockDim.x) Dt[(q % 32) * 33 + q / 32] = slot[q];
+      __syncthreads();
+    }
+    // x_b = D^-1 y_b: rows 4g..4g+3 of column lane
+    cx<T> x[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) x[t] = mk((T)0, (T)0);
+    for (int k = 0; k < 4 * g + 4; k++) {
+      const cx<T> y = B[(kb + k) * 33 + lane];
+#pragma unroll
+      for (int t = 0; t < 4; t++)
+        if (k <= 4 * g + t) x[t] = x[t] + Dt[(4 * g + t) * 33 + k] * y;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 4; t++) B[(kb + 4 * g + t) * 33 + lane] = x[t];
+    __syncthreads();
+    // rows below the block: y_i -= sum_k L(i, k) x_k
+    for (int i = 32 + g; i < R; i += 8) {
+      cx<T> acc = mk((T)0, (T)0);
+#pragma unroll 8
+      for (int k = 0; k < 32; k++) acc = acc + Lc[i * 33 + k] * B[(kb + k) * 33 + lane];
+      B[(kb + i) * 33 + lane] = B[(kb + i) * 33 + lane] - acc;
+    }
+    __syncthreads();
+  }
+  for (int q = tid; q < w * nc; q += blockDim.x) {
+    const int i = q % w, j = q / w;
+    A[(c0 + i) + (long long)(j0 + j) * ld] = B[i * 33 + j];
+  }
+}
+
 // unit-lower inverses of the 32 x 32 diagonal blocks of columns [c0, c0+w)
-// (w a multiple of 32), one CTA per block, into dinv's slots (see trsm_kernel)
+// (w a multiple of 32), one CTA per block, into dinv's slots (see trsm_blocked)
 template <typename T>
 __global__ void __launch_bounds__(256) tri_inv_blocks(const cx<T>* A, long long ld, int c0, cx<T>* dinv) {
   __shared__ cx<T> L[32][33], X[32][33];
@@ -880,8 +920,11 @@ static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, in
   const int wr = w - h, m2 = N - c - h;
   const bool dm = ds && h % 32 == 0 && c % 32 == 0;
   const unsigned make = dm ? dinv_make_mask(ds, c, h) : 0u;
-  trsm_kernel<float><<<(wr + 31) / 32, 256, (size_t)(h + (dm ? 32 : 0)) * 33 * sizeof(cx<float>), s>>>(
-      A, ld, c, h, c + h, c + w, dm ? ds->dinv : nullptr, make);
+  if (dm)
+    trsm_blocked<float><<<(wr + 31) / 32, 256, (size_t)(2 * h + 32) * 33 * sizeof(cx<float>), s>>>(
+        A, ld, c, h, c + h, c + w, ds->dinv, make);
+  else
+    trsm_kernel<float><<<(wr + 31) / 32, 256, (size_t)h * 33 * sizeof(cx<float>), s>>>(A, ld, c, h, c + h, c + w);
   ++*launches;
   if (m2 > 0) {
     cx<float>* C = A + (c + h) + (long long)(c + h) * ld;
@@ -960,8 +1003,10 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   if (e != cudaSuccess) return cuda_status(e, "info");
   // the U12 solves (outer and inside recursive panels) stage at most w rows
   // plus one inverted diagonal tile
-  e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)((size_t)(w + 32) * 33 * esz));
+  e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)((size_t)w * 33 * esz));
+  if (e == cudaSuccess && (size_t)(2 * w + 32) * 33 * esz <= smem_cap)
+    e = cudaFuncSetAttribute(trsm_blocked<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)((size_t)(2 * w + 32) * 33 * esz));
   if (e != cudaSuccess) return cuda_status(e, "trsm smem");
   for (int c0 = 0; c0 < N; c0 += w) {
     const int wc = std::min(w, N - c0);
@@ -992,8 +1037,8 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     const int cb = c0 + wc;
     if (cb >= N) break;
     const int nrest = N - cb;
-    const bool dm = wc % 32 == 0 && c0 % 32 == 0;
-    size_t tsm = (size_t)(wc + (dm ? 32 : 0)) * 33 * esz;
+    const bool dm = wc % 32 == 0 && c0 % 32 == 0 && (size_t)(2 * wc + 32) * 33 * esz <= smem_cap;
+    size_t tsm = (size_t)(dm ? 2 * wc + 32 : wc) * 33 * esz;
     {
       StatTimer tt(ST_PANEL, s);
       unsigned make = 0u;
@@ -1005,7 +1050,10 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
         stats_launch(ST_PANEL);
       }
       stats_launch(ST_PANEL);
-      trsm_kernel<T><<<(nrest + 31) / 32, 256, tsm, s>>>(A, ld, c0, wc, cb, N, dm ? dinv : nullptr, make);
+      if (dm)
+        trsm_blocked<T><<<(nrest + 31) / 32, 256, tsm, s>>>(A, ld, c0, wc, cb, N, dinv, make);
+      else
+        trsm_kernel<T><<<(nrest + 31) / 32, 256, tsm, s>>>(A, ld, c0, wc, cb, N);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
     }
     StatTimer tg(ST_GEMM, s);
