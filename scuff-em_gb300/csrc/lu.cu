@@ -680,8 +680,9 @@ __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c
 // block step at a time: x_b = D_b^-1 y_b, then every row below the block at
 // once, y -= L(rows below, b) x_b, from a column block of L staged in shared
 // memory.  Thread (lane j, warp g) owns column j: rows 4g..4g+3 of x_b and
-// rows g, g+8, ... below, so the L operands of a warp are broadcasts and each
-// column element of x is loaded once per k.  Three barriers per block step.
+// rows g, g+8, ... below, with the column's 32 values of x_b in registers,
+// so the only shared-memory operand per complex MAC is an L element that
+// the whole warp reads at once (a broadcast).  Three barriers per block step.
 template <typename T>
 __global__ void __launch_bounds__(256) trsm_blocked(cx<T>* A, long long ld, int c0, int w, int cb, int ce, cx<T>* dinv,
                                                     unsigned make) {
@@ -738,11 +739,15 @@ __global__ void __launch_bounds__(256) trsm_blocked(cx<T>* A, long long ld, int 
 #pragma unroll
     for (int t = 0; t < 4; t++) B[(kb + 4 * g + t) * 33 + lane] = x[t];
     __syncthreads();
-    // rows below the block: y_i -= sum_k L(i, k) x_k
+    // rows below the block: y_i -= sum_k L(i, k) x_k, with the column's x_b in
+    // registers and L(i, k) a broadcast over the warp
+    cx<T> xb[32];
+#pragma unroll
+    for (int k = 0; k < 32; k++) xb[k] = B[(kb + k) * 33 + lane];
     for (int i = 32 + g; i < R; i += 8) {
       cx<T> acc = mk((T)0, (T)0);
-#pragma unroll 8
-      for (int k = 0; k < 32; k++) acc = acc + Lc[i * 33 + k] * B[(kb + k) * 33 + lane];
+#pragma unroll
+      for (int k = 0; k < 32; k++) acc = acc + Lc[i * 33 + k] * xb[k];
       B[(kb + i) * 33 + lane] = B[(kb + i) * 33 + lane] - acc;
     }
     __syncthreads();
