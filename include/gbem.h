@@ -225,6 +225,31 @@ gbem_status gbem_solve_mixed(gbem_geometry *g, double omega_re, double omega_im,
                              const double *B, int ldb, double *X, int ldx,
                              double tol, int max_iter, int *iters, double *resid);
 
+/* A batch of independent mixed-precision solves (frequency sweeps and
+ * multi-geometry jobs of uneven N; no counterpart in the reference, whose
+ * drivers loop over frequencies and geometries one solve at a time).  Up to
+ * max_concurrent jobs run at once, each on its geometry's own CUDA stream
+ * from its own host thread, so the kernels of small jobs share the GPU;
+ * jobs on the same geometry run one after another (a geometry holds one
+ * stream and one set of cached buffers).  Largest N first.  Each job's
+ * status, sweeps and residual are written to its own fields. */
+typedef struct {
+  gbem_geometry *g;
+  double omega_re, omega_im;
+  const double *eps, *mu;  /* per region, interleaved complex (as gbem_assemble) */
+  int nrhs;
+  const double *B;         /* host N x nrhs complex128, column-major */
+  int ldb;
+  double *X;               /* host N x nrhs complex128 */
+  int ldx;
+  double tol;
+  int max_iter;
+  int iters;               /* out */
+  double resid;            /* out */
+  gbem_status status;      /* out */
+} gbem_batch_job;
+gbem_status gbem_solve_mixed_batch(int njobs, gbem_batch_job *jobs, int max_concurrent);
+
 /* Device-resident variant of gbem_solve_mixed: dB and dX are device
  * pointers (N x nrhs complex128, column-major).  No counterpart in the
  * reference, whose solves run on host arrays; it serves callers whose

@@ -1,6 +1,11 @@
 // capi.cu -- the extern "C" boundary declared in include/gbem.h.
+#include <algorithm>
+#include <atomic>
 #include <cstdarg>
+#include <map>
 #include <mutex>
+#include <string>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <cmath>
@@ -64,6 +69,25 @@ static void stats_collect() {
 
 gbem_status rhs_planewave_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, const double* E0,
                                  const double* nh, void* d_rhs, cudaStream_t s);
+
+cudaError_t allow_max_smem_raw(const void* kernel) {
+  static std::mutex mu;
+  static std::vector<std::pair<int, const void*>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> l(mu);
+  for (auto& d : done)
+    if (d.first == dev && d.second == kernel) return cudaSuccess;
+  int optin = 0;
+  cudaFuncAttributes fa;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  if (e == cudaSuccess) done.emplace_back(dev, kernel);
+  return e;
+}
 
 static size_t esize(int dtype) { return dtype == GBEM_C128 ? 16 : (dtype == GBEM_C64 ? 8 : 8); }
 static bool omega_is_zero(double wr, double wi) { return wr == 0.0 && wi == 0.0; }
@@ -954,6 +978,47 @@ gbem_status gbem_solve_mixed(gbem_geometry* g, double omega_re, double omega_im,
                              int nrhs, const double* B, int ldb, double* X, int ldx, double tol, int max_iter, int* iters,
                              double* resid) {
   return solve_mixed_impl(g, omega_re, omega_im, eps, mu, nrhs, B, ldb, true, X, ldx, true, tol, max_iter, iters, resid);
+}
+
+gbem_status gbem_solve_mixed_batch(int njobs, gbem_batch_job* jobs, int max_concurrent) {
+  if (njobs < 0 || (njobs > 0 && !jobs) || max_concurrent < 1) {
+    set_error("gbem_solve_mixed_batch: bad arguments");
+    return GBEM_EINVAL;
+  }
+  for (int i = 0; i < njobs; i++)
+    if (!jobs[i].g) { set_error("gbem_solve_mixed_batch: job %d has no geometry", i); return GBEM_EINVAL; }
+  // largest N first; one lock per geometry (its stream and cached buffers)
+  std::vector<int> order(njobs);
+  for (int i = 0; i < njobs; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return jobs[a].g->N > jobs[b].g->N; });
+  std::map<gbem_geometry*, std::mutex> locks;
+  for (int i = 0; i < njobs; i++) locks[jobs[i].g];
+  std::atomic<int> next(0);
+  std::vector<std::string> errs(njobs);
+  auto worker = [&]() {
+    for (;;) {
+      const int q = next.fetch_add(1);
+      if (q >= njobs) return;
+      gbem_batch_job& j = jobs[order[q]];
+      std::lock_guard<std::mutex> l(locks[j.g]);
+      j.iters = 0;
+      j.resid = 0.0;
+      j.status = gbem_solve_mixed(j.g, j.omega_re, j.omega_im, j.eps, j.mu, j.nrhs, j.B, j.ldb, j.X, j.ldx, j.tol,
+                                  j.max_iter, &j.iters, &j.resid);
+      if (j.status != GBEM_OK && j.status != GBEM_ENOCONV) errs[order[q]] = gbem_last_error();
+    }
+  };
+  const int nt = std::min(max_concurrent, std::max(njobs, 1));
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; t++) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
+  gbem_status worst = GBEM_OK;
+  int bad = -1;
+  for (int i = 0; i < njobs; i++)
+    if (jobs[i].status != GBEM_OK && jobs[i].status != GBEM_ENOCONV) { worst = jobs[i].status; if (bad < 0) bad = i; }
+  if (bad >= 0) set_error("gbem_solve_mixed_batch: job %d: %s", bad, errs[bad].c_str());
+  return worst;
 }
 
 gbem_status gbem_solve_mixed_device(gbem_geometry* g, double omega_re, double omega_im, const double* eps,

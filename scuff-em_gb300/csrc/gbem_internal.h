@@ -162,6 +162,14 @@ struct StatTimer {
   ~StatTimer();
 };
 
+// Raise a kernel's dynamic shared-memory limit to what the device allows
+// (its opt-in maximum less the kernel's static shared memory), once per
+// kernel and device.  The limit is process-wide state of the function:
+// setting it to each launch's own size would let concurrent solves of
+// different sizes lower it under one another's launches.
+cudaError_t allow_max_smem_raw(const void* kernel);
+template <typename K> inline cudaError_t allow_max_smem(K* kernel) { return allow_max_smem_raw((const void*)kernel); }
+
 // error helpers
 void set_error(const char* fmt, ...);
 gbem_status cuda_status(cudaError_t e, const char* what);

@@ -396,7 +396,7 @@ bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long l
   if (!make_map(&ma, pa, m, Kp, tc::BM) || !make_map(&mb, pb, 2 * n, Kp, tc::BN)) return false;
   static bool attr = false;
   if (!attr) {
-    *err = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+    *err = allow_max_smem(tc_gemm_kernel);
     if (*err != cudaSuccess) return false;
     attr = true;
   }

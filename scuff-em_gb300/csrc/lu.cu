@@ -834,7 +834,10 @@ static int leaf_cluster_size(int N, int smem_optin) {
   for (int CL : {16, 8}) {
     const size_t smem = (size_t)((N + CL - 1) / CL) * LEAF_STRIDE * sizeof(cx<float>);
     if (smem + 2048 > (size_t)smem_optin) continue;
-    if (cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) continue;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, leaf_kernel) != cudaSuccess || smem + fa.sharedSizeBytes > (size_t)smem_optin ||
+        allow_max_smem(leaf_kernel) != cudaSuccess)
+      continue;
     if (CL > 8 && (cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
                    cudaFuncSetAttribute(leaf_kernel_reg<1, 1024>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                        cudaSuccess ||
@@ -859,38 +862,99 @@ static int leaf_cluster_size(int N, int smem_optin) {
   return 0;
 }
 
-static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w, int pc0, int pc1, int* ipiv, int* info,
-                               int CL, cudaStream_t s) {
-  const int m = N - c0;
-  LeafArgs la;
-  la.A = A; la.ld = ld; la.N = N; la.c0 = c0; la.w = w; la.Rr = (m + CL - 1) / CL; la.ipiv = ipiv; la.info = info;
-  la.pc0 = pc0; la.pc1 = pc1;
+static cudaError_t leaf_launch_shape(const LeafArgs& la, int CL, int shape, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CL);
-  cfg.blockDim = dim3(512);
+  cfg.blockDim = dim3(shape == 1024 ? 1024 : 512);
   cfg.stream = s;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  // rows in registers when each thread holds at most two, else in shared memory
-  // 512-thread CTAs holding up to two rows per thread measured faster than
-  // 1024-thread CTAs with one row each (45.7 vs 49.8 us per 16-column leaf
-  // at 960 rows per CTA); GBEM_LU_LEAF_THREADS=1024 selects the latter
-  static int threads = -1;
-  if (threads < 0) {
-    const char* e = getenv("GBEM_LU_LEAF_THREADS");
-    threads = (e && atoi(e) == 1024) ? 1024 : 512;
-  }
-  if (la.Rr <= 1024 && threads == 1024) {
-    cfg.blockDim = dim3(1024);
-    return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<1, 1024>, la);
-  }
+  if (la.Rr <= 1024 && shape == 1024) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<1, 1024>, la);
   if (la.Rr <= 512) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<1, 512>, la);
   if (la.Rr <= 1024) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<2, 512>, la);
+  // rows in shared memory beyond two per thread
   cfg.dynamicSmemBytes = (size_t)la.Rr * LEAF_STRIDE * sizeof(cx<float>);
   return cudaLaunchKernelEx(&cfg, leaf_kernel, la);
+}
+
+// Leaf shape autotuner.  For 512 < rows per CTA <= 1024 the leaf exists in
+// two register shapes, 1024 threads x 1 row and 512 threads x 2 rows, whose
+// order depends on the row count (45.7 vs 49.8 us for the latter at 960
+// rows).  The first leaf of each 64-row bucket (per device) times both on a
+// scratch copy of its panel columns -- the same data, the real launch
+// geometry -- and the faster shape serves every later leaf of that bucket.
+// GBEM_LU_LEAF_THREADS=512 or 1024 fixes the shape instead.
+static int leaf_shape(const LeafArgs& la, int CL, cudaStream_t s) {
+  if (la.Rr <= 512 || la.Rr > 1024) return 512;
+  static int forced = -1;
+  if (forced < 0) {
+    const char* e = getenv("GBEM_LU_LEAF_THREADS");
+    forced = e ? (atoi(e) == 1024 ? 1024 : 512) : 0;
+  }
+  if (forced) return forced;
+  static std::mutex mu;
+  static std::vector<std::pair<long long, int>> tuned;  // (device * 1024 + bucket, shape)
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const long long key = (long long)dev * 1024 + (la.Rr - 1) / 64;
+  {
+    std::lock_guard<std::mutex> l(mu);
+    for (auto& t : tuned)
+      if (t.first == key) return t.second;
+  }
+  // scratch: the leaf's rows [c0, N) of the panel columns [pc0, pc1), with
+  // its own pivots and info, indexed like the real matrix
+  const long long rows = la.N - la.c0, cols = la.pc1 - la.pc0;
+  cx<float>* scr = nullptr;
+  int* sp = nullptr;
+  int best = 512;
+  float tbest = 1e30f;
+  if (cudaMallocAsync((void**)&scr, sizeof(cx<float>) * (size_t)(rows * cols), s) == cudaSuccess &&
+      cudaMallocAsync((void**)&sp, sizeof(int) * (size_t)(la.N + 1), s) == cudaSuccess) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    LeafArgs t = la;
+    t.ld = rows;
+    t.A = scr - la.c0 - (long long)la.pc0 * rows;  // element (r, c) of the panel at scr[(r - c0) + (c - pc0) rows]
+    t.ipiv = sp;
+    t.info = sp + la.N;
+    for (int shape : {512, 1024}) {
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; rep++) {
+        cudaMemcpy2DAsync(scr, rows * sizeof(cx<float>), la.A + la.c0 + (long long)la.pc0 * la.ld,
+                          la.ld * sizeof(cx<float>), rows * sizeof(cx<float>), cols, cudaMemcpyDeviceToDevice, s);
+        cudaMemsetAsync(t.info, 0, sizeof(int), s);
+        cudaEventRecord(e0, s);
+        cudaError_t e = leaf_launch_shape(t, CL, shape, s);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        if (e != cudaSuccess) { ms = 1e30f; break; }
+        cudaEventElapsedTime(&ms, e0, e1);
+      }
+      if (ms < tbest) { tbest = ms; best = shape; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  cudaGetLastError();
+  if (scr) cudaFreeAsync(scr, s);
+  if (sp) cudaFreeAsync(sp, s);
+  std::lock_guard<std::mutex> l(mu);
+  tuned.emplace_back(key, best);
+  return best;
+}
+
+static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w, int pc0, int pc1, int* ipiv, int* info,
+                               int CL, cudaStream_t s) {
+  const int m = N - c0;
+  LeafArgs la;
+  la.A = A; la.ld = ld; la.N = N; la.c0 = c0; la.w = w; la.Rr = (m + CL - 1) / CL; la.ipiv = ipiv; la.info = info;
+  la.pc0 = pc0; la.pc1 = pc1;
+  return leaf_launch_shape(la, CL, leaf_shape(la, CL, s), s);
 }
 
 // factor columns [c, c+w) of rows [c, N) inside the panel [pc0, pc1): left
@@ -973,7 +1037,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   if (w > N) w = std::max(1, N);
   R = std::max(R, 1);
   size_t smem = std::min((size_t)(R * panel_stride(w) + w) * esz, smem_cap);
-  cudaError_t e = cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = allow_max_smem(panel_kernel<T>);
   if (e != cudaSuccess) return cuda_status(e, "panel smem");
   int maxb = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, panel_kernel<T>, 512, smem);
@@ -1008,10 +1072,8 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   if (e != cudaSuccess) return cuda_status(e, "info");
   // the U12 solves (outer and inside recursive panels) stage at most w rows
   // plus one inverted diagonal tile
-  e = cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)((size_t)w * 33 * esz));
-  if (e == cudaSuccess && (size_t)(2 * w + 32) * 33 * esz <= smem_cap)
-    e = cudaFuncSetAttribute(trsm_blocked<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)((size_t)(2 * w + 32) * 33 * esz));
+  e = allow_max_smem(trsm_kernel<T>);
+  if (e == cudaSuccess) e = allow_max_smem(trsm_blocked<T>);
   if (e != cudaSuccess) return cuda_status(e, "trsm smem");
   for (int c0 = 0; c0 < N; c0 += w) {
     const int wc = std::min(w, N - c0);
@@ -1345,16 +1407,16 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
       if (e != cudaSuccess) return cuda_status(e, "solve workspace");
       cx<T>* DinvU = Dinv + (size_t)nb * bs * bs;
       size_t ism = sizeof(cx<T>) * 2 * bs * (bs + 1);
-      cudaFuncSetAttribute(diag_inverse<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
-      cudaFuncSetAttribute(diag_inverse<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+      allow_max_smem(diag_inverse<T, true>);
+      allow_max_smem(diag_inverse<T, false>);
       diag_inverse<T, true><<<nb, 256, ism, s>>>(A, ld, N, bs, Dinv);
       diag_inverse<T, false><<<nb, 256, ism, s>>>(A, ld, N, bs, DinvU);
       int dev = 0, nsm = 0, per = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
       size_t dsm = sizeof(cx<T>) * 2 * bs * bs;
-      cudaFuncSetAttribute(trsv_coop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
-      cudaFuncSetAttribute(trsv_coop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+      allow_max_smem(trsv_coop<T, true>);
+      allow_max_smem(trsv_coop<T, false>);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, dsm);
       // 4 threads per row; one CTA per SM is enough to keep the reads in flight
       int G = std::max(1, std::min(nsm * std::max(per, 1), std::min(nsm, (4 * N + 255) / 256)));
@@ -1434,8 +1496,8 @@ static gbem_status solve_many_impl(const cx<T>* A, int N, int ld, const int* d_p
   cx<T>* DinvU = Dinv + (size_t)nb * bs * bs;
   gather_rows<T><<<(N + 255) / 256, 256, 0, s>>>(B, ldb, Y, N, d_perm, N, nrhs);
   const size_t ism = sizeof(cx<T>) * 2 * bs * (bs + 1);
-  cudaFuncSetAttribute(diag_inverse<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
-  cudaFuncSetAttribute(diag_inverse<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+  allow_max_smem(diag_inverse<T, true>);
+  allow_max_smem(diag_inverse<T, false>);
   diag_inverse<T, true><<<nb, 256, ism, s>>>(A, ld, N, bs, Dinv);
   diag_inverse<T, false><<<nb, 256, ism, s>>>(A, ld, N, bs, DinvU);
   const dim3 ga((nrhs + 15) / 16);
@@ -1659,16 +1721,16 @@ static gbem_status solve_chunk_n(const cx<T>* A, int N, int ld, const int* d_per
   gather_rows<T><<<(N + 255) / 256, 256, 0, s>>>(Bc, ldb, Y, N, d_perm, N, nr);
   cx<T>* DinvU = Dinv + (size_t)nb * bs * bs;
   size_t ism = sizeof(cx<T>) * 2 * bs * (bs + 1);
-  cudaFuncSetAttribute(diag_inverse<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
-  cudaFuncSetAttribute(diag_inverse<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
+  allow_max_smem(diag_inverse<T, true>);
+  allow_max_smem(diag_inverse<T, false>);
   diag_inverse<T, true><<<nb, 256, ism, s>>>(A, ld, N, bs, Dinv);
   diag_inverse<T, false><<<nb, 256, ism, s>>>(A, ld, N, bs, DinvU);
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   size_t dsm = sizeof(cx<T>) * 2 * bs * bs;
-  cudaFuncSetAttribute(trsv_coop<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
-  cudaFuncSetAttribute(trsv_coop<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+  allow_max_smem(trsv_coop<T, true>);
+  allow_max_smem(trsv_coop<T, false>);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, dsm);
   int G = std::max(1, std::min(nsm * std::max(per, 1), std::min(nsm, (4 * N + 255) / 256)));
   int Nn = N, bsn = bs, nrn = nr;

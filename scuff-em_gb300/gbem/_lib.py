@@ -27,6 +27,7 @@ EXPORTS = [
     "gbem_lu_solve_noalloc", "gbem_assemble_block", "gbem_assemble_block_host",
     "gbem_assemble_block_gradient", "gbem_assemble_block_gradient_host", "gbem_power_emt",
     "gbem_lu_trace", "gbem_lu_trace_host", "gbem_assemble_block_dmdt", "gbem_assemble_block_dmdt_host",
+    "gbem_solve_mixed_batch",
 ]
 
 
@@ -40,6 +41,14 @@ class SurfaceDesc(ctypes.Structure):
     _fields_ = [("num_vertices", ctypes.c_int), ("vertices", ctypes.c_void_p), ("num_panels", ctypes.c_int),
                 ("panel_vertices", ctypes.c_void_p), ("exterior_region", ctypes.c_int),
                 ("interior_region", ctypes.c_int), ("is_pec", ctypes.c_int)]
+
+
+class BatchJob(ctypes.Structure):
+    _fields_ = [("g", ctypes.c_void_p), ("omega_re", ctypes.c_double), ("omega_im", ctypes.c_double),
+                ("eps", ctypes.c_void_p), ("mu", ctypes.c_void_p), ("nrhs", ctypes.c_int), ("B", ctypes.c_void_p),
+                ("ldb", ctypes.c_int), ("X", ctypes.c_void_p), ("ldx", ctypes.c_int), ("tol", ctypes.c_double),
+                ("max_iter", ctypes.c_int), ("iters", ctypes.c_int), ("resid", ctypes.c_double),
+                ("status", ctypes.c_int)]
 
 
 _lib = None
@@ -73,6 +82,7 @@ def lib():
             "gbem_assemble_block_gradient_host": ([P, I, I, D, D, P, P, P, P, P, I, I, I, I], I),
             "gbem_power_emt": ([P, D, D, P, P, I, I, P, I, P, I, P, P], I),
             "gbem_lu_trace": ([P, P, I, P], I),
+            "gbem_solve_mixed_batch": ([I, P, I], I),
             "gbem_assemble_block_dmdt": ([P, I, I, D, D, P, P, I, P, P, I, I, I, I], I),
             "gbem_assemble_block_dmdt_host": ([P, I, I, D, D, P, P, I, P, P, I, I, I, I], I),
             "gbem_lu_trace_host": ([P, P, I, I, P], I),

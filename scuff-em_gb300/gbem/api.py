@@ -325,3 +325,31 @@ class RWGGeometry:
         if st not in (_lib.GBEM_OK, _lib.GBEM_ENOCONV):
             check(st)
         return X, it.value, res.value
+
+
+def solve_mixed_batch(jobs, max_concurrent=4, tol=1e-10, max_iter=10):
+    """Independent mixed-precision solves run as one batch
+    (gbem_solve_mixed_batch): jobs is a list of (RWGGeometry, Omega, B);
+    up to max_concurrent at once, each on its geometry's stream from its own
+    host thread, jobs on one geometry in turn, largest N first.  Returns
+    [(X, iterations, relative residual)] in job order."""
+    arr = (_lib.BatchJob * len(jobs))()
+    keep = []
+    for j, (G, Omega, B) in enumerate(jobs):
+        eps, mu = G.eps_mu(Omega)
+        Omega = complex(Omega)
+        B = np.asfortranarray(np.asarray(B, dtype=np.complex128).reshape(G.TotalBFs, -1))
+        X = np.zeros_like(B, order="F")
+        keep.append((eps, mu, B, X))
+        arr[j].g = G._h
+        arr[j].omega_re, arr[j].omega_im = Omega.real, Omega.imag
+        arr[j].eps, arr[j].mu = eps.ctypes.data, mu.ctypes.data
+        arr[j].nrhs = B.shape[1]
+        arr[j].B, arr[j].ldb = B.ctypes.data, G.TotalBFs
+        arr[j].X, arr[j].ldx = X.ctypes.data, G.TotalBFs
+        arr[j].tol, arr[j].max_iter = tol, max_iter
+    st = lib().gbem_solve_mixed_batch(len(jobs), arr, max_concurrent)
+    if st not in (_lib.GBEM_OK, _lib.GBEM_ENOCONV):
+        check(st)
+    return [(keep[j][3], arr[j].iters, arr[j].resid) for j in range(len(jobs))]
+

@@ -55,7 +55,7 @@ def build(verbose: bool = False) -> str:
                 print(lg)
     objs = [os.path.join(BUILD, u + ".o") for u in CUDA_UNITS + CXX_UNITS]
     tmp = OUT + ".tmp"
-    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
     os.replace(tmp, OUT)
     return OUT
 
