@@ -701,41 +701,44 @@ struct PPairArgs {
   float* out;         // [NF][9][ncp][nrow]
 };
 
-// pass 1: block (32, 8) = 32 row panels x 8 column panels, one pair per thread
+// pass 1: block (32, PP_COLS) = 32 row panels x PP_COLS column panels, one
+// pair per thread; 168 registers let 12 warps share an SM
+constexpr int PP_COLS = 12, PP_SLOTS = 32 + PP_COLS, PP_THREADS = 32 * PP_COLS;
+
 template <int NC>
-__global__ void __launch_bounds__(256) ppair_kernel(PPairArgs p, RegionArgs ra) {
+__global__ void __launch_bounds__(PP_THREADS, 1) ppair_kernel(PPairArgs p, RegionArgs ra) {
   constexpr int NF = ppair_fields<NC>();
-  __shared__ float s_node[40][NODE_STRIDE];
-  __shared__ float s_geo[40][GEO_STRIDE];
-  __shared__ double s_pcd[40][4];
-  __shared__ float s_cf[40][4];
+  __shared__ float s_node[PP_SLOTS][NODE_STRIDE];
+  __shared__ float s_geo[PP_SLOTS][GEO_STRIDE];
+  __shared__ double s_pcd[PP_SLOTS][4];
+  __shared__ float s_cf[PP_SLOTS][4];
   __shared__ SinCosTab s_tab;
   __shared__ FFRule s_rule;
   __shared__ cff s_k[2], s_m4[2], s_p1[2], s_p3[2];  // s_k[r] = (Re k, Im k) as float-float
   __shared__ cx<float> s_pcf[2];
   __shared__ int s_live[2];
   const int tid = threadIdx.y * 32 + threadIdx.x;
-  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 8;
-  // the CTA's 32 row and 8 column panels (global index, -1 past the end)
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * PP_COLS;
+  // the CTA's 32 row and PP_COLS column panels (global index, -1 past the end)
   auto panel_of = [&](int sl) -> int {
     if (sl < 32) return r0 + sl < p.nrow ? p.offa + r0 + sl : -1;
     return c0 + sl - 32 < p.ncp ? p.offb + p.cpan[c0 + sl - 32] : -1;
   };
-  for (int q = tid; q < 40 * 36; q += 256) {
+  for (int q = tid; q < PP_SLOTS * 36; q += PP_THREADS) {
     const int sl = q / 36, f = q - sl * 36, gp = panel_of(sl);
     if (gp >= 0) s_node[sl][f] = p.node[36 * (size_t)gp + f];
   }
-  for (int q = tid; q < 40 * 18; q += 256) {
+  for (int q = tid; q < PP_SLOTS * 18; q += PP_THREADS) {
     const int sl = q / 18, f = q - sl * 18, gp = panel_of(sl);
     if (gp >= 0) s_geo[sl][f] = p.geo[18 * (size_t)gp + f];
   }
-  for (int q = tid; q < 40 * 4; q += 256) {
+  for (int q = tid; q < PP_SLOTS * 4; q += PP_THREADS) {
     const int sl = q / 4, f = q - sl * 4, gp = panel_of(sl);
     if (gp >= 0) { s_pcd[sl][f] = p.pc[4 * (size_t)gp + f]; s_cf[sl][f] = (float)p.pc[4 * (size_t)gp + f]; }
   }
-  for (int q = tid; q < (int)(sizeof(SinCosTab) / 4); q += 256)
+  for (int q = tid; q < (int)(sizeof(SinCosTab) / 4); q += PP_THREADS)
     reinterpret_cast<float*>(&s_tab)[q] = reinterpret_cast<const float*>(&c_sctab)[q];
-  for (int q = tid; q < (int)(sizeof(FFRule) / 4); q += 256)
+  for (int q = tid; q < (int)(sizeof(FFRule) / 4); q += PP_THREADS)
     reinterpret_cast<float*>(&s_rule)[q] = reinterpret_cast<const float*>(&c_ffrule)[q];
   if (tid < 2) {
     // region constants, formed once per CTA in FP64
@@ -905,7 +908,7 @@ static inline cx<double> cxd(double r, double i) { return mk(r, i); }
 template <int NC>
 static cudaError_t launch_tiles64(const TileArgs& ta, const RegionArgs& ra, int ntiles, cudaStream_t s) {
   const size_t smem = (size_t)TE * TE * 4 * NC * sizeof(cx<double>);
-  cudaError_t e = cudaFuncSetAttribute(tile_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = allow_max_smem(tile_kernel<NC>);
   if (e != cudaSuccess) return e;
   tile_kernel<NC><<<ntiles, 256, smem, s>>>(ta, ra);
   return cudaGetLastError();
@@ -936,7 +939,7 @@ static cudaError_t far_mixed(Geometry* g, const Block& b, DevBlock* db, const Ti
     pp.node = g->d_ffnode; pp.geo = g->d_ffgeo; pp.pc = g->d_pc; pp.cpan = st.cpan;
     pp.offa = g->S[b.sa].panel_offset; pp.offb = g->S[b.sb].panel_offset;
     pp.nrow = st.nrow; pp.ncp = st.ncp; pp.out = (float*)g->ppv;
-    ppair_kernel<NC><<<dim3((st.nrow + 31) / 32, (st.ncp + 7) / 8), dim3(32, 8), 0, s>>>(pp, ra);
+    ppair_kernel<NC><<<dim3((st.nrow + 31) / 32, (st.ncp + PP_COLS - 1) / PP_COLS), dim3(32, PP_COLS), 0, s>>>(pp, ra);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     StampArgs sp;
     sp.ta = ta; sp.tiles = st.tiles; sp.edge_a = db->edge_a; sp.edge_b = db->edge_b; sp.ecol = db->ecol;
