@@ -1266,16 +1266,21 @@ __global__ void __launch_bounds__(256) diag_inverse(const cx<T>* A, long long ld
 // block.  Step s applies x_k (k = the s-th block in solve order) to the rows
 // still unsolved: CTA 0 takes the rows of the next block k1 and at once solves
 // that block from shared memory (x_k1 = Dinv_k1 (y_k1 - A(k1, k) x_k)), while
-// the other CTAs update every row beyond k1.  Before the barrier CTA 0 stages
-// the next step's Dinv block and A(k2 rows, k1 columns) in shared memory.
-// Dynamic shared memory: 2 * bs * bs elements (bs <= 64, nrhs <= 8).
+// the other CTAs update every row beyond k1.  CTA 0's operands for the next
+// step (Dinv_k2 and A(k2 rows, k1 columns)) do not depend on x, so their
+// cp.async copies into the second buffer are issued at the start of a step
+// and land during its work and the grid barrier, off the critical path.
+// Dynamic shared memory: 4 * bs * bs elements (bs <= 64, nrhs <= 8).
 template <typename T, bool LOWER>
 __global__ void __launch_bounds__(256) trsv_coop(const cx<T>* A, long long lda, int N, int bs, const cx<T>* Dinv,
                                                   cx<T>* Y, int nrhs) {
   cg::grid_group grid = cg::this_grid();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<T>* D = reinterpret_cast<cx<T>*>(smem_raw);  // Dinv of the block CTA 0 solves next, bs x bs column-major
-  cx<T>* Ab = D + bs * bs;                          // A(rows of that block, columns of the current one)
+  cx<T>* base = reinterpret_cast<cx<T>*>(smem_raw);
+  // per buffer: Dinv of the block CTA 0 solves next (bs x bs, column-major)
+  // and A(rows of that block, columns of the current one)
+  cx<T>* const Dbuf[2] = {base, base + 2 * bs * bs};
+  cx<T>* const Abuf[2] = {base + bs * bs, base + 3 * bs * bs};
   __shared__ cx<T> xs[64][8];                       // x of the block CTA 0 solved last
   __shared__ cx<T> rk[64][8];
   __shared__ cx<T> xk[64][8];                       // x_k for the general update
@@ -1284,40 +1289,34 @@ __global__ void __launch_bounds__(256) trsv_coop(const cx<T>* A, long long lda, 
   const cx<T> zero = mk((T)0, (T)0);
   auto kb_of = [&](int s) { return LOWER ? s : nb - 1 - s; };
   auto n_of = [&](int k) { return min(bs, N - k * bs); };
-  // CTA 0: D <- Dinv[kd], Ab <- A(rows of block kr, columns of block kc); loads batched 8 deep
-  auto stage = [&](int kd, int kr, int kc) {
+  // CTA 0: Dbuf[b] <- Dinv[kd], Abuf[b] <- A(rows of block kr, columns of block kc), asynchronously
+  auto stage = [&](int b, int kd, int kr, int kc) {
     const cx<T>* Dg = Dinv + (size_t)kd * bs * bs;
     const int nr_ = n_of(kr), nc_ = n_of(kc), r0_ = kr * bs, c0_ = kc * bs, bb = bs * bs;
-    for (int q0 = 0; q0 < bb; q0 += nt * 8) {
-      cx<T> v[8], u[8];
-#pragma unroll
-      for (int t = 0; t < 8; t++) {
-        const int q = q0 + t * nt + tid, r = q % bs, cc = q / bs;
-        v[t] = q < bb ? Dg[q] : zero;
-        u[t] = (q < bb && r < nr_ && cc < nc_) ? A[(r0_ + r) + (long long)(c0_ + cc) * lda] : zero;
-      }
-#pragma unroll
-      for (int t = 0; t < 8; t++) {
-        const int q = q0 + t * nt + tid;
-        if (q < bb) { D[q] = v[t]; Ab[q] = u[t]; }
-      }
+    for (int q = tid; q < bb; q += nt) {
+      const int r = q % bs, cc = q / bs;
+      cp_async_cx(&Dbuf[b][q], Dg + q);
+      if (r < nr_ && cc < nc_) cp_async_cx(&Abuf[b][q], &A[(r0_ + r) + (long long)(c0_ + cc) * lda]);
+      else Abuf[b][q] = zero;
     }
+    cp_async_commit();
   };
   if (blockIdx.x == 0) {
     // first block: x = Dinv y
     const int k = kb_of(0), i0 = k * bs, n = n_of(k);
-    stage(k, k, k);
+    stage(0, k, k, k);
     for (int q = tid; q < n * nrhs; q += nt) rk[q % n][q / n] = ldcg_cx(Y + i0 + q % n + (long long)(q / n) * N);
+    cp_async_wait_all();
     __syncthreads();
     for (int q = tid; q < n * nrhs; q += nt) {
       const int r = q % n, c = q / n;
       cx<T> acc = zero;
-      for (int kk = 0; kk < n; kk++) acc = acc + D[r + kk * bs] * rk[kk][c];
+      for (int kk = 0; kk < n; kk++) acc = acc + Dbuf[0][r + kk * bs] * rk[kk][c];
       Y[i0 + r + (long long)c * N] = acc;
       xs[r][c] = acc;
     }
     __syncthreads();
-    if (nb > 1) stage(kb_of(1), kb_of(1), k);
+    if (nb > 1) stage(1, kb_of(1), kb_of(1), k);
     __threadfence();
   }
   grid.sync();
@@ -1325,6 +1324,12 @@ __global__ void __launch_bounds__(256) trsv_coop(const cx<T>* A, long long lda, 
     const int k = kb_of(s), k1 = kb_of(s + 1);
     const int i0 = k * bs, n = n_of(k), i1 = k1 * bs, n1 = n_of(k1);
     if (blockIdx.x == 0) {
+      const int cur = (s + 1) & 1;
+      cp_async_wait_all();  // this step's operands
+      __syncthreads();
+      if (s + 2 < nb) stage(cur ^ 1, kb_of(s + 2), kb_of(s + 2), k1);  // the next step's, in flight meanwhile
+      const cx<T>* D = Dbuf[cur];
+      const cx<T>* Ab = Abuf[cur];
       // rows of k1: r = y - A(k1, k) x_k, then x_k1 = Dinv_k1 r
       for (int q = tid; q < n1 * nrhs; q += nt) {
         const int r = q % n1, c = q / n1;
@@ -1341,7 +1346,6 @@ __global__ void __launch_bounds__(256) trsv_coop(const cx<T>* A, long long lda, 
         xs[r][c] = acc;
       }
       __syncthreads();
-      if (s + 2 < nb) stage(kb_of(s + 2), kb_of(s + 2), k1);
       __threadfence();
     }
     // rows beyond k1 (below it for L, above it for U), 4 threads per row
@@ -1414,7 +1418,7 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
       int dev = 0, nsm = 0, per = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      size_t dsm = sizeof(cx<T>) * 2 * bs * bs;
+      size_t dsm = sizeof(cx<T>) * 4 * bs * bs;
       allow_max_smem(trsv_coop<T, true>);
       allow_max_smem(trsv_coop<T, false>);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, dsm);
@@ -1728,7 +1732,7 @@ static gbem_status solve_chunk_n(const cx<T>* A, int N, int ld, const int* d_per
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  size_t dsm = sizeof(cx<T>) * 2 * bs * bs;
+  size_t dsm = sizeof(cx<T>) * 4 * bs * bs;
   allow_max_smem(trsv_coop<T, true>);
   allow_max_smem(trsv_coop<T, false>);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, dsm);
