@@ -283,6 +283,30 @@ gbem_status gbem_power_emt(gbem_geometry *g, double omega_re, double omega_im, c
                            const double *mu, int precision, int nrhs, const double *KN, int ldkn,
                            const double *rhs, int ldr, double *pscat, double *pext);
 
+/* ---- shape derivatives (adjoint) -------------------------------------------
+ * No reference counterpart: the reference differentiates rigid motions of
+ * whole surfaces only (GradM, dMdT of AssembleBEMMatrixBlock, libscuff.h:500-505).
+ * Vertices are numbered surface by surface (surface 0's first); grad holds
+ * 3 doubles per vertex and is overwritten.
+ *
+ * gbem_vertex_vjp_matrix: grad[3 v + c] = Re sum_r sum_ij conj(lam_ir)
+ * dM_ij/dV_vc x_jr for the full matrix of gbem_assemble at this frequency;
+ * lam, x: N x nrhs complex128 (host, column-major).  Far pairs are
+ * differentiated analytically; near and common-vertex pairs by central
+ * differences of their FP64 evaluation with displacement rel_step times the
+ * pair's larger panel radius (1e-4 keeps both truncation and rounding near
+ * 1e-9 of the derivative). */
+gbem_status gbem_vertex_vjp_matrix(gbem_geometry *g, double omega_re, double omega_im, const double *eps,
+                                   const double *mu, int nrhs, const double *lam, int ldl, const double *x,
+                                   int ldx, double rel_step, double *grad);
+/* grad[3 v + c] = Re sum_w sum_i conj(gb_iw) d b_iw/dV_vc for the plane-wave
+ * right-hand sides of gbem_rhs_planewave (E0: 6 doubles, nhat: 3 per wave). */
+gbem_status gbem_vertex_vjp_rhs_planewave(gbem_geometry *g, double omega_re, double omega_im, const double *eps,
+                                          const double *mu, int nwaves, const double *E0, const double *nhat,
+                                          const double *gb, int ldg, double *grad);
+/* total vertices over all surfaces */
+gbem_status gbem_geometry_num_vertices(const gbem_geometry *g, int *nv);
+
 /* ---- right-hand sides ----------------------------------------------------- */
 /* Plane-wave right-hand side (AssembleRHSVector.cc:145-255 with a PlaneWave
  * incident field, libs/libIncField/PlaneWave.cc): E0 (complex, 6 doubles),

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <new>
 #include <vector>
+#include "adjoint.cuh"
 #include "bem_math.cuh"
 #include "ffmath.cuh"
 #include "gbem_internal.h"
@@ -269,6 +270,9 @@ void free_geometry_device(Geometry* g) {
   }
   g->dblocks.clear();
   cudaFree(g->d_ffnode); cudaFree(g->d_ffgeo); cudaFree(g->ppv);
+  cudaFree(g->d_pvi); cudaFree(g->d_sbf); cudaFree(g->d_ssl);
+  g->d_pvi = g->d_sbf = nullptr;
+  g->d_ssl = nullptr;
   g->d_ffnode = g->d_ffgeo = nullptr;
   g->ppv = nullptr;
   g->ppv_bytes = 0;
@@ -1457,5 +1461,444 @@ gbem_status rhs_planewave_device(Geometry* g, double wr, double wi, const double
   }
   return GBEM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Adjoint contraction with the vertex derivatives of the matrix and of the
+// plane-wave right-hand side (no reference counterpart: the reference
+// differentiates rigid motions of whole surfaces only, GradM / dMdT).
+//   grad[3 v + c] = Re sum_r sum_ij conj(lam_ir) dM_ij/dV_vc x_jr
+// The matrix derivative is never formed: every panel pair adds its share to
+// the vertex gradients directly.
+//  vjp_far_kernel   far pairs (rRel > 4), one thread per pair: reverse-mode
+//                   derivative of the 6x6-rule integrals (adjoint.cuh), the
+//                   edge-length factors La Lb included.
+//  vjp_near_kernel  near and common-vertex pairs, one thread per (pair,
+//                   vertex, coordinate): central differences of the FP64
+//                   near-pair evaluation (static integrals recomputed for the
+//                   displaced vertices), contracted with the same weights.
+//  rhs_vjp_kernel   Re sum conj(g_i) db_i/dV for plane-wave right-hand sides.
+// ---------------------------------------------------------------------------
+struct VjpTables {
+  const double* pv;   // 9 per global panel: vertices in mesh order
+  const double* pc;   // 4 per global panel: centroid, radius
+  const int* pvi;     // 3 per global panel: global vertex indices
+  const int* sbf;     // 3 per global panel: basis function of the edge whose Q is vertex j (-1: none)
+  const double* ssl;  // 3 per global panel: +L on the edge's positive panel, -L on its negative one
+  const cx<double>* lam;
+  const cx<double>* x;
+  long long ldl, ldx;
+  int nrhs;
+  double* grad;       // 3 per global vertex
+};
+
+__device__ __forceinline__ cx<double> conj_mul(cx<double> a, cx<double> b) {
+  return mk(a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re);
+}
+
+// W[ch][3 ja + jb]: sum over the right-hand sides of conj(lam_i) x_j for the
+// entry (i, j) of the (Qa, Qb) edge pair, plus its mirror (j, i) when the
+// pair stands for both orders; channel 0 = (E, E), 1 = (E, H) + (H, E),
+// 2 = (H, H) (the (K, K), (K, N), (N, N) entries of SurfaceSurfaceInteractions.cc:205-327)
+__device__ void vjp_weights(const VjpTables& t, int gpa, int gpb, int bpe_a, int bpe_b, bool mirror, cx<double> W[3][9]) {
+  for (int ch = 0; ch < 3; ch++)
+    for (int m = 0; m < 9; m++) W[ch][m] = mk(0.0, 0.0);
+  for (int ja = 0; ja < 3; ja++) {
+    const int ia = t.sbf[3 * gpa + ja];
+    if (ia < 0) continue;
+    for (int jb = 0; jb < 3; jb++) {
+      const int ib = t.sbf[3 * gpb + jb];
+      if (ib < 0) continue;
+      for (int r = 0; r < t.nrhs; r++) {
+        const cx<double>* L = t.lam + (long long)r * t.ldl;
+        const cx<double>* X = t.x + (long long)r * t.ldx;
+        for (int al = 0; al < bpe_a; al++)
+          for (int bt = 0; bt < bpe_b; bt++) {
+            const int ch = (al == 0 && bt == 0) ? 0 : (al != bt ? 1 : 2);
+            cx<double> w = conj_mul(L[ia + al], X[ib + bt]);
+            if (mirror) w = w + conj_mul(L[ib + bt], X[ia + al]);
+            W[ch][3 * ja + jb] = W[ch][3 * ja + jb] + w;
+          }
+      }
+    }
+  }
+}
+
+struct VjpFarArgs {
+  VjpTables t;
+  int offa, offb, npa, npb, bpe_a, bpe_b, sym;
+};
+
+// grid (column panels / 128, row panels): one far pair per thread; the row
+// panel's gradient is reduced over each warp before its atomics
+__global__ void __launch_bounds__(128) vjp_far_kernel(VjpFarArgs a, RegionArgs ra) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gpa = a.offa + i, gpb = a.offb + j;
+  const VjpTables& t = a.t;
+  double gA[9], gB[9];
+  for (int q = 0; q < 9; q++) gA[q] = gB[q] = 0.0;
+  bool act = j < a.npb && !(a.sym && j <= i);
+  if (act) act = is_far(t.pc + 4 * (size_t)gpa, t.pc + 4 * (size_t)gpb, t.pc[4 * (size_t)gpa + 3], t.pc[4 * (size_t)gpb + 3]);
+  if (act) {
+    double Va[9], Vb[9], slA[3], slB[3];
+    for (int q = 0; q < 9; q++) { Va[q] = t.pv[9 * (size_t)gpa + q]; Vb[q] = t.pv[9 * (size_t)gpb + q]; }
+    for (int q = 0; q < 3; q++) {
+      slA[q] = t.sbf[3 * gpa + q] >= 0 ? t.ssl[3 * gpa + q] : 0.0;
+      slB[q] = t.sbf[3 * gpb + q] >= 0 ? t.ssl[3 * gpb + q] : 0.0;
+    }
+    cx<double> W[3][9];
+    vjp_weights(t, gpa, gpb, a.bpe_a, a.bpe_b, true, W);
+    double ErT[3] = {0.0, 0.0, 0.0}, EcT[3] = {0.0, 0.0, 0.0};
+    for (int r = 0; r < ra.nreg; r++) {
+      const cx<double> k = ra.k[r];
+      if (k.re == 0.0 && k.im == 0.0) continue;
+      cx<double> C0[9], C1[9];
+      for (int m = 0; m < 9; m++) {
+        const double fac = slA[m / 3] * slB[m % 3];
+        C0[m] = fac * (ra.pf1[r] * W[0][m] + ra.pf3[r] * W[2][m]);
+        C1[m] = fac * (ra.pfc[r] * W[1][m]);
+      }
+      double Er[3], Ec[3];
+      far_pair_vjp(Va, Vb, k, C0, C1, c_lo64, 6, gA, gB, Er, Ec);
+      for (int q = 0; q < 3; q++) { ErT[q] += Er[q]; EcT[q] += Ec[q]; }
+    }
+    // the coefficients hold La Lb: d/dL = (slot sum)/L, dL/dV along the edge
+    for (int q = 0; q < 3; q++) {
+      const int q1 = (q + 1) % 3, q2 = (q + 2) % 3;
+      if (slA[q] != 0.0) {
+        const double s = ErT[q] / (slA[q] * slA[q]);
+        for (int c = 0; c < 3; c++) {
+          const double d = Va[3 * q1 + c] - Va[3 * q2 + c];
+          gA[3 * q1 + c] += s * d; gA[3 * q2 + c] -= s * d;
+        }
+      }
+      if (slB[q] != 0.0) {
+        const double s = EcT[q] / (slB[q] * slB[q]);
+        for (int c = 0; c < 3; c++) {
+          const double d = Vb[3 * q1 + c] - Vb[3 * q2 + c];
+          gB[3 * q1 + c] += s * d; gB[3 * q2 + c] -= s * d;
+        }
+      }
+    }
+    for (int q = 0; q < 9; q++)
+      if (gB[q] != 0.0) atomicAdd(&t.grad[3 * (size_t)t.pvi[3 * gpb + q / 3] + q % 3], gB[q]);
+  }
+  for (int q = 0; q < 9; q++) {
+    double v = gA[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffff, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&t.grad[3 * (size_t)t.pvi[3 * gpa + q / 3] + q % 3], v);
+  }
+}
+
+// Re sum over regions and (Qa, Qb) of the pair's weighted values at the given
+// vertex positions -- the arithmetic of self_kernel, near_kernel and
+// td_touch_kernel for one pair in one thread, with the edge lengths taken
+// from the positions
+__device__ double near_pair_energy(const DevNear& d, const double* Va, const double* Vb, const double* sgA,
+                                   const double* sgB, const RegionArgs& ra, const cx<double> W[3][9]) {
+  const bool self = d.pa == d.pb;
+  double fac[9];
+  for (int ja = 0; ja < 3; ja++)
+    for (int jb = 0; jb < 3; jb++) {
+      double La = 0.0, Lb = 0.0;
+      for (int c = 0; c < 3; c++) {
+        const double ea = Va[3 * ((ja + 1) % 3) + c] - Va[3 * ((ja + 2) % 3) + c];
+        const double eb = Vb[3 * ((jb + 1) % 3) + c] - Vb[3 * ((jb + 2) % 3) + c];
+        La += ea * ea; Lb += eb * eb;
+      }
+      fac[3 * ja + jb] = sgA[ja] * sgB[jb] * sqrt(La) * sqrt(Lb);
+    }
+  PairGeom<double> g;
+  for (int c = 0; c < 3; c++) {
+    g.D0[c] = Va[c] - Vb[c];
+    g.Aa[c] = Va[3 + c] - Va[c]; g.Ba[c] = Va[6 + c] - Va[c];
+    g.Ab[c] = Vb[3 + c] - Vb[c]; g.Bb[c] = Vb[6 + c] - Vb[c];
+  }
+  Fippi F;
+  bool haveF = false;
+  double E = 0.0;
+  for (int r = 0; r < ra.nreg; r++) {
+    const cx<double> k = ra.k[r];
+    if (k.re == 0.0 && k.im == 0.0) continue;
+    const cx<double> m4ok2 = cdiv(mk(-4.0, 0.0), k * k);
+    cx<double> H0[9], H1[9];
+    if (self) {
+      cx<double> MG[9], MP[9];
+      self_moments(Va, k, c_gx16, c_gw16, NT_SELF, MG, 0, 1);
+      for (int m = 0; m < 9; m++) MP[m] = mk(0.0, 0.0);
+      for (int m = 0; m < 9; m++) {
+        double c[9], dd[9];
+        combo_coeffs(Va, Va, m / 3, m % 3, c, dd);
+        combine(MG, MP, c, dd, m4ok2, &H0[m], &H1[m]);
+        H1[m] = mk(0.0, 0.0);
+      }
+    } else {
+      const bool sw = hypot(k.re * d.rmax, k.im * d.rmax) > M_PI;
+      cx<double> MG[9], MP[9];
+      bool desing = false, td = false;
+      cx<double> T[10];
+      if (!sw) {
+        if (!haveF) {
+          if (d.ncv == 0) fippi_far(Va, Vb, c_gx12, c_gw12, N_FIP, &F);
+          else fippi_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, c_gx12, c_gw12, N_FIP, &F);
+          haveF = true;
+        }
+        pair_moments<double, 1>(g, k, c_lo64, 6, MG, MP);
+        add_taylor_terms(F, k, MG, MP);
+        desing = true;
+      } else if (d.ncv == 0) {
+        pair_moments<double, 0>(g, k, c_ho, HO_N * HO_N, MG, MP);
+      } else {
+        td_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, k, c_gx12, c_gw12, N_TD, 0, 1, MG, T);
+        for (int m = 0; m < 9; m++) MP[m] = mk(0.0, 0.0);
+        td = true;
+      }
+      VecMoments<double> vm;
+      vec_moments(g, MG, MP, &vm);
+      for (int m = 0; m < 9; m++) {
+        vec_combine(g, vm, m / 3, m % 3, m4ok2, &H0[m], &H1[m]);
+        if (desing) H1[m] = H1[m] + mk(-0.079577471545947667884 * htimes_rm3(F, Va, Vb, m / 3, m % 3), 0.0);
+        if (td) H1[m] = td_h1(Va, Vb, T, m / 3, m % 3);
+      }
+    }
+    for (int m = 0; m < 9; m++) {
+      const cx<double> v = ra.pf1[r] * (W[0][m] * H0[m]) + ra.pfc[r] * (W[1][m] * H1[m]) + ra.pf3[r] * (W[2][m] * H0[m]);
+      E += fac[m] * v.re;
+    }
+  }
+  return E;
+}
+
+struct VjpNearArgs {
+  VjpTables t;
+  const DevNear* near;
+  int nnear, bpe_a, bpe_b;
+  double rel_step;  // displacement = rel_step * the pair's larger panel radius
+};
+
+__global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs ra) {
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long pair = tid / 18;
+  if (pair >= a.nnear) return;
+  const int dir = (int)(tid % 18), v = dir / 3, c = dir % 3;
+  const VjpTables& t = a.t;
+  const DevNear d = a.near[pair];
+  const bool self = d.pa == d.pb;
+  if (self && v >= 3) return;
+  const int gv = v < 3 ? t.pvi[3 * d.pa + v] : t.pvi[3 * d.pb + v - 3];
+  if (v >= 3)
+    for (int q = 0; q < 3; q++)
+      if (t.pvi[3 * d.pa + q] == gv) return;  // a shared vertex moves with panel a's slot
+  double sgA[3], sgB[3];
+  for (int q = 0; q < 3; q++) {
+    sgA[q] = t.sbf[3 * d.pa + q] >= 0 ? (t.ssl[3 * d.pa + q] > 0.0 ? 1.0 : -1.0) : 0.0;
+    sgB[q] = t.sbf[3 * d.pb + q] >= 0 ? (t.ssl[3 * d.pb + q] > 0.0 ? 1.0 : -1.0) : 0.0;
+  }
+  cx<double> W[3][9];
+  vjp_weights(t, d.pa, d.pb, a.bpe_a, a.bpe_b, !self, W);
+  const double h = a.rel_step * d.rmax;
+  double E[2];
+  for (int s = 0; s < 2; s++) {
+    double Va[9], Vb[9];
+    for (int q = 0; q < 9; q++) { Va[q] = t.pv[9 * (size_t)d.pa + q]; Vb[q] = t.pv[9 * (size_t)d.pb + q]; }
+    const double dv = s == 0 ? h : -h;
+    for (int q = 0; q < 3; q++) {
+      if (t.pvi[3 * d.pa + q] == gv) Va[3 * q + c] += dv;
+      if (t.pvi[3 * d.pb + q] == gv) Vb[3 * q + c] += dv;
+    }
+    E[s] = near_pair_energy(d, Va, Vb, sgA, sgB, ra, W);
+  }
+  atomicAdd(&t.grad[3 * (size_t)gv + c], (E[0] - E[1]) / (2.0 * h));
+}
+
+struct RhsVjpArgs {
+  const double* V;  // surface vertices
+  const int* E;     // 8 ints per edge
+  const double* elen;
+  int ne, bf_offset, pec, sign, voff, nw;
+  cx<double> k, Z;
+  const double* E0;  // 6 per wave (complex)
+  const double* nh;  // 3 per wave
+  const cx<double>* gb;
+  long long ldg;
+  double* grad;
+};
+
+// one thread per edge: the gradient of Re sum_w conj(g_iw) b_iw (rhs_kernel's
+// integrals) with respect to the edge's four vertices
+__global__ void rhs_vjp_kernel(RhsVjpArgs a) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.ne) return;
+  const int* ed = a.E + 8 * e;
+  const double* V1 = a.V + 3 * ed[0];
+  const double* V2 = a.V + 3 * ed[1];
+  const double L = a.elen[e];
+  const double ZVAC = 376.73031346177;
+  const cx<double> ik = mk(-a.k.im, a.k.re);
+  double g1[3] = {0.0, 0.0, 0.0}, g2[3] = {0.0, 0.0, 0.0};
+  for (int side = 0; side < 2; side++) {
+    const int iq = side == 0 ? ed[2] : ed[3];
+    if (iq < 0) continue;
+    const double ss = side == 0 ? 1.0 : -1.0;
+    const double* Q = a.V + 3 * iq;
+    double A[3], B[3], gq[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < 3; i++) { A[i] = V1[i] - Q[i]; B[i] = V2[i] - Q[i]; }
+    double Ire = 0.0;
+    for (int w = 0; w < a.nw; w++) {
+      const int i0 = a.bf_offset + (a.pec ? e : 2 * e);
+      const cx<double> gE = a.gb[i0 + (long long)w * a.ldg];
+      const cx<double> gH = a.pec ? mk(0.0, 0.0) : a.gb[i0 + 1 + (long long)w * a.ldg];
+      const double* nh = a.nh + 3 * w;
+      cx<double> E0[3], P[3];
+      for (int i = 0; i < 3; i++) E0[i] = mk(a.E0[6 * w + 2 * i], a.E0[6 * w + 2 * i + 1]);
+      // P = (sign/ZVAC) conj(gE) E0 + sign conj(gH) (nh x E0)/Z
+      const cx<double> cE = (a.sign / ZVAC) * mk(gE.re, -gE.im);
+      const cx<double> cH = cdiv((double)a.sign * mk(gH.re, -gH.im), a.Z);
+      cx<double> nxE[3];
+      rcvcross(nh, E0, nxE);
+      for (int i = 0; i < 3; i++) P[i] = cE * E0[i] + cH * nxE[i];
+      for (int q = 0; q < HO_N * HO_N; q++) {
+        const double u = c_ho[3 * q], v = c_ho[3 * q + 1], wq = c_ho[3 * q + 2];
+        double X[3], F[3];
+        for (int i = 0; i < 3; i++) { F[i] = u * A[i] + v * B[i]; X[i] = Q[i] + F[i]; }
+        const double ph = nh[0] * X[0] + nh[1] * X[1] + nh[2] * X[2];
+        const cx<double> ex = wq * cexpo(mk(-a.k.im * ph, a.k.re * ph));
+        const cx<double> FP = F[0] * P[0] + F[1] * P[1] + F[2] * P[2];
+        Ire += (FP * ex).re;
+        const cx<double> t = FP * ik;
+        for (int i = 0; i < 3; i++) {
+          const cx<double> dX = (P[i] + nh[i] * t) * ex;  // d(F.P e^{ik nh.X})/dX
+          const double dr = ss * L * dX.re;
+          g1[i] += u * dr; g2[i] += v * dr;
+          gq[i] += (1.0 - u - v) * dr - ss * L * (P[i] * ex).re;
+        }
+      }
+    }
+    for (int i = 0; i < 3; i++) {
+      const double dl = ss * Ire * (V1[i] - V2[i]) / L;
+      g1[i] += dl; g2[i] -= dl;
+      atomicAdd(&a.grad[3 * (size_t)(a.voff + iq) + i], gq[i]);
+    }
+  }
+  for (int i = 0; i < 3; i++) {
+    atomicAdd(&a.grad[3 * (size_t)(a.voff + ed[0]) + i], g1[i]);
+    atomicAdd(&a.grad[3 * (size_t)(a.voff + ed[1]) + i], g2[i]);
+  }
+}
+
+// per-panel tables of the adjoint (built on first use)
+static gbem_status upload_vjp_tables(Geometry* g) {
+  if (g->d_pvi) return GBEM_OK;
+  const size_t np = (size_t)g->np_total;
+  std::vector<int> pvi(3 * np), sbf(3 * np, -1);
+  std::vector<double> ssl(3 * np, 0.0);
+  int voff = 0;
+  for (const Surface& S : g->S) {
+    for (int p = 0; p < S.np; p++) {
+      const size_t gp = S.panel_offset + p;
+      for (int j = 0; j < 3; j++) {
+        pvi[3 * gp + j] = voff + S.PV[3 * p + j];
+        const int e = S.he_edge[3 * p + j];
+        if (e < 0) continue;
+        sbf[3 * gp + j] = S.bf_offset + (S.pec ? 1 : 2) * e;
+        ssl[3 * gp + j] = (S.he_side[3 * p + j] == 0 ? 1.0 : -1.0) * S.elen[e];
+      }
+    }
+    voff += S.nv;
+  }
+  cudaError_t e = dupload(&g->d_pvi, pvi.data(), pvi.size());
+  if (e == cudaSuccess) e = dupload(&g->d_sbf, sbf.data(), sbf.size());
+  if (e == cudaSuccess) e = dupload(&g->d_ssl, ssl.data(), ssl.size());
+  return cuda_status(e, "adjoint tables");
+}
+
+static int total_vertices(const Geometry* g) {
+  int n = 0;
+  for (const Surface& S : g->S) n += S.nv;
+  return n;
+}
+
+gbem_status vertex_vjp_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int nrhs,
+                              const void* d_lam, int ldl, const void* d_x, int ldx, double* d_grad, double rel_step,
+                              cudaStream_t s) {
+  gbem_status st = upload_geometry(g);
+  if (st == GBEM_OK) st = upload_vjp_tables(g);
+  if (st != GBEM_OK) return st;
+  VjpTables t;
+  t.pv = g->d_pv; t.pc = g->d_pc; t.pvi = g->d_pvi; t.sbf = g->d_sbf; t.ssl = g->d_ssl;
+  t.lam = (const cx<double>*)d_lam; t.x = (const cx<double>*)d_x; t.ldl = ldl; t.ldx = ldx; t.nrhs = nrhs;
+  t.grad = d_grad;
+  cudaError_t e = cudaSuccess;
+  for (size_t bi = 0; bi < g->blocks.size() && e == cudaSuccess; bi++) {
+    const Block& b = g->blocks[bi];
+    const DevBlock* db = g->dblocks[bi];
+    if (b.nreg == 0) continue;
+    const Surface& A = g->S[b.sa];
+    const Surface& B = g->S[b.sb];
+    const RegionArgs ra = region_args(b, wr, wi, eps, mu);
+    VjpFarArgs fa;
+    fa.t = t; fa.offa = A.panel_offset; fa.offb = B.panel_offset; fa.npa = A.np; fa.npb = B.np;
+    fa.bpe_a = A.pec ? 1 : 2; fa.bpe_b = B.pec ? 1 : 2; fa.sym = b.sym ? 1 : 0;
+    if (A.np && B.np) {
+      vjp_far_kernel<<<dim3((B.np + 127) / 128, A.np), 128, 0, s>>>(fa, ra);
+      stats_launch(ST_OTHER);
+    }
+    if (db->nnear) {
+      VjpNearArgs na;
+      na.t = t; na.near = db->near; na.nnear = db->nnear; na.bpe_a = fa.bpe_a; na.bpe_b = fa.bpe_b;
+      na.rel_step = rel_step;
+      const long long n = 18LL * db->nnear;
+      vjp_near_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(na, ra);
+      stats_launch(ST_OTHER);
+    }
+    e = cudaGetLastError();
+  }
+  return cuda_status(e, "vertex adjoint");
+}
+
+gbem_status rhs_vjp_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int nw,
+                           const double* E0, const double* nh, const void* d_gb, int ldg, double* d_grad, cudaStream_t s) {
+  gbem_status st = upload_geometry(g);
+  if (st != GBEM_OK) return st;
+  double *dE0 = nullptr, *dnh = nullptr;
+  cudaError_t e = dupload(&dE0, E0, 6 * (size_t)nw);
+  if (e == cudaSuccess) e = dupload(&dnh, nh, 3 * (size_t)nw);
+  int voff = 0;
+  for (const Surface& S : g->S) {
+    const int vo = voff;
+    voff += S.nv;
+    if (e != cudaSuccess) break;
+    int sign;
+    if (S.reg_ext == 0) sign = -1;
+    else if (S.reg_int == 0) sign = 1;
+    else continue;
+    if (!S.ne) continue;
+    double *dV = nullptr, *dL = nullptr;
+    int* dE = nullptr;
+    e = dupload(&dV, S.V.data(), S.V.size());
+    if (e == cudaSuccess) e = dupload(&dE, S.E.data(), S.E.size());
+    if (e == cudaSuccess) e = dupload(&dL, S.elen.data(), S.elen.size());
+    if (e == cudaSuccess) {
+      RhsVjpArgs a;
+      a.V = dV; a.E = dE; a.elen = dL; a.ne = S.ne; a.bf_offset = S.bf_offset; a.pec = S.pec ? 1 : 0; a.sign = sign;
+      a.voff = vo; a.nw = nw;
+      cx<double> ep = cxd(eps[0], eps[1]), m = cxd(mu[0], mu[1]), em = ep * m;
+      double rr = std::sqrt(std::hypot(em.re, em.im)), th = 0.5 * std::atan2(em.im, em.re);
+      a.k = cxd(rr * std::cos(th), rr * std::sin(th)) * cxd(wr, wi);
+      cx<double> q = cdiv(m, ep);
+      double rq = std::sqrt(std::hypot(q.re, q.im)), tq = 0.5 * std::atan2(q.im, q.re);
+      a.Z = 376.73031346177 * cxd(rq * std::cos(tq), rq * std::sin(tq));
+      a.E0 = dE0; a.nh = dnh; a.gb = (const cx<double>*)d_gb; a.ldg = ldg; a.grad = d_grad;
+      rhs_vjp_kernel<<<(S.ne + 127) / 128, 128, 0, s>>>(a);
+      stats_launch(ST_OTHER);
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    cudaFree(dV); cudaFree(dE); cudaFree(dL);
+  }
+  cudaFree(dE0); cudaFree(dnh);
+  return cuda_status(e, "rhs adjoint");
+}
+
+int geometry_total_vertices(const Geometry* g) { return total_vertices(g); }
 
 }  // namespace gbem

@@ -470,6 +470,73 @@ gbem_status gbem_power_emt(gbem_geometry* g, double omega_re, double omega_im, c
   return GBEM_OK;
 }
 
+gbem_status gbem_vertex_vjp_matrix(gbem_geometry* g, double omega_re, double omega_im, const double* eps,
+                                   const double* mu, int nrhs, const double* lam, int ldl, const double* x, int ldx,
+                                   double rel_step, double* grad) {
+  if (!g || !eps || !mu || !lam || !x || !grad || nrhs <= 0 || ldl < g->N || ldx < g->N || !(rel_step > 0.0)) {
+    set_error("gbem_vertex_vjp_matrix: bad arguments");
+    return GBEM_EINVAL;
+  }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  cudaStream_t s = g->stream;
+  const int N = g->N, nv = geometry_total_vertices(g);
+  void *dL = nullptr, *dX = nullptr, *dG = nullptr;
+  cudaError_t e = cudaMallocAsync(&dL, (size_t)N * nrhs * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dX, (size_t)N * nrhs * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dG, sizeof(double) * 3 * (size_t)std::max(nv, 1), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dL, (size_t)N * 16, lam, (size_t)ldl * 16, (size_t)N * 16, nrhs, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dX, (size_t)N * 16, x, (size_t)ldx * 16, (size_t)N * 16, nrhs, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dG, 0, sizeof(double) * 3 * (size_t)nv, s);
+  st = cuda_status(e, "gbem_vertex_vjp_matrix setup");
+  if (st == GBEM_OK) st = vertex_vjp_device(g, omega_re, omega_im, eps, mu, nrhs, dL, N, dX, N, (double*)dG, rel_step, s);
+  if (st == GBEM_OK) {
+    e = cudaMemcpyAsync(grad, dG, sizeof(double) * 3 * (size_t)nv, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    st = cuda_status(e, "gbem_vertex_vjp_matrix");
+  }
+  cudaFreeAsync(dL, s); cudaFreeAsync(dX, s); cudaFreeAsync(dG, s);
+  cudaStreamSynchronize(s);
+  return st;
+}
+
+gbem_status gbem_vertex_vjp_rhs_planewave(gbem_geometry* g, double omega_re, double omega_im, const double* eps,
+                                          const double* mu, int nwaves, const double* E0, const double* nhat,
+                                          const double* gb, int ldg, double* grad) {
+  if (!g || !eps || !mu || !E0 || !nhat || !gb || !grad || nwaves <= 0 || ldg < g->N) {
+    set_error("gbem_vertex_vjp_rhs_planewave: bad arguments");
+    return GBEM_EINVAL;
+  }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  cudaStream_t s = g->stream;
+  const int N = g->N, nv = geometry_total_vertices(g);
+  void *dB = nullptr, *dG = nullptr;
+  cudaError_t e = cudaMallocAsync(&dB, (size_t)N * nwaves * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dG, sizeof(double) * 3 * (size_t)std::max(nv, 1), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dB, (size_t)N * 16, gb, (size_t)ldg * 16, (size_t)N * 16, nwaves, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dG, 0, sizeof(double) * 3 * (size_t)nv, s);
+  st = cuda_status(e, "gbem_vertex_vjp_rhs_planewave setup");
+  if (st == GBEM_OK) st = rhs_vjp_device(g, omega_re, omega_im, eps, mu, nwaves, E0, nhat, dB, N, (double*)dG, s);
+  if (st == GBEM_OK) {
+    e = cudaMemcpyAsync(grad, dG, sizeof(double) * 3 * (size_t)nv, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    st = cuda_status(e, "gbem_vertex_vjp_rhs_planewave");
+  }
+  cudaFreeAsync(dB, s); cudaFreeAsync(dG, s);
+  cudaStreamSynchronize(s);
+  return st;
+}
+
+gbem_status gbem_geometry_num_vertices(const gbem_geometry* g, int* nv) {
+  if (!g || !nv) { set_error("gbem_geometry_num_vertices: NULL argument"); return GBEM_EINVAL; }
+  *nv = geometry_total_vertices(g);
+  return GBEM_OK;
+}
+
 gbem_status gbem_assemble_block_gradient(gbem_geometry* g, int nsa, int nsb, double omega_re, double omega_im,
                                          const double* eps, const double* mu, void* gx, void* gy, void* gz, int ld,
                                          int row0, int col0, int dtype) {

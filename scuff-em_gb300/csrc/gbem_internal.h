@@ -97,6 +97,10 @@ struct Geometry {
   float* d_ffgeo = nullptr;   // per global panel: V0 - ff_origin, V1 - V0, V2 - V0 as float-float (18 floats)
   void* ppv = nullptr;        // pair-value scratch of the mixed far field
   size_t ppv_bytes = 0;
+  // adjoint tables, per global panel (built on first use)
+  int* d_pvi = nullptr;       // 3: global vertex indices
+  int* d_sbf = nullptr;       // 3: basis function of the edge at each vertex slot, -1 if none
+  double* d_ssl = nullptr;    // 3: +-edge length (sign of the panel's side)
   // cached buffers of the mixed-precision solve
   void* mixedM = nullptr;
   void* mixedF = nullptr;
@@ -134,6 +138,15 @@ gbem_status assemble_gradient_device(Geometry* g, double wr, double wi, const do
                                      int nta = 0, const double* gamma = nullptr, void* const* outT = nullptr);
 gbem_status upload_geometry(Geometry* g);
 void free_geometry_device(Geometry* g);
+// adjoint contractions (device arrays, complex128 column-major): grad (3 per
+// vertex, surfaces in order) += Re sum conj(lam) dM/dV x, and
+// += Re sum conj(gb) db/dV for nw plane waves (E0: 6 doubles, nh: 3 per wave)
+gbem_status vertex_vjp_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int nrhs,
+                              const void* d_lam, int ldl, const void* d_x, int ldx, double* d_grad, double rel_step,
+                              cudaStream_t s);
+gbem_status rhs_vjp_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int nw,
+                           const double* E0, const double* nh, const void* d_gb, int ldg, double* d_grad, cudaStream_t s);
+int geometry_total_vertices(const Geometry* g);
 
 // lu.cu
 gbem_status lu_factor_device(void* dA, int N, int ld, int dtype, int* d_ipiv, int* h_info, cudaStream_t s,

@@ -27,7 +27,8 @@ EXPORTS = [
     "gbem_lu_solve_noalloc", "gbem_assemble_block", "gbem_assemble_block_host",
     "gbem_assemble_block_gradient", "gbem_assemble_block_gradient_host", "gbem_power_emt",
     "gbem_lu_trace", "gbem_lu_trace_host", "gbem_assemble_block_dmdt", "gbem_assemble_block_dmdt_host",
-    "gbem_solve_mixed_batch",
+    "gbem_solve_mixed_batch", "gbem_vertex_vjp_matrix", "gbem_vertex_vjp_rhs_planewave",
+    "gbem_geometry_num_vertices",
 ]
 
 
@@ -86,6 +87,9 @@ def lib():
             "gbem_assemble_block_dmdt": ([P, I, I, D, D, P, P, I, P, P, I, I, I, I], I),
             "gbem_assemble_block_dmdt_host": ([P, I, I, D, D, P, P, I, P, P, I, I, I, I], I),
             "gbem_lu_trace_host": ([P, P, I, I, P], I),
+            "gbem_vertex_vjp_matrix": ([P, D, D, P, P, I, P, I, P, I, D, P], I),
+            "gbem_vertex_vjp_rhs_planewave": ([P, D, D, P, P, I, P, P, P, I, P], I),
+            "gbem_geometry_num_vertices": ([P, P], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -1,0 +1,105 @@
+"""Shape derivatives through PyTorch autograd.
+
+``scatter(V, topology, Omega, waves)`` solves the plane-wave scattering
+problem M(V) x = b(V) for the vertex positions V (a float64 tensor, all
+surfaces' vertices stacked) and returns the surface currents x and the
+right-hand sides b (N x nwaves, complex128) as differentiable functions of V.
+Any real loss built from x and b (``extinction_power`` below, for one)
+back-propagates to V through one adjoint solve,
+
+    lam = M^-H dL/dx,    dL/dV = -Re lam^H (dM/dV) x + Re (lam + dL/db)^H (db/dV),
+
+whose two contractions run on the GPU (``RWGGeometry.VertexVJP`` and
+``RWGGeometry.RHSVertexVJP``) without forming dM/dV.  The matrix is complex
+symmetric (M^T = M, AssembleBEMMatrix.cc:753-758), so M^-H g = conj(M^-1
+conj(g)) reuses the forward factorisation.
+
+The reference has no shape derivative: its GradM/dMdT blocks differentiate
+rigid motions of whole surfaces (libscuff.h:500-505).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .api import ZVAC, RWGGeometry
+
+
+class MeshTopology:
+    """The fixed part of a geometry: per surface its panels (np x 3, 0-based
+    vertex indices) and material (None = PEC); vertex positions come later."""
+
+    def __init__(self, surfaces, exterior=None, device=0):
+        self.surfaces = [{"P": np.asarray(s["P"], dtype=np.int32), "material": s.get("material"),
+                          "nv": int(s["nv"])} for s in surfaces]
+        self.exterior = exterior
+        self.device = device
+
+    @classmethod
+    def from_surfaces(cls, surfaces, exterior=None, device=0):
+        """From RWGGeometry-style dicts (V, P, material); returns (topology, V0)."""
+        topo = cls([{"P": s["P"], "material": s.get("material"), "nv": len(s["V"])} for s in surfaces],
+                   exterior, device)
+        return topo, np.concatenate([np.asarray(s["V"], dtype=np.float64) for s in surfaces])
+
+    @property
+    def num_vertices(self):
+        return sum(s["nv"] for s in self.surfaces)
+
+    def geometry(self, V):
+        V = np.asarray(V, dtype=np.float64).reshape(-1, 3)
+        if V.shape[0] != self.num_vertices:
+            raise ValueError("V has %d vertices, the topology %d" % (V.shape[0], self.num_vertices))
+        out, off = [], 0
+        for s in self.surfaces:
+            out.append({"V": V[off:off + s["nv"]], "P": s["P"], "material": s["material"]})
+            off += s["nv"]
+        return RWGGeometry(out, exterior=self.exterior, device=self.device)
+
+
+class _Scatter(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, V, topology, Omega, waves, precision, rel_step):
+        geo = topology.geometry(V.detach().cpu().numpy())
+        b = np.stack([geo.AssembleRHSVector(Omega, E0, nh) for E0, nh in waves], axis=1)
+        if precision == "fp64":
+            M = geo.AssembleBEMMatrix(Omega)
+            if M.LUFactorize() != 0:
+                raise RuntimeError("singular BEM matrix")
+            x = M.LUSolve(b)
+            solve = M.LUSolve
+        elif precision == "mixed":
+            x = geo.solve_mixed(Omega, b)[0]
+            solve = lambda B: geo.solve_mixed(Omega, B)[0]  # noqa: E731
+        else:
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        ctx.geo, ctx.solve, ctx.Omega, ctx.waves, ctx.rel_step = geo, solve, Omega, waves, rel_step
+        ctx.x = x
+        ctx.vdevice, ctx.vdtype = V.device, V.dtype
+        return torch.from_numpy(np.ascontiguousarray(x)), torch.from_numpy(np.ascontiguousarray(b))
+
+    @staticmethod
+    def backward(ctx, gx, gb):
+        x = ctx.x
+        gx = np.zeros_like(x) if gx is None else gx.detach().resolve_conj().cpu().numpy().astype(np.complex128)
+        gb = np.zeros_like(x) if gb is None else gb.detach().resolve_conj().cpu().numpy().astype(np.complex128)
+        # lam = M^-H gx = conj(M^-1 conj(gx))  (M complex symmetric)
+        lam = np.conj(ctx.solve(np.conj(gx)))
+        g = -ctx.geo.VertexVJP(ctx.Omega, lam, x, rel_step=ctx.rel_step)
+        g += ctx.geo.RHSVertexVJP(ctx.Omega, ctx.waves, lam + gb)
+        return torch.from_numpy(g).to(device=ctx.vdevice, dtype=ctx.vdtype), None, None, None, None, None
+
+
+def scatter(V, topology, Omega, waves, precision="fp64", rel_step=1e-4):
+    """(x, b) for plane waves [(E0, nHat), ...] incident from the exterior
+    region, differentiable with respect to the vertex tensor V (nv x 3)."""
+    return _Scatter.apply(V, topology, complex(Omega), [(tuple(E0), tuple(nh)) for E0, nh in waves], precision,
+                          rel_step)
+
+
+def extinction_power(x, b, types):
+    """Extinction power per wave, -1/2 ZVAC sum_i s_i Re(conj(x_i) b_i) with
+    s_i = -1 on magnetic (N) rows (the reference's EMT extinction,
+    EMTPFT.cc:305-392); ``types`` from ``RWGGeometry.basis_types()``."""
+    s = torch.from_numpy(np.where(np.asarray(types) == 1, -1.0, 1.0)).to(x.device)
+    return -0.5 * ZVAC * (s[:, None] * (torch.conj(x) * b).real).sum(dim=0)

@@ -311,6 +311,59 @@ class RWGGeometry:
                                        e0.ctypes.data, nh.ctypes.data, out.ctypes.data))
         return out
 
+    @property
+    def NumVertices(self):
+        n = ctypes.c_int()
+        check(lib().gbem_geometry_num_vertices(self._h, ctypes.byref(n)))
+        return n.value
+
+    def VertexVJP(self, Omega, lam, x, rel_step=1e-4):
+        """Re sum conj(lam) (dM/dV) x over the columns of lam and x (N x nrhs):
+        the adjoint contraction with the vertex derivatives of the full BEM
+        matrix, without forming them.  Returns (NumVertices, 3), surfaces'
+        vertices stacked in order.  Near and common-vertex pairs take central
+        differences with displacement rel_step times the pair's panel radius."""
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        lam = np.asfortranarray(np.asarray(lam, dtype=np.complex128).reshape(self.TotalBFs, -1))
+        x = np.asfortranarray(np.asarray(x, dtype=np.complex128).reshape(self.TotalBFs, -1))
+        if lam.shape != x.shape:
+            raise ValueError("lam and x need the same shape")
+        g = np.zeros((self.NumVertices, 3))
+        check(lib().gbem_vertex_vjp_matrix(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data,
+                                           x.shape[1], lam.ctypes.data, self.TotalBFs, x.ctypes.data, self.TotalBFs,
+                                           float(rel_step), g.ctypes.data))
+        return g
+
+    def RHSVertexVJP(self, Omega, waves, gb):
+        """Re sum conj(gb) (db/dV) for plane waves [(E0, nHat), ...] (the
+        columns of gb, N x len(waves)).  Returns (NumVertices, 3)."""
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        gb = np.asfortranarray(np.asarray(gb, dtype=np.complex128).reshape(self.TotalBFs, -1))
+        if gb.shape[1] != len(waves):
+            raise ValueError("one column of gb per wave")
+        e0 = np.array([[[complex(c).real, complex(c).imag] for c in E0] for E0, _ in waves], dtype=np.float64).ravel()
+        nh = np.array([np.asarray(n, dtype=np.float64) for _, n in waves]).ravel()
+        g = np.zeros((self.NumVertices, 3))
+        check(lib().gbem_vertex_vjp_rhs_planewave(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data,
+                                                  len(waves), e0.ctypes.data, nh.ctypes.data, gb.ctypes.data,
+                                                  self.TotalBFs, g.ctypes.data))
+        return g
+
+    def basis_types(self):
+        """Per basis function: 0 for an electric (K) current, 1 for a magnetic (N) one."""
+        t = np.zeros(self.TotalBFs, dtype=np.int8)
+        off = 0
+        for i, s in enumerate(self.surfaces):
+            ne = self.edges(i)[0].shape[0]
+            if s["pec"]:
+                off += ne
+            else:
+                t[off + 1:off + 2 * ne:2] = 1
+                off += 2 * ne
+        return t
+
     def solve_mixed(self, Omega, B, tol=1e-10, max_iter=10):
         """Mixed-precision solve (FP32 far field, complex-FP32 LU, FP64
         refinement).  Returns (X, iterations, relative residual)."""
