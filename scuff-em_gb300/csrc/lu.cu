@@ -10,7 +10,7 @@
 //                 are exchanged through double-buffered global stashes, so
 //                 row swaps need no second barrier).  Pivots maximise
 //                 |Re|+|Im| in FP64 (LAPACK's IZAMAX); ties go to the lowest row.
-//   laswp_kernel  applies the panel's row interchanges outside the panel.
+//   swap_compose / swap_apply  apply the panel's row interchanges outside the panel.
 //   trsm_kernel   U12 = L11^{-1} A12 (unit lower triangle).
 //   trailing update A22 -= L21 U12: gemm_simt<T> for FP64, the tensor-core
 //                 split-BF16 GEMM (gemm_tc.cu) for the complex-FP32 form.
@@ -591,15 +591,77 @@ __global__ void __launch_bounds__(NT, 1) leaf_kernel_reg(LeafArgs a) {
   }
 }
 
-// row interchanges of columns [cb, ce) for pivots of rows [r0, r1)
+// Row interchanges outside a panel, in two steps.  swap_compose (one CTA)
+// folds the panel's interchanges (rows [r0, r1) with ipiv, LAPACK order) into
+// the list of rows whose content moves: mv[2e] = destination row, mv[2e+1] =
+// the row it takes its content from; rows beyond the panel are tracked in a
+// shared-memory hash table (pivots are always at or below their row).  Then
+// swap_apply moves each column's rows with one gather per listed row, all
+// loads of a column before its stores -- no chain of dependent swaps, and
+// nothing to do for rows that pivot on the diagonal.
+constexpr int SWAP_HASH = 1024;  // >= 2 x the widest panel (256)
+
+__global__ void __launch_bounds__(256) swap_compose(const int* ipiv, int r0, int r1, int* mv, int* mv_n) {
+  __shared__ int psrc[256];
+  __shared__ int hkey[SWAP_HASH], hval[SWAP_HASH];
+  __shared__ int cnt;
+  const int w = r1 - r0;
+  for (int i = threadIdx.x; i < w; i += blockDim.x) psrc[i] = r0 + i;
+  for (int i = threadIdx.x; i < SWAP_HASH; i += blockDim.x) hkey[i] = -1;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = r0; i < r1; i++) {
+      const int p = ipiv[i];
+      if (p == i) continue;
+      const int si = psrc[i - r0];
+      if (p < r1) {
+        psrc[i - r0] = psrc[p - r0];
+        psrc[p - r0] = si;
+      } else {
+        unsigned h = ((unsigned)p * 2654435761u) >> 22;  // 10 bits
+        while (hkey[h] != -1 && hkey[h] != p) h = (h + 1) & (SWAP_HASH - 1);
+        const int sp = hkey[h] == p ? hval[h] : p;
+        hkey[h] = p;
+        hval[h] = si;
+        psrc[i - r0] = sp;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < w; i += blockDim.x)
+    if (psrc[i] != r0 + i) {
+      const int e = atomicAdd(&cnt, 1);
+      mv[2 * e] = r0 + i; mv[2 * e + 1] = psrc[i];
+    }
+  for (int i = threadIdx.x; i < SWAP_HASH; i += blockDim.x)
+    if (hkey[i] != -1 && hval[i] != hkey[i]) {
+      const int e = atomicAdd(&cnt, 1);
+      mv[2 * e] = hkey[i]; mv[2 * e + 1] = hval[i];
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) *mv_n = cnt;
+}
+
+// one warp per column of [cb, ce) outside [skip0, skip1); at most 2 x 256 moved rows
 template <typename T>
-__global__ void laswp_kernel(cx<T>* A, long long ld, const int* ipiv, int r0, int r1, int cb, int ce, int skip0, int skip1) {
-  int j = cb + blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= ce || (j >= skip0 && j < skip1)) return;
+__global__ void __launch_bounds__(256) swap_apply(cx<T>* A, long long ld, const int* mv, const int* mv_n, int cb, int ce,
+                                                  int skip0, int skip1) {
+  const int j = cb + (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (j >= ce || (j >= skip0 && j < skip1)) return;  // whole warps leave together
+  const int n = *mv_n;
   cx<T>* col = A + (long long)j * ld;
-  for (int i = r0; i < r1; i++) {
-    int p = ipiv[i];
-    if (p != i) { cx<T> t = col[i]; col[i] = col[p]; col[p] = t; }
+  cx<T> v[16];
+#pragma unroll
+  for (int q = 0; q < 16; q++) {
+    const int e = lane + 32 * q;
+    if (e < n) v[q] = col[mv[2 * e + 1]];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < 16; q++) {
+    const int e = lane + 32 * q;
+    if (e < n) col[mv[2 * e]] = v[q];
   }
 }
 
@@ -1048,7 +1110,8 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   size_t tcb = 0;
   if (sizeof(T) == 4) tcb = tc_gemm_ws_bytes(N, N, w);
   const size_t dinv_bytes = (size_t)((N + 31) / 32) * 1024 * esz;
-  size_t total = need + tcb + 1024 + dinv_bytes + 256;
+  const size_t swap_bytes = sizeof(int) * (4 * 256 + 16);
+  size_t total = need + tcb + 1024 + dinv_bytes + 256 + swap_bytes + 256;
   if (*ws_bytes < total) {
     if (*ws) cudaFree(*ws);
     *ws = nullptr;
@@ -1065,6 +1128,8 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   int* d_info = (int*)(((uintptr_t)wp + 15) & ~(uintptr_t)15); wp = (unsigned char*)(d_info + 4);
   void* tcws = (void*)(((uintptr_t)wp + 1023) & ~(uintptr_t)1023);
   cx<T>* dinv = (cx<T>*)(((uintptr_t)tcws + tcb + 255) & ~(uintptr_t)255);
+  int* swap_mv = (int*)(((uintptr_t)((unsigned char*)dinv + dinv_bytes) + 255) & ~(uintptr_t)255);
+  int* swap_n = swap_mv + 4 * 256;
   DinvState ds;
   ds.dinv = (cx<float>*)dinv;
   ds.made.assign((N + 31) / 32, 0);
@@ -1090,16 +1155,18 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
       if (leaf_cl) {
         int nl = 0;
         e = rec_panel((cx<float>*)A, ld, N, c0, wc, c0, c0 + wc, d_ipiv, d_info, leaf_cl, tcws, tcb, &ds, s, &nl);
-        stats_launch(ST_PANEL, nl + 1);
+        stats_launch(ST_PANEL, nl);
         if (e != cudaSuccess) return cuda_status(e, "recursive panel");
       } else {
-        stats_launch(ST_PANEL, 2);
+        stats_launch(ST_PANEL, 1);
         e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(512), args, sm, s);
         if (e != cudaSuccess) return cuda_status(e, "panel_kernel");
       }
       // interchanges to the left and right of the panel
-      laswp_kernel<T><<<(N + 255) / 256, 256, 0, s>>>(A, ld, d_ipiv, c0, c0 + wc, 0, N, c0, c0 + wc);
-      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "laswp");
+      swap_compose<<<1, 256, 0, s>>>(d_ipiv, c0, c0 + wc, swap_mv, swap_n);
+      swap_apply<T><<<(unsigned)((32LL * N + 255) / 256), 256, 0, s>>>(A, ld, swap_mv, swap_n, 0, N, c0, c0 + wc);
+      stats_launch(ST_PANEL, 2);
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "row interchanges");
     }
     const int cb = c0 + wc;
     if (cb >= N) break;
