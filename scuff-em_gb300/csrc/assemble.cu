@@ -47,6 +47,11 @@ __constant__ double c_ho[3 * HO_N * HO_N];
 constexpr int NT_SELF = 16;              // 1-D rule of the common-triangle reduction
 constexpr int N_FIP = 12;                // rules of the static near-pair integrals
 __constant__ double c_gx16[NT_SELF], c_gw16[NT_SELF], c_gx12[N_FIP], c_gw12[N_FIP];
+// static integrals inside the adjoint's central differences: 8 points per
+// dimension move their derivatives by < 1e-8 (relative) against 12, at a
+// third of the cost (touching pairs are the worst case)
+constexpr int N_FIP_ADJ = 8;
+__constant__ double c_gx8[N_FIP_ADJ], c_gw8[N_FIP_ADJ];
 
 static void gauss01(int n, double* x, double* w) {
   for (int i = 0; i < n; i++) {
@@ -81,6 +86,8 @@ static gbem_status init_rules() {
   double gx16[NT_SELF], gw16[NT_SELF], gx12[N_FIP], gw12[N_FIP];
   gauss01(NT_SELF, gx16, gw16);
   gauss01(N_FIP, gx12, gw12);
+  double gx8[N_FIP_ADJ], gw8[N_FIP_ADJ];
+  gauss01(N_FIP_ADJ, gx8, gw8);
   FFRule ffr;
   fill_ff_rule(h_lo, &ffr);
   SinCosTab sct;
@@ -93,6 +100,8 @@ static gbem_status init_rules() {
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gw16, gw16, sizeof gw16);
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gx12, gx12, sizeof gx12);
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gw12, gw12, sizeof gw12);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gx8, gx8, sizeof gx8);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gw8, gw8, sizeof gw8);
   if (e != cudaSuccess) return cuda_status(e, "copy quadrature rules");
   if (dev < 64) done[dev] = true;
   return GBEM_OK;
@@ -1591,8 +1600,8 @@ __global__ void __launch_bounds__(128) vjp_far_kernel(VjpFarArgs a, RegionArgs r
 
 // Re sum over regions and (Qa, Qb) of the pair's weighted values at the given
 // vertex positions -- the arithmetic of self_kernel, near_kernel and
-// td_touch_kernel for one pair in one thread, with the edge lengths taken
-// from the positions
+// td_touch_kernel for one pair in one thread (the static integrals at the
+// adjoint's 8-point rule), with the edge lengths taken from the positions
 __device__ double near_pair_energy(const DevNear& d, const double* Va, const double* Vb, const double* sgA,
                                    const double* sgB, const RegionArgs& ra, const cx<double> W[3][9]) {
   const bool self = d.pa == d.pb;
@@ -1638,8 +1647,8 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
       cx<double> T[10];
       if (!sw) {
         if (!haveF) {
-          if (d.ncv == 0) fippi_far(Va, Vb, c_gx12, c_gw12, N_FIP, &F);
-          else fippi_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, c_gx12, c_gw12, N_FIP, &F);
+          if (d.ncv == 0) fippi_far(Va, Vb, c_gx8, c_gw8, N_FIP_ADJ, &F);
+          else fippi_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, c_gx8, c_gw8, N_FIP_ADJ, &F);
           haveF = true;
         }
         pair_moments<double, 1>(g, k, c_lo64, 6, MG, MP);
