@@ -174,7 +174,7 @@ gbem_status gbem_lu_factor(gbem_matrix *M, int *ipiv, int *info);
 /* Replaces HMatrix::LUSolve(HMatrix *X, char Trans, int nrhs)
  * (LBWrappers.cc:208-236): solves op(M) X = B in place on a host
  * column-major array B (N x nrhs, ldb) of the factor's type (C128, C64, or
- * real F64); trans is 'N' or 'T'. */
+ * real F64); trans is 'N', 'T' or 'C' (conjugate transpose, as zgetrs). */
 gbem_status gbem_lu_solve(gbem_matrix *M, char trans, int nrhs, void *B, int ldb);
 
 /* Trace of M^-1 B over the first ncols diagonal entries, for a factored M
@@ -282,6 +282,23 @@ gbem_status gbem_stats(int enable, double ms[8], long long counts[8]);
 gbem_status gbem_power_emt(gbem_geometry *g, double omega_re, double omega_im, const double *eps,
                            const double *mu, int precision, int nrhs, const double *KN, int ldkn,
                            const double *rhs, int ldr, double *pscat, double *pext);
+
+/* ---- cache of the static near-pair integrals ----------------------------------
+ * Replaces PreloadCache / StoreCache (libscuff.h:662-663) and reads and writes
+ * their file format (FIPPICache.cc:195-400: "FIPPICACHE" + records of a
+ * 15-float key and the reference's QIFIPPIData), so a cache written by the
+ * reference warms this library's near field and the other way round.  The
+ * cache is process-wide, like the reference's GlobalFIPPICache: preloaded
+ * records are used by every later cold near-field pass (pairs not found are
+ * computed as usual); gbem_cache_store writes the preloaded records and the
+ * tables of every live geometry whose near field has been computed. */
+gbem_status gbem_cache_preload(const char *path);
+gbem_status gbem_cache_store(const char *path);
+gbem_status gbem_cache_clear(void);
+gbem_status gbem_cache_size(long long *nrecords);
+/* near pairs of g (common-triangle pairs excepted) found / not found in the
+ * cache (host only; no GPU needed) */
+gbem_status gbem_cache_lookup_stats(const gbem_geometry *g, long long *hits, long long *misses);
 
 /* ---- shape derivatives (adjoint) -------------------------------------------
  * No reference counterpart: the reference differentiates rigid motions of

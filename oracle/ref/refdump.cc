@@ -6,6 +6,9 @@
 // Commands (all output is plain text or raw little-endian binary):
 //   refdump geom   GEO OUT                   panels and RWG edges of every surface
 //   refdump matrix GEO wr wi OUT             full BEM matrix (int32 N, then N*N complex128, column-major)
+//   refdump cache  GEO wr wi OUT             assemble, then write the FIPPI cache file (StoreCache)
+//   refdump cachematrix GEO wr wi CACHE OUT  PreloadCache(CACHE), assemble, write the matrix
+//                                            (both print the cache's hits and misses)
 //   refdump ppi    GEO ns LIST OUT           panel-panel integrals for "npa iQa npb iQb kr ki" lines
 //   refdump fippi  GEO ns LIST OUT           Q-independent FIPPI data for "npa npb" lines
 //   refdump rhs    GEO wr wi E0x E0y E0z nx ny nz OUT   plane-wave RHS (int32 N, N complex128)
@@ -93,6 +96,28 @@ int main(int argc, char **argv) {
       }
     }
     fclose(f);
+    return 0;
+  }
+
+  if (!strcmp(cmd, "cache")) {
+    // assemble once (every near pair's FIPPI record goes to the global cache),
+    // then write the cache file (StoreCache, FIPPICache.cc:223-293)
+    cdouble Omega(atof(argv[3]), atof(argv[4]));
+    HMatrix *M = G->AllocateBEMMatrix();
+    G->AssembleBEMMatrix(Omega, M);
+    StoreCache(argv[5]);
+    printf("%d %d\n", (int)GlobalFIPPICache.Hits, (int)GlobalFIPPICache.Misses);
+    return 0;
+  }
+
+  if (!strcmp(cmd, "cachematrix")) {
+    // PreloadCache(CACHE), assemble, write the matrix; prints the cache hits and misses
+    PreloadCache(argv[5]);
+    cdouble Omega(atof(argv[3]), atof(argv[4]));
+    HMatrix *M = G->AllocateBEMMatrix();
+    G->AssembleBEMMatrix(Omega, M);
+    write_matrix(argv[6], M);
+    printf("%d %d\n", (int)GlobalFIPPICache.Hits, (int)GlobalFIPPICache.Misses);
     return 0;
   }
 

@@ -964,18 +964,50 @@ static cudaError_t far_mixed(Geometry* g, const Block& b, DevBlock* db, const Ti
   return cudaSuccess;
 }
 
+// The static table of every near pair.  With records in the process-wide
+// cache (gbem_cache_preload), the pairs found there are converted on the host
+// and uploaded, and the kernel computes only the others.
 gbem_status compute_fippi(Geometry* g, cudaStream_t s) {
+  const bool cached = cache_active();
   for (size_t bi = 0; bi < g->blocks.size(); bi++) {
     DevBlock* db = g->dblocks[bi];
     if (db->nother == 0) continue;
     StatTimer t(ST_NEAR, s);
-    fippi_kernel<<<(db->nother + 63) / 64, 64, 0, s>>>(db->near, db->other_list, db->nother, g->d_pv, db->fippi);
-    stats_launch(ST_NEAR);
+    const int* list = db->other_list;
+    int n = db->nother;
+    int* dmiss = nullptr;
+    if (cached) {
+      std::vector<Fippi> table;
+      std::vector<int> miss;
+      cache_lookup(g, g->blocks[bi], table, miss);
+      cudaError_t e = cudaMemcpyAsync(db->fippi, table.data(), sizeof(Fippi) * table.size(), cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess && !miss.empty()) e = cudaMallocAsync((void**)&dmiss, sizeof(int) * miss.size(), s);
+      if (e == cudaSuccess && !miss.empty())
+        e = cudaMemcpyAsync(dmiss, miss.data(), sizeof(int) * miss.size(), cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host vectors go out of scope
+      if (e != cudaSuccess) return cuda_status(e, "cached near table");
+      list = dmiss;
+      n = (int)miss.size();
+    }
+    if (n > 0) {
+      fippi_kernel<<<(n + 63) / 64, 64, 0, s>>>(db->near, list, n, g->d_pv, db->fippi);
+      stats_launch(ST_NEAR);
+    }
     cudaError_t e = cudaGetLastError();
+    if (dmiss) cudaFreeAsync(dmiss, s);
     if (e != cudaSuccess) return cuda_status(e, "fippi_kernel");
   }
   g->fippi_ready = true;
   return GBEM_OK;
+}
+
+gbem_status download_fippi(Geometry* g, size_t bi, std::vector<Fippi>& table) {
+  const DevBlock* db = g->dblocks[bi];
+  table.assign((size_t)db->nnear, Fippi());
+  if (!db->nnear) return GBEM_OK;
+  cudaError_t e = cudaSetDevice(g->device);
+  if (e == cudaSuccess) e = cudaMemcpy(table.data(), db->fippi, sizeof(Fippi) * table.size(), cudaMemcpyDeviceToHost);
+  return cuda_status(e, "download near table");
 }
 
 // per-region wavenumbers and PMCHWT/EFIE prefactors of a surface block

@@ -200,6 +200,7 @@ gbem_status gbem_geometry_create(int num_surfaces, const gbem_surface_desc* surf
   if (st != GBEM_OK) { delete g; return st; }
   // no CUDA call here: the device stream is created on first device use, so
   // the mesh bookkeeping also works on a host without a GPU
+  cache_register(g);
   *out = g;
   return GBEM_OK;
 }
@@ -211,6 +212,7 @@ static gbem_status ensure_stream(gbem_geometry* g) {
 }
 
 static void geometry_release(gbem_geometry* g) {
+  cache_unregister(g);
   if (g->stream) {
     cudaSetDevice(g->device);
     cudaStreamSynchronize(g->stream);
@@ -529,6 +531,12 @@ gbem_status gbem_vertex_vjp_rhs_planewave(gbem_geometry* g, double omega_re, dou
   cudaFreeAsync(dB, s); cudaFreeAsync(dG, s);
   cudaStreamSynchronize(s);
   return st;
+}
+
+gbem_status gbem_cache_lookup_stats(const gbem_geometry* g, long long* hits, long long* misses) {
+  if (!g || !hits || !misses) { set_error("gbem_cache_lookup_stats: NULL argument"); return GBEM_EINVAL; }
+  cache_stats(g, hits, misses);
+  return GBEM_OK;
 }
 
 gbem_status gbem_geometry_num_vertices(const gbem_geometry* g, int* nv) {

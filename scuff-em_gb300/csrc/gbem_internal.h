@@ -72,6 +72,7 @@ struct Block {
 };
 
 struct DevBlock;  // defined in assemble.cu
+struct Fippi;     // static near-pair integrals (bem_math.cuh)
 
 struct Geometry {
   int device = 0;
@@ -122,6 +123,8 @@ struct Matrix {
 
 // geometry.cpp
 gbem_status build_geometry(int ns, const gbem_surface_desc* d, int nreg, Geometry* g);
+// common-vertex count and common-vertices-first order of a panel pair (AssessPanelPair.cc:52-103)
+int assess_pair(const double* Va[3], const double* Vb[3], double rmax, int8_t pa[3], int8_t pb[3]);
 
 // assemble.cu
 // block selection: only the (nsa, nsb) surface block, placed at (row0, col0)
@@ -147,6 +150,15 @@ gbem_status vertex_vjp_device(Geometry* g, double wr, double wi, const double* e
 gbem_status rhs_vjp_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int nw,
                            const double* E0, const double* nh, const void* d_gb, int ldg, double* d_grad, cudaStream_t s);
 int geometry_total_vertices(const Geometry* g);
+gbem_status download_fippi(Geometry* g, size_t bi, std::vector<Fippi>& table);
+
+// fippi_cache.cu: the process-wide cache of static near-pair integrals in the
+// reference's FIPPI cache format
+void cache_register(Geometry* g);
+void cache_unregister(Geometry* g);
+bool cache_active();
+int cache_lookup(const Geometry* g, const Block& b, std::vector<Fippi>& table, std::vector<int>& miss);
+void cache_stats(const Geometry* g, long long* hits, long long* misses);
 
 // lu.cu
 gbem_status lu_factor_device(void* dA, int N, int ld, int dtype, int* d_ipiv, int* h_info, cudaStream_t s,

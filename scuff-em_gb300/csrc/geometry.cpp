@@ -198,6 +198,10 @@ static int assess(const double* Va[3], const double* Vb[3], double rmax, int8_t 
   return ncv;
 }
 
+int assess_pair(const double* Va[3], const double* Vb[3], double rmax, int8_t pa[3], int8_t pb[3]) {
+  return assess(Va, Vb, rmax, pa, pb);
+}
+
 // rRel exactly as AssessPanelPair.cc:160-166 computes it
 static double rrel_of(const double* ca, const double* cb, double rmax) {
   double DC, r2;

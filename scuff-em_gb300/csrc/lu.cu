@@ -1605,13 +1605,38 @@ gbem_status lu_solve_many_device(const void* dA, int N, int ld, int dtype, const
   return GBEM_EINVAL;
 }
 
+// B <- conj(B): A^H x = b is A^T conj(x) = conj(b) (zgetrs with Trans = 'C')
+template <typename T>
+__global__ void conj_cols(cx<T>* B, long long ldb, int N, int nrhs) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= (long long)N * nrhs) return;
+  cx<T>* b = B + (q % N) + (q / N) * ldb;
+  b->im = -b->im;
+}
+
+template <typename T>
+static gbem_status solve_any(const cx<T>* A, int N, int ld, const int* d_perm, char trans, int nrhs, cx<T>* B, int ldb,
+                             cx<T>* Y, cudaStream_t s) {
+  if (trans != 'C') return solve_impl<T>(A, N, ld, d_perm, trans, nrhs, B, ldb, Y, s);
+  const unsigned nb = (unsigned)(((long long)N * nrhs + 255) / 256);
+  conj_cols<T><<<nb, 256, 0, s>>>(B, ldb, N, nrhs);
+  gbem_status st = solve_impl<T>(A, N, ld, d_perm, 'T', nrhs, B, ldb, Y, s);
+  if (st != GBEM_OK) return st;
+  conj_cols<T><<<nb, 256, 0, s>>>(B, ldb, N, nrhs);
+  stats_launch(ST_SOLVE, 2);
+  return cuda_status(cudaGetLastError(), "solve conj");
+}
+
 gbem_status lu_solve_device(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs, void* dB,
                             int ldb, void* dY, cudaStream_t s) {
-  if (trans != 'N' && trans != 'T') { set_error("lu_solve: trans must be 'N' or 'T'"); return GBEM_EINVAL; }
+  if (trans != 'N' && trans != 'T' && trans != 'C') {
+    set_error("lu_solve: trans must be 'N', 'T' or 'C'");
+    return GBEM_EINVAL;
+  }
   if (dtype == GBEM_C128)
-    return solve_impl<double>((const cx<double>*)dA, N, ld, d_perm, trans, nrhs, (cx<double>*)dB, ldb, (cx<double>*)dY, s);
+    return solve_any<double>((const cx<double>*)dA, N, ld, d_perm, trans, nrhs, (cx<double>*)dB, ldb, (cx<double>*)dY, s);
   if (dtype == GBEM_C64)
-    return solve_impl<float>((const cx<float>*)dA, N, ld, d_perm, trans, nrhs, (cx<float>*)dB, ldb, (cx<float>*)dY, s);
+    return solve_any<float>((const cx<float>*)dA, N, ld, d_perm, trans, nrhs, (cx<float>*)dB, ldb, (cx<float>*)dY, s);
   set_error("lu_solve: dtype must be C128 or C64");
   return GBEM_EINVAL;
 }
@@ -1835,7 +1860,7 @@ static gbem_status solve_static_impl(const cx<T>* A, int N, int ld, const int* d
                                       cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_status(e, "solve upload");
     gbem_status st = trans == 'N' ? solve_chunk_n<T>(A, N, ld, d_perm, nr, Bd, N, Y, Dinv, s)
-                                  : solve_impl<T>(A, N, ld, d_perm, 'T', nr, Bd, N, Y, s);  // the 'T' form allocates nothing
+                                  : solve_any<T>(A, N, ld, d_perm, trans, nr, Bd, N, Y, s);  // 'T'/'C' allocate nothing
     if (st != GBEM_OK) return st;
     e = cudaMemcpy2DAsync(hc, (size_t)ldb * es, Bd, (size_t)N * es, (size_t)N * es, nr, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -1846,7 +1871,10 @@ static gbem_status solve_static_impl(const cx<T>* A, int N, int ld, const int* d
 
 gbem_status lu_solve_static_scratch(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs,
                                     void* hB, int ldb, cudaStream_t s) {
-  if (trans != 'N' && trans != 'T') { set_error("gbem_lu_solve_noalloc: trans must be 'N' or 'T'"); return GBEM_EINVAL; }
+  if (trans != 'N' && trans != 'T' && trans != 'C') {
+    set_error("gbem_lu_solve_noalloc: trans must be 'N', 'T' or 'C'");
+    return GBEM_EINVAL;
+  }
   if (dtype != GBEM_C128 && dtype != GBEM_C64) { set_error("gbem_lu_solve_noalloc: dtype must be C128 or C64"); return GBEM_EINVAL; }
   const size_t need = solve_scratch_need(N, dtype);
   if (need > kSolveScratchBytes) {

@@ -28,7 +28,8 @@ EXPORTS = [
     "gbem_assemble_block_gradient", "gbem_assemble_block_gradient_host", "gbem_power_emt",
     "gbem_lu_trace", "gbem_lu_trace_host", "gbem_assemble_block_dmdt", "gbem_assemble_block_dmdt_host",
     "gbem_solve_mixed_batch", "gbem_vertex_vjp_matrix", "gbem_vertex_vjp_rhs_planewave",
-    "gbem_geometry_num_vertices",
+    "gbem_geometry_num_vertices", "gbem_cache_preload", "gbem_cache_store", "gbem_cache_clear", "gbem_cache_size",
+    "gbem_cache_lookup_stats",
 ]
 
 
@@ -90,6 +91,8 @@ def lib():
             "gbem_vertex_vjp_matrix": ([P, D, D, P, P, I, P, I, P, I, D, P], I),
             "gbem_vertex_vjp_rhs_planewave": ([P, D, D, P, P, I, P, P, P, I, P], I),
             "gbem_geometry_num_vertices": ([P, P], I),
+            "gbem_cache_preload": ([ctypes.c_char_p], I), "gbem_cache_store": ([ctypes.c_char_p], I),
+            "gbem_cache_clear": ([], I), "gbem_cache_size": ([P], I), "gbem_cache_lookup_stats": ([P, P, P], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -204,6 +204,12 @@ class RWGGeometry:
         check(lib().gbem_geometry_edges(self._h, surface, ctypes.byref(n), E.ctypes.data, L.ctypes.data))
         return E, L
 
+    def cache_lookup_stats(self):
+        """(hits, misses) of this geometry's near pairs in the process-wide cache."""
+        h, m = ctypes.c_longlong(), ctypes.c_longlong()
+        check(lib().gbem_cache_lookup_stats(self._h, ctypes.byref(h), ctypes.byref(m)))
+        return h.value, m.value
+
     def near_counts(self):
         c = (ctypes.c_longlong * 4)()
         check(lib().gbem_geometry_near_counts(self._h, c))
@@ -378,6 +384,29 @@ class RWGGeometry:
         if st not in (_lib.GBEM_OK, _lib.GBEM_ENOCONV):
             check(st)
         return X, it.value, res.value
+
+
+def PreloadCache(path):
+    """Load a FIPPI cache file (the reference's format, written by either
+    side) into the process-wide cache (PreloadCache, libscuff.h:662)."""
+    check(lib().gbem_cache_preload(os.fsencode(path)))
+
+
+def StoreCache(path):
+    """Write the process-wide cache -- preloaded records plus the static
+    tables of every live geometry -- in the reference's format (StoreCache,
+    libscuff.h:663)."""
+    check(lib().gbem_cache_store(os.fsencode(path)))
+
+
+def ClearCache():
+    check(lib().gbem_cache_clear())
+
+
+def CacheSize():
+    n = ctypes.c_longlong()
+    check(lib().gbem_cache_size(ctypes.byref(n)))
+    return n.value
 
 
 def solve_mixed_batch(jobs, max_concurrent=4, tol=1e-10, max_iter=10):

@@ -21,6 +21,8 @@ Fixtures:
                    right-hand sides, solutions and EMT powers for small geometries.
   ref_<case>_grad.npz, ref_<case>_torque.npz  surface blocks with their
                    derivatives for displacements (GradM) and rotations (dMdT).
+  ref_fippi_cache_s1.bin  the reference's own FIPPI cache file for the s=1
+                   dielectric sphere (with its mesh, ref_fippi_cache_s1_mesh.npz).
   mie_pft_tables.json  the reference's tables of sphere powers (R = 1 um, PEC,
                    SiO2, gold at omega = 0.01, 0.1, 1; unitTests/unit-test-PFT.cc:
                    77-130), read from the test source as text: they pin the Mie
@@ -257,19 +259,32 @@ def mie_tables(ref):
                   indent=1)
 
 
+def cache_fixture(tmp):
+    """ref_fippi_cache_s1.bin: the reference's FIPPI cache file (StoreCache)
+    after assembling the dielectric s=1 sphere at kR = 2, with the mesh it
+    read (ref_fippi_cache_s1_mesh.npz) and its matrix (column sample)."""
+    V1, P1 = icosphere(1)
+    geo = geo_file(tmp, "cache_s1", [("sph", V1, P1, "CONST_EPS_2.25+0.01i", None)])
+    out = os.path.join(HERE, "ref_fippi_cache_s1.bin")
+    run(["cache", os.path.basename(geo), 2.0, 0.0, out], tmp)
+    V, P = read_msh(os.path.join(tmp, "sph.msh"))
+    np.savez_compressed(os.path.join(HERE, "ref_fippi_cache_s1_mesh.npz"), V=V, P=P)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", choices=["gradients", "torque", "mie"], help="regenerate one group of fixtures only")
+    ap.add_argument("--only", choices=["gradients", "torque", "mie", "cache"],
+                    help="regenerate one group of fixtures only")
     a = ap.parse_args()
     if a.only == "mie":
         mie_tables(a.ref)
         return
     if not os.path.exists(REFDUMP):
         sys.exit("build the reference first: make -C oracle/ref REF=%s" % a.ref)
-    if a.only in ("gradients", "torque"):
+    if a.only in ("gradients", "torque", "cache"):
         with tempfile.TemporaryDirectory() as tmp:
-            (gradient_fixtures if a.only == "gradients" else torque_fixtures)(tmp)
+            {"gradients": gradient_fixtures, "torque": torque_fixtures, "cache": cache_fixture}[a.only](tmp)
         return
     rng = np.random.default_rng(0)
     with tempfile.TemporaryDirectory() as tmp:
@@ -289,6 +304,7 @@ def main():
         matrix_case(tmp, "diel_s1_w12", [("sph", V1, P1, "CONST_EPS_4+0.1i", None)], 12.0)
         gradient_fixtures(tmp)
         torque_fixtures(tmp)
+        cache_fixture(tmp)
     mie_tables(a.ref)
 
 

@@ -41,6 +41,8 @@ def test_lu_matches_lapack(N):
     assert np.abs(A @ X - B).max() / np.abs(B).max() < 1e-9
     XT = _solve_host(LU, ipiv, B, "T")
     assert np.abs(A.T @ XT - B).max() / np.abs(B).max() < 1e-9
+    XC = _solve_host(LU, ipiv, B, "C")  # zgetrs Trans = 'C': A^H x = b
+    assert np.abs(A.conj().T @ XC - B).max() / np.abs(B).max() < 1e-9
 
 
 def test_singular_info():
