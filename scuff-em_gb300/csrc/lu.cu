@@ -1173,7 +1173,33 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     const int nrest = N - cb;
     const bool dm = wc % 32 == 0 && c0 % 32 == 0 && (size_t)(2 * wc + 32) * 33 * esz <= smem_cap;
     size_t tsm = (size_t)(dm ? 2 * wc + 32 : wc) * 33 * esz;
-    {
+    // complex FP32 with a whole 256-row panel: U12 = L11^-1 A12 in two halves,
+    // X1 = L11a^-1 B1, B2 -= L21 X1 on the tensor cores, X2 = L22^-1 B2 -- the
+    // off-diagonal half of the solve's products leaves the FP32 pipes
+    bool split = false;
+    if (sizeof(T) == 4 && dm && leaf_cl && wc == 256) {
+      StatTimer tt(ST_PANEL, s);
+      const int h = wc / 2;
+      const size_t hsm = (size_t)(2 * h + 32) * 33 * esz;
+      trsm_blocked<T><<<(nrest + 31) / 32, 256, hsm, s>>>(A, ld, c0, h, cb, N, dinv, dinv_make_mask(&ds, c0, h));
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
+      stats_launch(ST_PANEL);
+      cx<float>* B2 = (cx<float>*)(A + (c0 + h) + (long long)cb * ld);
+      const cx<float>* L21h = (const cx<float>*)(A + (c0 + h) + (long long)c0 * ld);
+      const cx<float>* X1 = (const cx<float>*)(A + c0 + (long long)cb * ld);
+      if (tc_gemm_update(B2, ld, L21h, ld, X1, ld, h, nrest, h, tcws, tcb, s, &e)) {
+        stats_launch(ST_PANEL, 3);
+      } else {
+        if (e != cudaSuccess) return cuda_status(e, "tensor-core update");
+        gemm_simt<float><<<dim3((h + 63) / 64, (nrest + 63) / 64), 256, 0, s>>>(B2, ld, L21h, ld, X1, ld, h, nrest, h);
+        stats_launch(ST_PANEL);
+      }
+      trsm_blocked<T><<<(nrest + 31) / 32, 256, hsm, s>>>(A, ld, c0 + h, h, cb, N, dinv, dinv_make_mask(&ds, c0 + h, h));
+      stats_launch(ST_PANEL);
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
+      split = true;
+    }
+    if (!split) {
       StatTimer tt(ST_PANEL, s);
       unsigned make = 0u;
       if (dm && leaf_cl) {
