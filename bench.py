@@ -37,6 +37,13 @@ METRIC = "BEM solves/s at N=15360, mixed-prec vs FP64 on one GB300 @<=1e-6 rel e
 PLANE_WAVES = [((1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1)), ((1, 0, 0), (0, 0, -1)), ((0, 1, 0), (0, 0, -1))]
 
 
+
+# DRAM read + write bytes per trailing-update launch at N = 15360, measured by
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass) over 48 of the 59
+# launches of a factorisation, the 11 smallest estimated from the last captured
+# one's bytes per entry (the capture's summary is kept under profiles/)
+TC_TRAFFIC_BYTES_PER_LAUNCH = 1.45e9
+
 def workload(subdiv):
     from gbem import mesh
     V, P = mesh.icosphere(subdiv)
@@ -334,8 +341,11 @@ def main():
     if gemm_ms > 0:
         n_upd = max(1, (N + 255) // 256 - 1)
         ach = upd_flops / (gemm_ms * 1e-3) / 1e12
+        # DRAM bytes per trailing-update launch from one ncu capture of this
+        # workload; valid for N = 15360 only
+        traffic = TC_TRAFFIC_BYTES_PER_LAUNCH if N == 15360 else None
         out["roofline"] = {"bound": "tensor", "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s",
-                           "frac": ach / bf16_peak, "traffic": None, "kernel": "tc_gemm_kernel (+split packing)",
+                           "frac": ach / bf16_peak, "traffic": traffic, "kernel": "tc_gemm_kernel (+split packing)",
                            "launches_per_step": n_upd, "peak_kind": peak_kind,
                            "note": "algorithmic complex flops 8mnk; the split-BF16 form issues 3x that on the "
                                    "tensor pipe"}
