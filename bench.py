@@ -36,13 +36,12 @@ ZVAC = 376.73031346177
 METRIC = "BEM solves/s at N=15360, mixed-prec vs FP64 on one GB300 @<=1e-6 rel err"
 PLANE_WAVES = [((1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1)), ((1, 0, 0), (0, 0, -1)), ((0, 1, 0), (0, 0, -1))]
 
-
-
 # DRAM read + write bytes per trailing-update launch at N = 15360, measured by
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass) over 48 of the 59
 # launches of a factorisation, the 11 smallest estimated from the last captured
 # one's bytes per entry (the capture's summary is kept under profiles/)
 TC_TRAFFIC_BYTES_PER_LAUNCH = 1.45e9
+
 
 def workload(subdiv):
     from gbem import mesh
