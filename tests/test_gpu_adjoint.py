@@ -84,3 +84,33 @@ def test_mixed_gradient_matches_fp64():
     rel = np.abs(g32 - g64).max() / np.abs(g64).max()
     print("mixed vs fp64 gradient: %.2e" % rel)
     assert rel < 1e-5
+
+
+def test_vertex_gradient_sums_to_the_rigid_displacement_gradient():
+    """Summed over one body's vertices, the vertex contraction is the
+    derivative under a rigid displacement of that body -- the reference's own
+    dM/dx_mu force path (AssembleBEMMatrixBlock's GradM, pinned against the
+    reference in test_gpu_gradient.py).  Bodies 2.2 apart: every inter-body
+    pair is a far pair, where both use the 6x6 rule, so they agree to rounding."""
+    from gbem import RWGGeometry, mesh
+    from gbem.api import Material
+    V, P = mesh.icosphere(1)
+    G = RWGGeometry([{"V": V, "P": P, "material": None},
+                     {"V": 0.8 * V + np.array([0.3, 0.0, 4.0]), "P": P, "material": Material(4.0 + 0.2j)}])
+    w = 1.5
+    N, n0 = G.TotalBFs, G.NumBFs(0)
+    rng = np.random.default_rng(3)
+    # lam only on body 1's rows and x only on body 0's: the self blocks drop out
+    # (their translation-invariant terms would cancel only to the near pairs'
+    # difference accuracy, ~1e-7 of this weak inter-body term)
+    lam = rng.standard_normal((N, 2)) + 1j * rng.standard_normal((N, 2))
+    x = rng.standard_normal((N, 2)) + 1j * rng.standard_normal((N, 2))
+    lam[:n0] = 0.0
+    x[n0:] = 0.0
+    g = G.VertexVJP(w, lam, x)
+    rigid = g[len(V):].sum(axis=0)
+    D = G.AssembleBEMMatrixBlockGradient(1, 0, w)  # block (1, 0), surface 1 displaced
+    ref = np.array([np.real(np.sum(np.conj(lam[n0:]) * (D[m] @ x[:n0]))) for m in range(3)])
+    rel = np.abs(rigid - ref).max() / np.abs(ref).max()
+    print("sum of vertex gradients vs GradM contraction: %.2e" % rel)
+    assert rel < 1e-9
