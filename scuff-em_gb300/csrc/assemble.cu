@@ -1514,7 +1514,8 @@ gbem_status rhs_planewave_device(Geometry* g, double wr, double wi, const double
 //                   derivative of the 6x6-rule integrals (adjoint.cuh), the
 //                   edge-length factors La Lb included.
 //  vjp_near_kernel  near and common-vertex pairs, one thread per (pair,
-//                   vertex, coordinate): central differences of the FP64
+//                   vertex, coordinate) -- one vertex per pair follows from
+//                   translation invariance: central differences of the FP64
 //                   near-pair evaluation (static integrals recomputed for the
 //                   displaced vertices), contracted with the same weights.
 //  rhs_vjp_kernel   Re sum conj(g_i) db_i/dV for plane-wave right-hand sides.
@@ -1724,8 +1725,13 @@ __global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs
   const VjpTables& t = a.t;
   const DevNear d = a.near[pair];
   const bool self = d.pa == d.pb;
-  if (self && v >= 3) return;
+  // a pair's value does not change when both panels move together, so the
+  // derivative for panel a's vertex 0 is minus the sum of the others': that
+  // vertex is not displaced, each other direction subtracts its share from it
+  if (v == 0 || (self && v >= 3)) return;
   const int gv = v < 3 ? t.pvi[3 * d.pa + v] : t.pvi[3 * d.pb + v - 3];
+  const int g0 = t.pvi[3 * d.pa];
+  if (gv == g0) return;
   if (v >= 3)
     for (int q = 0; q < 3; q++)
       if (t.pvi[3 * d.pa + q] == gv) return;  // a shared vertex moves with panel a's slot
@@ -1748,7 +1754,9 @@ __global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs
     }
     E[s] = near_pair_energy(d, Va, Vb, sgA, sgB, ra, W);
   }
-  atomicAdd(&t.grad[3 * (size_t)gv + c], (E[0] - E[1]) / (2.0 * h));
+  const double dE = (E[0] - E[1]) / (2.0 * h);
+  atomicAdd(&t.grad[3 * (size_t)gv + c], dE);
+  atomicAdd(&t.grad[3 * (size_t)g0 + c], -dE);
 }
 
 struct RhsVjpArgs {

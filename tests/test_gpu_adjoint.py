@@ -65,8 +65,9 @@ def test_extinction_gradient_matches_central_differences(kind):
 
 def test_gradient_is_translation_invariant():
     """The power does not change when the whole scatterer moves, so the
-    vertex gradients sum to zero -- a check of every pair class at once,
-    on a larger mesh (icosphere s=3, N = 3840)."""
+    vertex gradients sum to zero, on a larger mesh (icosphere s=3, N = 3840):
+    a check of the far pairs' reverse-mode derivative against the right-hand
+    side's (the near pairs use the same invariance to skip one vertex each)."""
     topo, V0, w = _case("diel", subdiv=3)
     t0 = time.perf_counter()
     p0, g = _power(topo, V0, w)
