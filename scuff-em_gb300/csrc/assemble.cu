@@ -1718,10 +1718,12 @@ struct VjpNearArgs {
 };
 
 __global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs ra) {
+  // 15 threads per pair: vertices 1..5 of the pair's six slots (panel a's
+  // vertex 0 follows from the others)
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long pair = tid / 18;
+  const long long pair = tid / 15;
   if (pair >= a.nnear) return;
-  const int dir = (int)(tid % 18), v = dir / 3, c = dir % 3;
+  const int dir = (int)(tid % 15), v = 1 + dir / 3, c = dir % 3;
   const VjpTables& t = a.t;
   const DevNear d = a.near[pair];
   const bool self = d.pa == d.pb;
@@ -1895,7 +1897,7 @@ gbem_status vertex_vjp_device(Geometry* g, double wr, double wi, const double* e
       VjpNearArgs na;
       na.t = t; na.near = db->near; na.nnear = db->nnear; na.bpe_a = fa.bpe_a; na.bpe_b = fa.bpe_b;
       na.rel_step = rel_step;
-      const long long n = 18LL * db->nnear;
+      const long long n = 15LL * db->nnear;
       vjp_near_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(na, ra);
       stats_launch(ST_OTHER);
     }
