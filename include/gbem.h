@@ -189,7 +189,10 @@ gbem_status gbem_lu_trace_host(gbem_matrix *M, const void *B, int ldb, int ncols
 
 /* gbem_lu_solve without any device allocation.  No counterpart in the
  * reference (HMatrix::LUSolve runs LAPACK on host memory).  Same arguments
- * and results as gbem_lu_solve.  It serves callers that cannot allocate GPU
+ * and results as gbem_lu_solve for complex128 and complex64 matrices; a real
+ * F64 matrix (imaginary frequency) returns GBEM_EINVAL, since its solve runs
+ * through a complex128 copy of the whole factor that no fixed scratch could
+ * hold -- use gbem_lu_solve there.  It serves callers that cannot allocate GPU
  * memory at solve time: a process whose HBM is already taken by its
  * matrices or held by another allocator's pool (a PyTorch caching allocator,
  * say), where a cudaMalloc/cudaMallocAsync inside the solve would fail.
@@ -203,7 +206,8 @@ gbem_status gbem_lu_trace_host(gbem_matrix *M, const void *B, int ldb, int ncols
  * in it has to start at zero, since each call writes every scratch byte
  * before reading it.  Calls that overlap in time on one device (other host
  * threads, other matrices) race on the array and must be serialised by the
- * caller; each call synchronises the matrix's stream before returning. */
+ * caller; each call synchronises the matrix's stream before returning, on
+ * success and on error alike. */
 gbem_status gbem_lu_solve_noalloc(gbem_matrix *M, char trans, int nrhs, void *B, int ldb);
 
 /* Host-buffer drop-in for LUFactorize on a whole HMatrix: factors the host

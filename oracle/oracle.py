@@ -31,10 +31,24 @@ def build():
     return LIB
 
 
-def build_reference(ref="/root/reference", jobs=8):
+def reference_tree():
+    """The reference source tree, if this machine has one: the directory named
+    by SCUFF_REF, else a checkout named ``reference`` beside this repository.
+    None where neither exists (the GPU host has no reference tree and uses the
+    committed fixtures)."""
+    cands = [os.environ.get("SCUFF_REF"),
+             os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "libs", "libscuff")):
+            return os.path.abspath(c)
+    return None
+
+
+def build_reference(ref=None, jobs=8):
     """Build the reference from its sources into oracle/_ref (only where the
     reference tree exists; the GPU host uses the committed fixtures)."""
-    if not os.path.isdir(ref):
+    ref = ref or reference_tree()
+    if not ref or not os.path.isdir(ref):
         return None
     subprocess.run(["make", "-C", os.path.join(HERE, "ref"), "REF=" + ref, "-j%d" % jobs], check=True,
                    capture_output=True)

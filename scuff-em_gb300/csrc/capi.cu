@@ -844,6 +844,8 @@ gbem_status gbem_lu_trace_host(gbem_matrix* M, const void* B, int ldb, int ncols
 gbem_status gbem_lu_solve_noalloc(gbem_matrix* M, char trans, int nrhs, void* B, int ldb) {
   if (!M || !B || nrhs <= 0 || ldb < M->N) { set_error("gbem_lu_solve_noalloc: bad arguments"); return GBEM_EINVAL; }
   CHECK_CUDA(cudaSetDevice(M->g->device), "cudaSetDevice");
+  if (M->dtype == GBEM_F64)  // rejected with its reason before the size check
+    return lu_solve_static_scratch(M->d, M->N, M->ld, M->dtype, M->d_perm, trans, nrhs, B, ldb, M->stream);
   if (M->N > lu_solve_noalloc_max_n(M->dtype)) {
     set_error("gbem_lu_solve_noalloc: N = %d exceeds the static scratch (N <= %d for this dtype)", M->N,
               lu_solve_noalloc_max_n(M->dtype));

@@ -1879,20 +1879,25 @@ static gbem_status solve_static_impl(const cx<T>* A, int N, int ld, const int* d
   cx<T>* Bd = (cx<T>*)scratch;
   cx<T>* Y = (cx<T>*)(scratch + align256((size_t)N * 8 * es));
   cx<T>* Dinv = (cx<T>*)(scratch + 2 * align256((size_t)N * 8 * es));
-  for (int r0 = 0; r0 < nrhs; r0 += 8) {
+  gbem_status st = GBEM_OK;
+  for (int r0 = 0; r0 < nrhs && st == GBEM_OK; r0 += 8) {
     const int nr = std::min(8, nrhs - r0);
     cx<T>* hc = hB + (long long)r0 * ldb;
     cudaError_t e = cudaMemcpy2DAsync(Bd, (size_t)N * es, hc, (size_t)ldb * es, (size_t)N * es, nr,
                                       cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return cuda_status(e, "solve upload");
-    gbem_status st = trans == 'N' ? solve_chunk_n<T>(A, N, ld, d_perm, nr, Bd, N, Y, Dinv, s)
-                                  : solve_any<T>(A, N, ld, d_perm, trans, nr, Bd, N, Y, s);  // 'T'/'C' allocate nothing
-    if (st != GBEM_OK) return st;
+    if (e != cudaSuccess) { st = cuda_status(e, "solve upload"); break; }
+    st = trans == 'N' ? solve_chunk_n<T>(A, N, ld, d_perm, nr, Bd, N, Y, Dinv, s)
+                      : solve_any<T>(A, N, ld, d_perm, trans, nr, Bd, N, Y, s);  // 'T'/'C' allocate nothing
+    if (st != GBEM_OK) break;
     e = cudaMemcpy2DAsync(hc, (size_t)ldb * es, Bd, (size_t)N * es, (size_t)N * es, nr, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return cuda_status(e, "solve download");
+    if (e != cudaSuccess) st = cuda_status(e, "solve download");
   }
-  return GBEM_OK;
+  // whatever happened, nothing of this call may still be queued on the shared
+  // scratch array when it returns: the first error is kept
+  cudaError_t es2 = cudaStreamSynchronize(s);
+  if (st == GBEM_OK && es2 != cudaSuccess) st = cuda_status(es2, "solve");
+  return st;
 }
 
 gbem_status lu_solve_static_scratch(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs,
@@ -1901,7 +1906,12 @@ gbem_status lu_solve_static_scratch(const void* dA, int N, int ld, int dtype, co
     set_error("gbem_lu_solve_noalloc: trans must be 'N', 'T' or 'C'");
     return GBEM_EINVAL;
   }
-  if (dtype != GBEM_C128 && dtype != GBEM_C64) { set_error("gbem_lu_solve_noalloc: dtype must be C128 or C64"); return GBEM_EINVAL; }
+  if (dtype != GBEM_C128 && dtype != GBEM_C64) {
+    set_error("gbem_lu_solve_noalloc: only complex128 and complex64 matrices are supported (a real F64 factor is "
+              "solved through a complex128 copy of the whole matrix, which the static scratch cannot hold); use "
+              "gbem_lu_solve for F64 matrices");
+    return GBEM_EINVAL;
+  }
   const size_t need = solve_scratch_need(N, dtype);
   if (need > kSolveScratchBytes) {
     set_error("gbem_lu_solve_noalloc: N = %d needs %zu bytes of scratch; the static scratch holds %zu bytes "

@@ -6,7 +6,7 @@ drives the reference build made by oracle/ref/Makefile, oracle/_ref/refdump).
 The fixtures it writes are small and committed; tests never read the reference
 tree at run time.
 
-  python tests/golden/make_golden.py --ref /root/reference
+  python tests/golden/make_golden.py --ref <reference source tree>
 
 Fixtures:
   ppi_unit.npz     the 12 known-answer panel-panel cases of the reference's own
@@ -40,7 +40,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(REPO, "scuff-em_gb300"))
+sys.path.insert(0, REPO)
 from gbem.mesh import icosphere, read_msh, write_msh  # noqa: E402
+from oracle import oracle  # noqa: E402
 
 REFDUMP = os.path.join(REPO, "oracle", "_ref", "refdump")
 
@@ -273,7 +275,8 @@ def cache_fixture(tmp):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=oracle.reference_tree(),
+                    help="reference source tree (default: SCUFF_REF, or a 'reference' checkout beside the repo)")
     ap.add_argument("--only", choices=["gradients", "torque", "mie", "cache"],
                     help="regenerate one group of fixtures only")
     a = ap.parse_args()
