@@ -876,3 +876,138 @@ void ora_assemble(int ns, ora_surface **S, const int *reg, const int *pec,
       M[r + (size_t)c*N] = M[c + (size_t)r*N];
     }
 }
+
+/* ------------------------------------------------------------------ */
+/* Selected whole columns of the same matrix (every row), for parity  */
+/* checks of matrices too large for the full oracle.  Entry (R, C) is */
+/* the one ora_assemble produces: computed in the upper triangle      */
+/* (R <= C) with the same calls and summation order, mirrored below   */
+/* it (AssembleBEMMatrix.cc:753-758).  cols: ncols column indices;    */
+/* Mout: N x ncols column-major complex128 with leading dimension ldm. */
+/* ------------------------------------------------------------------ */
+typedef struct { int s, e, c; } ora_bf;
+
+static ora_bf bf_of(int ns, const int *pec, const int *off, int X)
+{
+  ora_bf b = {0, 0, 0};
+  for (int s = ns - 1; s >= 0; s--)
+    if (X >= off[s]) {
+      b.s = s;
+      if (pec[s]) { b.e = X - off[s]; b.c = 0; }
+      else { b.e = (X - off[s]) / 2; b.c = (X - off[s]) % 2; }
+      return b;
+    }
+  return b;
+}
+
+/* entry (R, C), R <= C, of the full matrix */
+static cplx entry_upper(int ns, ora_surface **S, const int *reg, const int *pec, const int *off, cplx omega,
+                        const double *eps, const double *mu, int R, int C)
+{
+  ora_bf a = bf_of(ns, pec, off, R), b = bf_of(ns, pec, off, C);
+  int sa = a.s, sb = b.s;
+  int cr[2], nc = 0; double sg[2];
+  const int *Ra = reg + 2*sa, *Rb = reg + 2*sb;
+  if (Ra[0] == Rb[0]) { cr[nc] = Ra[0]; sg[nc] = 1.0; nc++; }
+  else if (Ra[0] == Rb[1]) { cr[nc] = Ra[0]; sg[nc] = -1.0; nc++; }
+  if (Ra[1] == Rb[0] && Ra[1] >= 0) { cr[nc] = Ra[1]; sg[nc] = -1.0; nc++; }
+  else if (!pec[sa] && !pec[sb] && Ra[1] == Rb[1]) { cr[nc] = Ra[1]; sg[nc] = 1.0; nc++; }
+  int sym = (sa == sb);
+  int ca = a.c, cb = b.c;
+  /* inside a diagonal 2x2 block of one edge the (1,0) entry is never
+     stamped: it is the mirror of (0,1) */
+  if (sym && a.e == b.e && ca == 1 && cb == 0) { ca = 0; cb = 1; }
+  cplx v = 0.0;
+  for (int r = 0; r < nc; r++) {
+    cplx e = eps[2*cr[r]] + I*eps[2*cr[r]+1], m = mu[2*cr[r]] + I*mu[2*cr[r]+1];
+    cplx kk = csqrt2(e*m) * omega;
+    cplx PF1 = sg[r]*I*m*omega, PF2 = -sg[r]*I*kk, PF3 = -sg[r]*I*e*omega;
+    cplx GC[2];
+    ora_eei(S[sa], a.e, S[sb], b.e, kk, GC);
+    if (pec[sa] && pec[sb]) v += PF1*GC[0];
+    else if (pec[sa]) v += cb == 0 ? PF1*GC[0] : PF2*GC[1];
+    else if (pec[sb]) v += ca == 0 ? PF1*GC[0] : PF2*GC[1];
+    else if (ca == 0 && cb == 0) v += PF1*GC[0];
+    else if (ca == 1 && cb == 1) v += PF3*GC[0];
+    else v += PF2*GC[1];
+  }
+  return v;
+}
+
+void ora_assemble_cols(int ns, ora_surface **S, const int *reg, const int *pec,
+                       double wr, double wi, const double *eps, const double *mu,
+                       int ncols, const int *cols, double *Mout, int ldm)
+{
+  cplx omega = wr + I*wi;
+  cplx *M = (cplx *)Mout;
+  int off[64], N = 0;
+  for (int s = 0; s < ns; s++) { off[s] = N; N += pec[s] ? S[s]->ne : 2*S[s]->ne; }
+  for (int j = 0; j < ncols; j++) {
+    const int C = cols[j];
+    #pragma omp parallel for schedule(dynamic, 16)
+    for (int R = 0; R < N; R++)
+      M[R + (size_t)j*ldm] = R <= C ? entry_upper(ns, S, reg, pec, off, omega, eps, mu, R, C)
+                                    : entry_upper(ns, S, reg, pec, off, omega, eps, mu, C, R);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* The assembly loop of ora_assemble restricted to the column edges    */
+/* [eb0, eb1) of one single-surface geometry (every edge pair ea <= eb */
+/* with eb in the range, stamped into the full column-major M): the    */
+/* bounded slices the CPU baseline times.  Over a partition of        */
+/* [0, ne) the slices compute exactly ora_assemble's upper triangle.   */
+/* ------------------------------------------------------------------ */
+void ora_assemble_stripe(ora_surface *S, int reg_ext, int reg_int, int pec, double wr, double wi,
+                         const double *eps, const double *mu, int eb0, int eb1, double *Mout, int N)
+{
+  cplx omega = wr + I*wi;
+  cplx *M = (cplx *)Mout;
+  /* CountCommonRegions of a surface with itself: its exterior region, and
+     its interior one unless it is PEC (SurfaceSurfaceInteractions.cc:62-90) */
+  int cr[2], nc = 0; double sg[2];
+  cr[nc] = reg_ext; sg[nc] = 1.0; nc++;
+  if (!pec && reg_int >= 0) { cr[nc] = reg_int; sg[nc] = 1.0; nc++; }
+  cplx PF1[2], PF2[2], PF3[2], kk[2];
+  for (int r = 0; r < nc; r++) {
+    cplx e = eps[2*cr[r]] + I*eps[2*cr[r]+1], m = mu[2*cr[r]] + I*mu[2*cr[r]+1];
+    kk[r] = csqrt2(e*m) * omega;
+    PF1[r] = sg[r]*I*m*omega; PF2[r] = -sg[r]*I*kk[r]; PF3[r] = -sg[r]*I*e*omega;
+  }
+  #pragma omp parallel for schedule(dynamic, 4)
+  for (int ea = 0; ea < eb1; ea++)
+    for (int eb = ea > eb0 ? ea : eb0; eb < eb1; eb++)
+      for (int r = 0; r < nc; r++) {
+        cplx GC[2];
+        ora_eei(S, ea, S, eb, kk[r], GC);
+        if (pec) {
+          M[ea + (size_t)eb*N] += PF1[r]*GC[0];
+        } else {
+          size_t X = 2*ea, Y = 2*eb;
+          M[X + Y*N] += PF1[r]*GC[0];
+          M[X + (Y+1)*N] += PF2[r]*GC[1];
+          if (ea != eb) M[X+1 + Y*N] += PF2[r]*GC[1];
+          M[X+1 + (Y+1)*N] += PF3[r]*GC[0];
+        }
+      }
+}
+
+/* Fill a surface's memo of static near-pair integrals (the warm state of */
+/* the reference's FIPPI cache, FIPPICache.cc:135-187) for every ordered  */
+/* near pair the assembly of this surface looks up.                      */
+long long ora_warm_near(ora_surface *S)
+{
+  long long n = 0;
+  #pragma omp parallel for schedule(dynamic, 8) reduction(+:n)
+  for (int pa = 0; pa < S->np; pa++)
+    for (int pb = 0; pb < S->np; pb++) {
+      const double *Va[3], *Vb[3];
+      double rrel;
+      int ncv = assess_pair(S, pa, S, pb, &rrel, Va, Vb);
+      if (rrel > 4.0 || ncv == 3) continue;
+      cplx H[2];
+      ora_ppi(S, pa, 0, S, pb, 0, 1.0, H, 0);
+      n++;
+    }
+  return n;
+}

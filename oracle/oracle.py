@@ -25,7 +25,7 @@ def build():
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
     tmp = LIB + ".tmp"
-    subprocess.run(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-w", "-ffp-contract=off", "-o", tmp, SRC, "-lm"],
+    subprocess.run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-w", "-ffp-contract=off", "-o", tmp, SRC, "-lm"],
                    check=True)
     os.replace(tmp, LIB)
     return LIB
@@ -74,6 +74,10 @@ def lib():
         L.ora_set_orders.argtypes = [I, I, I, I, I]
         L.ora_assemble.argtypes = [I, P, P, P, D, D, P, P, P, I]
         L.ora_gc_matrix.argtypes = [P, D, D, P, P]
+        L.ora_assemble_cols.argtypes = [I, P, P, P, D, D, P, P, I, P, P, I]
+        L.ora_assemble_stripe.argtypes = [P, I, I, I, D, D, P, P, I, I, P, I]
+        L.ora_warm_near.argtypes = [P]
+        L.ora_warm_near.restype = ctypes.c_longlong
         _lib = L
     return _lib
 
@@ -163,6 +167,45 @@ def assemble(surfaces, regions, pec, omega, eps, mu):
     lib().ora_assemble(len(surfaces), handles, reg.ctypes.data, pe.ctypes.data, omega.real, omega.imag,
                        ep.ctypes.data, mm.ctypes.data, M.ctypes.data, N)
     return M
+
+
+def assemble_cols(surfaces, regions, pec, omega, eps, mu, cols):
+    """Whole columns ``cols`` (every row) of the matrix ``assemble`` returns,
+    equal to its columns entry for entry; for matrices too large to assemble
+    whole on the CPU.  Returns an N x len(cols) complex128 array."""
+    N = sum(s.edges()[0].shape[0] * (1 if p else 2) for s, p in zip(surfaces, pec))
+    handles = (ctypes.c_void_p * len(surfaces))(*[s.h for s in surfaces])
+    reg = np.array([r for pair in regions for r in pair], dtype=np.int32)
+    pe = np.array([1 if p else 0 for p in pec], dtype=np.int32)
+    ep = np.array([[complex(e).real, complex(e).imag] for e in eps], dtype=np.float64).ravel()
+    mm = np.array([[complex(m).real, complex(m).imag] for m in mu], dtype=np.float64).ravel()
+    cl = np.ascontiguousarray(cols, dtype=np.int32)
+    if cl.size and (cl.min() < 0 or cl.max() >= N):
+        raise ValueError("column index out of range")
+    M = np.zeros((N, len(cl)), dtype=np.complex128, order="F")
+    omega = complex(omega)
+    lib().ora_assemble_cols(len(surfaces), handles, reg.ctypes.data, pe.ctypes.data, omega.real, omega.imag,
+                            ep.ctypes.data, mm.ctypes.data, len(cl), cl.ctypes.data, M.ctypes.data, N)
+    return M
+
+
+def assemble_stripe(surface, pec, omega, eps, mu, eb0, eb1, M):
+    """ora_assemble's loop over the column edges [eb0, eb1) of a
+    single-surface geometry (exterior region 0, interior region 1 unless
+    PEC), added into the full N x N complex128 column-major M: the upper
+    triangle of those columns."""
+    ep = np.array([[complex(e).real, complex(e).imag] for e in eps], dtype=np.float64).ravel()
+    mm = np.array([[complex(m).real, complex(m).imag] for m in mu], dtype=np.float64).ravel()
+    assert M.dtype == np.complex128 and M.flags.f_contiguous
+    omega = complex(omega)
+    lib().ora_assemble_stripe(surface.h, 0, -1 if pec else 1, 1 if pec else 0, omega.real, omega.imag,
+                              ep.ctypes.data, mm.ctypes.data, int(eb0), int(eb1), M.ctypes.data, M.shape[0])
+
+
+def warm_near(surface):
+    """Compute and memoise the static near-pair integrals of every near pair
+    of a surface (the warm state of the reference's FIPPI cache)."""
+    return lib().ora_warm_near(surface.h)
 
 
 def set_orders(td3=32, td2=20, td1=14, fip0=24, fip12=16):

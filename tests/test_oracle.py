@@ -152,3 +152,38 @@ def test_mie_oracle_against_reference_tables():
                 assert abs(a) < 1e-20
             else:
                 assert abs(a - pabs) < 1e-6 * pabs, (name, w, a, pabs)
+
+
+def test_column_assembly_equals_full_assembly():
+    """oracle.assemble_cols (whole columns of matrices too large to assemble
+    on the CPU) gives the columns of oracle.assemble entry for entry: a
+    dielectric sphere, a PEC sphere, and a PEC + dielectric pair (mixed 1x1 /
+    2x2 stamping, mirrored blocks)."""
+    from gbem import mesh
+    V, P = mesh.icosphere(1)
+    S = ora.Surface(V, P)
+    S2 = ora.Surface(V + [0.0, 0.0, 3.0], P)
+    cases = [([S], [(0, 1)], [False], 2.0, [1.0, 2.25 + 0.01j], [1.0, 1.0]),
+             ([S], [(0, -1)], [True], 1.0, [1.0], [1.0]),
+             ([S, S2], [(0, -1), (0, 1)], [True, False], 1.5, [1.0, 4 + 0.1j], [1.0, 1.0])]
+    for args in cases:
+        M = ora.assemble(*args)
+        cols = [0, 1, 2, 17, 61, M.shape[0] // 2, M.shape[0] - 1]
+        assert np.array_equal(ora.assemble_cols(*args, cols), M[:, cols])
+
+
+def test_stripe_assembly_equals_upper_triangle():
+    """oracle.assemble_stripe over a partition of the column edges gives the
+    upper triangle of oracle.assemble (the slices the CPU baseline times)."""
+    from gbem import mesh
+    V, P = mesh.icosphere(1)
+    S = ora.Surface(V, P)
+    for pec in (False, True):
+        eps = [1.0] if pec else [1.0, 2.25 + 0.01j]
+        mu = [1.0] * len(eps)
+        M = ora.assemble([S], [(0, -1 if pec else 1)], [pec], 2.0, eps, mu)
+        ne = S.edges()[0].shape[0]
+        Ms = np.zeros_like(M, order="F")
+        for a, b in ((0, 7), (7, 40), (40, ne)):
+            ora.assemble_stripe(S, pec, 2.0, eps, mu, a, b, Ms)
+        assert np.array_equal(np.triu(Ms), np.triu(M))
