@@ -187,6 +187,13 @@ gbem_status gbem_lu_solve(gbem_matrix *M, char trans, int nrhs, void *B, int ldb
 gbem_status gbem_lu_trace(gbem_matrix *M, const gbem_matrix *B, int ncols, double *trace);
 gbem_status gbem_lu_trace_host(gbem_matrix *M, const void *B, int ldb, int ncols, double *trace);
 
+/* log|det M| of a factored M (gbem_lu_factor): the sum of log|U(n,n)| over
+ * the diagonal of its LU factor, the quantity GetLNDetMInvMInf sums from the
+ * factors of M and of its diagonal T blocks for the Casimir energy
+ * integrand (applications/scuff-cas3D/CasimirIntegrand.cc:50-63); -inf if a
+ * pivot is exactly zero. */
+gbem_status gbem_lu_log_abs_det(gbem_matrix *M, double *logdet);
+
 /* gbem_lu_solve without any device allocation.  No counterpart in the
  * reference (HMatrix::LUSolve runs LAPACK on host memory).  Same arguments
  * and results as gbem_lu_solve for complex128 and complex64 matrices; a real

@@ -302,20 +302,63 @@ struct RegionArgs {
 // ---------------------------------------------------------------------------
 // static near-pair table (once per geometry)
 // ---------------------------------------------------------------------------
-__global__ void fippi_kernel(const DevNear* near, const int* list, int n, const double* pv, Fippi* out) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  int i = list[t];
-  DevNear d = near[i];
+// One warp per near pair: the pair's cubature points are dealt to the lanes
+// (lane l takes points l, l + 32, ...), each lane keeps its 33 partial sums
+// in registers, and a shuffle reduction forms the pair's table entry.  The
+// rule sits in shared memory (lanes read different nodes at once).
+constexpr int FIPPI_THREADS = 128;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(FIPPI_THREADS) fippi_kernel(const DevNear* near, const int* list, int n,
+                                                               const double* pv, Fippi* out) {
+  __shared__ double sgx[N_FIP], sgw[N_FIP];
+  if (threadIdx.x < N_FIP) { sgx[threadIdx.x] = c_gx12[threadIdx.x]; sgw[threadIdx.x] = c_gw12[threadIdx.x]; }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (w >= n) return;  // whole warps
+  const int i = list[w];
+  const DevNear d = near[i];
   double Va[9], Vb[9];
+#pragma unroll
   for (int c = 0; c < 9; c++) { Va[c] = pv[9 * (size_t)d.pa + c]; Vb[c] = pv[9 * (size_t)d.pb + c]; }
   Fippi F;
+  fippi_zero(&F);
   if (d.ncv == 0) {
-    fippi_far(Va, Vb, c_gx12, c_gw12, N_FIP, &F);
+    double A[3], B[3], Ap[3], Bp[3], dV[3], a2;
+    fippi_far_setup(Va, Vb, A, B, Ap, Bp, dV, &a2);
+    for (int q = lane; q < N_FIP * N_FIP * N_FIP; q += 32) {
+      const int i1 = q / (N_FIP * N_FIP), j = (q / N_FIP) % N_FIP, l = q % N_FIP;
+      const double u = sgx[i1];
+      fippi_far_acc(A, B, Ap, Bp, dV, a2, u, u * sgx[j], sgx[l], sgw[i1] * sgw[j] * sgw[l] * u, F);
+    }
   } else {
-    fippi_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, c_gx12, c_gw12, N_FIP, &F);
+    double Ea[9], Eb[9];
+    touch_edges(Va, Vb, d.perm_a, d.perm_b, Ea, Eb);
+    const int np = duffy_npts(d.ncv, N_FIP);
+    DuffyPt pt;
+    for (int q = lane; q < np; q += 32) {
+      duffy_pt(d.ncv, q, sgx, sgw, N_FIP, pt);
+      fippi_touch_acc(Ea, Eb, d.perm_a, d.perm_b, Va, pt, F);
+    }
   }
-  out[i] = F;
+#pragma unroll
+  for (int m = 0; m < 9; m++) {
+    F.RM1[m] = warp_sum(F.RM1[m]);
+    F.R1[m] = warp_sum(F.R1[m]);
+    F.R2[m] = warp_sum(F.R2[m]);
+  }
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    F.XM[m] = warp_sum(F.XM[m]);
+    F.XX[m] = warp_sum(F.XX[m]);
+  }
+  if (lane == 0) out[i] = F;
 }
 
 // ---------------------------------------------------------------------------
@@ -990,7 +1033,8 @@ gbem_status compute_fippi(Geometry* g, cudaStream_t s) {
       n = (int)miss.size();
     }
     if (n > 0) {
-      fippi_kernel<<<(n + 63) / 64, 64, 0, s>>>(db->near, list, n, g->d_pv, db->fippi);
+      fippi_kernel<<<(unsigned)(((long long)n * 32 + FIPPI_THREADS - 1) / FIPPI_THREADS), FIPPI_THREADS, 0, s>>>(
+          db->near, list, n, g->d_pv, db->fippi);
       stats_launch(ST_NEAR);
     }
     cudaError_t e = cudaGetLastError();

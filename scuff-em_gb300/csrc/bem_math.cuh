@@ -468,44 +468,59 @@ GB_HD void fippi_zero(Fippi* F) {
 
 // Non-touching near pair: v' integrated in closed form, (u, v/u, u') by a
 // tensor Gauss-Legendre rule (the 3-D scheme of QIFIPPICubature.cc:187-325).
-// Va, Vb: 9 doubles each, mesh vertex order.
-GB_HD void fippi_far(const double* Va, const double* Vb, const double* gx, const double* gw, int n, Fippi* F) {
-  double A[3], B[3], Ap[3], Bp[3];
+// Va, Vb: 9 doubles each, mesh vertex order.  fippi_far_acc adds one point
+// (u, v = u t, u') of weight W; A, B, Ap, Bp are the panels' edge vectors,
+// dV = V0b - V0a, a2 = |Bp|^2.
+GB_HD void fippi_far_acc(const double* A, const double* B, const double* Ap, const double* Bp, const double* dV,
+                         double a2, double u, double v, double up, double W, Fippi& F) {
+  double Y[3], Xo[3], Zo[3];
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    Xo[m] = u * A[m] + v * B[m];   // x - V0a
+    Zo[m] = dV[m] + up * Ap[m];    // z - V0a
+    Y[m] = Xo[m] - Zo[m];
+  }
+  double v0 = vdot(Bp, Y) / a2;
+  double b2 = vdot(Y, Y) / a2 - v0 * v0;
+  if (b2 < 0) b2 = 0;
+  double J[4][2];
+  seg_integrals(a2, v0, b2, up, J);
+#pragma unroll
+  for (int m = 0; m < 3; m++) F.XM[m] += W * (Y[m] * J[0][0] - Bp[m] * J[0][1]);
+  double XZ[3], XB[3];
+  vcross(Xo, Zo, XZ); vcross(Xo, Bp, XB);
+#pragma unroll
+  for (int m = 0; m < 3; m++) F.XX[m] += W * (XZ[m] * J[0][0] + XB[m] * J[0][1]);
+  // TCR a-side monomials {1, u - v, v}; b-side {1, u' - v', v'}
+  const double ma[3] = {1.0, u - v, v};
+#pragma unroll
+  for (int al = 0; al < 3; al++) {
+    double f = W * ma[al];
+    F.RM1[3 * al + 0] += f * J[1][0]; F.RM1[3 * al + 1] += f * (up * J[1][0] - J[1][1]); F.RM1[3 * al + 2] += f * J[1][1];
+    F.R1[3 * al + 0] += f * J[2][0];  F.R1[3 * al + 1] += f * (up * J[2][0] - J[2][1]);  F.R1[3 * al + 2] += f * J[2][1];
+    F.R2[3 * al + 0] += f * J[3][0];  F.R2[3 * al + 1] += f * (up * J[3][0] - J[3][1]);  F.R2[3 * al + 2] += f * J[3][1];
+  }
+}
+
+GB_HD void fippi_far_setup(const double* Va, const double* Vb, double* A, double* B, double* Ap, double* Bp, double* dV,
+                           double* a2) {
   for (int i = 0; i < 3; i++) {
     A[i] = Va[3 + i] - Va[i]; B[i] = Va[6 + i] - Va[3 + i];
     Ap[i] = Vb[3 + i] - Vb[i]; Bp[i] = Vb[6 + i] - Vb[3 + i];
+    dV[i] = Vb[i] - Va[i];
   }
-  double a2 = vdot(Bp, Bp);
+  *a2 = vdot(Bp, Bp);
+}
+
+GB_HD void fippi_far(const double* Va, const double* Vb, const double* gx, const double* gw, int n, Fippi* F) {
+  double A[3], B[3], Ap[3], Bp[3], dV[3], a2;
+  fippi_far_setup(Va, Vb, A, B, Ap, Bp, dV, &a2);
   fippi_zero(F);
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++)
       for (int l = 0; l < n; l++) {
-        double u = gx[i], v = u * gx[j], up = gx[l];
-        double W = gw[i] * gw[j] * gw[l] * u;
-        double X[3], Z[3], Y[3], Xo[3], Zo[3];
-        for (int m = 0; m < 3; m++) {
-          Xo[m] = u * A[m] + v * B[m];                 // x - V0a
-          Zo[m] = (Vb[m] - Va[m]) + up * Ap[m];        // z - V0a
-          X[m] = Xo[m]; Z[m] = Zo[m];
-          Y[m] = X[m] - Z[m];
-        }
-        double v0 = vdot(Bp, Y) / a2;
-        double b2 = vdot(Y, Y) / a2 - v0 * v0;
-        if (b2 < 0) b2 = 0;
-        double J[4][2];
-        seg_integrals(a2, v0, b2, up, J);
-        for (int m = 0; m < 3; m++) F->XM[m] += W * (Y[m] * J[0][0] - Bp[m] * J[0][1]);
-        double XZ[3], XB[3];
-        vcross(Xo, Zo, XZ); vcross(Xo, Bp, XB);
-        for (int m = 0; m < 3; m++) F->XX[m] += W * (XZ[m] * J[0][0] + XB[m] * J[0][1]);
-        // TCR a-side monomials {1, u - v, v}; b-side {1, u' - v', v'}
-        double ma[3] = {1.0, u - v, v};
-        for (int al = 0; al < 3; al++) {
-          double f = W * ma[al];
-          F->RM1[3 * al + 0] += f * J[1][0]; F->RM1[3 * al + 1] += f * (up * J[1][0] - J[1][1]); F->RM1[3 * al + 2] += f * J[1][1];
-          F->R1[3 * al + 0] += f * J[2][0];  F->R1[3 * al + 1] += f * (up * J[2][0] - J[2][1]);  F->R1[3 * al + 2] += f * J[2][1];
-          F->R2[3 * al + 0] += f * J[3][0];  F->R2[3 * al + 1] += f * (up * J[3][0] - J[3][1]);  F->R2[3 * al + 2] += f * J[3][1];
-        }
+        double u = gx[i];
+        fippi_far_acc(A, B, Ap, Bp, dV, a2, u, u * gx[j], gx[l], gw[i] * gw[j] * gw[l] * u, *F);
       }
 }
 
@@ -537,96 +552,118 @@ GB_HD void tcr_from_edge(const int* perm, const double* s0, const double* s1, rp
   *v = rp_aff(v0, v1);
 }
 
-GB_HD_NOINLINE void fippi_touch_point(const double* Ea, const double* Eb, const int* pa, const int* pb,
-                                      const double* V0a, const DuffyPt& pt, Fippi* F) {
+// Duffy point q of a touching pair's cells (ncv = 1: 2 n^3 points, ncv = 2:
+// 8 n^2 points), in the order fippi_touch and td_touch walk them.
+GB_HD int duffy_npts(int ncv, int n) { return ncv == 1 ? 2 * n * n * n : 8 * n * n; }
+
+GB_HD void duffy_pt(int ncv, int q, const double* gx, const double* gw, int n, DuffyPt& pt) {
+  if (ncv == 1) {
+    const int reg = q / (n * n * n), rem = q % (n * n * n);
+    const int i1 = rem / (n * n), i2 = (rem / n) % n, i3 = rem % n;
+    const double al = gx[i1], be = gx[i2], ga = gx[i3];
+    pt.sa0[0] = pt.sa0[1] = pt.sb0[0] = pt.sb0[1] = 0.0;
+    if (reg == 0) { pt.sa1[0] = 1.0; pt.sa1[1] = al; pt.sb1[0] = be; pt.sb1[1] = be * ga; }
+    else { pt.sb1[0] = 1.0; pt.sb1[1] = al; pt.sa1[0] = be; pt.sa1[1] = be * ga; }
+    pt.om = rp_aff(0.0, 0.0); pt.om.c[3] = be;
+    pt.W = gw[i1] * gw[i2] * gw[i3];
+  } else {
+    const double tx[2] = {0.21132486540518711775, 0.78867513459481288225};
+    const int reg = q / (2 * n * n), rem = q % (2 * n * n);
+    const int ia = rem / (2 * n), ib = (rem / 2) % n, it = rem % 2;
+    const double al = gx[ia], be = gx[ib];
+    double z[3], J, lo;
+    if (reg == 0) { z[0] = 1.0 - al; z[1] = be; z[2] = al; J = 1.0; lo = al; }
+    else if (reg == 1) { z[0] = al; z[1] = 1.0; z[2] = (1.0 - al) * be; J = 1.0 - al; lo = 1.0 - al; }
+    else if (reg == 2) { z[0] = -al; z[1] = (1.0 - al) * be; z[2] = 1.0; J = 1.0 - al; lo = 1.0; }
+    else { z[0] = -al; z[1] = 1.0 - al; z[2] = be; J = 1.0; lo = 1.0; }
+    const double tau = tx[it];
+    pt.sb0[0] = tau; pt.sb1[0] = lo - tau;
+    pt.sb0[1] = 0.0; pt.sb1[1] = z[2];
+    pt.sa0[0] = tau; pt.sa1[0] = lo - tau + z[0];
+    pt.sa0[1] = 0.0; pt.sa1[1] = z[1];
+    pt.om = rp_aff(0.0, 0.0); pt.om.c[2] = 1.0; pt.om.c[3] = -1.0;
+    pt.W = gw[ia] * gw[ib] * 0.5 * J;
+  }
+}
+
+// One Duffy point of a touching pair's static integrals.  The cells'
+// Jacobian is om(w) = o2 w^2 + o3 w^3 (o2 = 0, o3 = beta for one common
+// vertex; o2 = 1, o3 = -1 for a common edge) and the monomials are affine in
+// w, so every radial integral int_0^1 om(w) w^e dw is the short closed sum
+// h(e) = o2 / (e+3) + o3 / (e+4) over the powers of the monomial product.
+GB_HD void fippi_touch_acc(const double* Ea, const double* Eb, const int* pa, const int* pb, const double* V0a,
+                           const DuffyPt& pt, Fippi& F) {
   double A[3], B[3], Ap[3], Bp[3], D[3];
+#pragma unroll
   for (int i = 0; i < 3; i++) {
     A[i] = Ea[3 + i] - Ea[i]; B[i] = Ea[6 + i] - Ea[3 + i];
     Ap[i] = Eb[3 + i] - Eb[i]; Bp[i] = Eb[6 + i] - Eb[3 + i];
     D[i] = pt.sa1[0] * A[i] + pt.sa1[1] * B[i] - pt.sb1[0] * Ap[i] - pt.sb1[1] * Bp[i];
   }
-  double X = sqrt(vdot(D, D));
+  const double X = sqrt(vdot(D, D));
+  const double o2 = pt.om.c[2], o3 = pt.om.c[3];
   rpoly ua, va, ub, vb;
   tcr_from_edge(pa, pt.sa0, pt.sa1, &ua, &va);
   tcr_from_edge(pb, pt.sb0, pt.sb1, &ub, &vb);
-  rpoly one = rp_aff(1.0, 0.0);
-  const rpoly ma[3] = {one, ua, va}, mb[3] = {one, ub, vb};
+  const double a0[3] = {1.0, ua.c[0], va.c[0]}, a1[3] = {0.0, ua.c[1], va.c[1]};
+  const double b0[3] = {1.0, ub.c[0], vb.c[0]}, b1[3] = {0.0, ub.c[1], vb.c[1]};
+  // the monomial product m0 + m1 w + m2 w^2 meets w^-1 (r^-1), w (r), w^2 (r^2)
+  constexpr double inv[9] = {0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 1.0 / 7, 1.0 / 8};
+  auto h = [&](int e) { return o2 * inv[e + 2] + o3 * inv[e + 3]; };
+  const double hm1[3] = {h(0), h(1), h(2)};   // r^-1
+  const double h1[3] = {h(2), h(3), h(4)};    // r
+  const double h2[3] = {h(3), h(4), h(5)};    // r^2
+  const double iX = 1.0 / X;
+  const double WX = pt.W * X, WXX = pt.W * X * X, WoX = pt.W * iX;
+#pragma unroll
   for (int al = 0; al < 3; al++)
+#pragma unroll
     for (int be = 0; be < 3; be++) {
-      rpoly q = rp_mul(pt.om, rp_mul(ma[al], mb[be]));
-      double sm1 = 0, s1 = 0, s2 = 0;
-      for (int n = 1; n < 8; n++) {
-        sm1 += q.c[n] / n;
-        s1 += q.c[n] / (n + 2.0);
-        s2 += q.c[n] / (n + 3.0);
-      }
-      F->RM1[3 * al + be] += pt.W * sm1 / X;
-      F->R1[3 * al + be] += pt.W * s1 * X;
-      F->R2[3 * al + be] += pt.W * s2 * X * X;
+      const double m0 = a0[al] * b0[be], m1 = a0[al] * b1[be] + a1[al] * b0[be], m2 = a1[al] * b1[be];
+      F.RM1[3 * al + be] += WoX * (m0 * hm1[0] + m1 * hm1[1] + m2 * hm1[2]);
+      F.R1[3 * al + be] += WX * (m0 * h1[0] + m1 * h1[1] + m2 * h1[2]);
+      F.R2[3 * al + be] += WXX * (m0 * h2[0] + m1 * h2[1] + m2 * h2[2]);
     }
-  double om2 = 0;
-  for (int n = 2; n < 8; n++) om2 += pt.om.c[n] / (n - 1.0);
-  double X3 = X * X * X;
-  for (int m = 0; m < 3; m++) F->XM[m] += pt.W * om2 * D[m] / X3;
-  // xi(w) = x(w) - V0a; (xi x xi')/r^3 -> -(xi(w) x D) w / (w^3 X^3)
-  rpoly xi[3];
-  for (int m = 0; m < 3; m++)
-    xi[m] = rp_aff(Ea[m] - V0a[m] + pt.sa0[0] * A[m] + pt.sa0[1] * B[m], pt.sa1[0] * A[m] + pt.sa1[1] * B[m]);
+  // (x - x')/r^3 = D / (w^2 X^3): int om w^-2 = o2 + o3 / 2
+  const double iX3 = iX * iX * iX;
+  const double om2 = o2 + 0.5 * o3;
+#pragma unroll
+  for (int m = 0; m < 3; m++) F.XM[m] += pt.W * om2 * D[m] * iX3;
+  // xi(w) = x(w) - V0a = c0 + c1 w; (xi x xi')/r^3 -> -(xi(w) x D) w / (w^3 X^3):
+  // int om (c0 + c1 w) w^-2 dw = c0 (o2 + o3/2) + c1 (o2/2 + o3/3)
+  const double g0 = om2, g1 = 0.5 * o2 + o3 / 3.0;
+  double c0[3], c1[3];
+#pragma unroll
   for (int m = 0; m < 3; m++) {
-    int m1 = (m + 1) % 3, m2 = (m + 2) % 3;
-    rpoly cxm;
-    for (int i = 0; i < 8; i++) cxm.c[i] = xi[m1].c[i] * D[m2] - xi[m2].c[i] * D[m1];
-    rpoly q = rp_mul(pt.om, cxm);
-    double s = 0;
-    for (int n = 2; n < 8; n++) s += q.c[n] / (n - 1.0);
-    F->XX[m] += -pt.W * s / X3;
+    c0[m] = Ea[m] - V0a[m] + pt.sa0[0] * A[m] + pt.sa0[1] * B[m];
+    c1[m] = pt.sa1[0] * A[m] + pt.sa1[1] * B[m];
+  }
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    const int m1 = (m + 1) % 3, m2 = (m + 2) % 3;
+    const double x0 = c0[m1] * D[m2] - c0[m2] * D[m1], x1 = c1[m1] * D[m2] - c1[m2] * D[m1];
+    F.XX[m] += -pt.W * (x0 * g0 + x1 * g1) * iX3;
   }
 }
 
-GB_HD void fippi_touch(int ncv, const double* Va, const double* Vb, const int* pa, const int* pb, const double* gx,
-                       const double* gw, int n, Fippi* F) {
-  double Ea[9], Eb[9];
+GB_HD void touch_edges(const double* Va, const double* Vb, const int* pa, const int* pb, double* Ea, double* Eb) {
   for (int i = 0; i < 3; i++)
     for (int c = 0; c < 3; c++) {
       Ea[3 * i + c] = pa[i] == 0 ? Va[c] : (pa[i] == 1 ? Va[3 + c] : Va[6 + c]);
       Eb[3 * i + c] = pb[i] == 0 ? Vb[c] : (pb[i] == 1 ? Vb[3 + c] : Vb[6 + c]);
     }
+}
+
+GB_HD void fippi_touch(int ncv, const double* Va, const double* Vb, const int* pa, const int* pb, const double* gx,
+                       const double* gw, int n, Fippi* F) {
+  double Ea[9], Eb[9];
+  touch_edges(Va, Vb, pa, pb, Ea, Eb);
   fippi_zero(F);
   DuffyPt pt;
-  if (ncv == 1) {
-    for (int reg = 0; reg < 2; reg++)
-      for (int i1 = 0; i1 < n; i1++)
-        for (int i2 = 0; i2 < n; i2++)
-          for (int i3 = 0; i3 < n; i3++) {
-            double al = gx[i1], be = gx[i2], ga = gx[i3];
-            pt.sa0[0] = pt.sa0[1] = pt.sb0[0] = pt.sb0[1] = 0.0;
-            if (reg == 0) { pt.sa1[0] = 1.0; pt.sa1[1] = al; pt.sb1[0] = be; pt.sb1[1] = be * ga; }
-            else { pt.sb1[0] = 1.0; pt.sb1[1] = al; pt.sa1[0] = be; pt.sa1[1] = be * ga; }
-            pt.om = rp_aff(0.0, 0.0); pt.om.c[3] = be;
-            pt.W = gw[i1] * gw[i2] * gw[i3];
-            fippi_touch_point(Ea, Eb, pa, pb, Va, pt, F);
-          }
-  } else {
-    const double tx[2] = {0.21132486540518711775, 0.78867513459481288225};
-    for (int reg = 0; reg < 4; reg++)
-      for (int ia = 0; ia < n; ia++)
-        for (int ib = 0; ib < n; ib++) {
-          double al = gx[ia], be = gx[ib], z[3], J, lo;
-          if (reg == 0) { z[0] = 1.0 - al; z[1] = be; z[2] = al; J = 1.0; lo = al; }
-          else if (reg == 1) { z[0] = al; z[1] = 1.0; z[2] = (1.0 - al) * be; J = 1.0 - al; lo = 1.0 - al; }
-          else if (reg == 2) { z[0] = -al; z[1] = (1.0 - al) * be; z[2] = 1.0; J = 1.0 - al; lo = 1.0; }
-          else { z[0] = -al; z[1] = 1.0 - al; z[2] = be; J = 1.0; lo = 1.0; }
-          for (int it = 0; it < 2; it++) {
-            double tau = tx[it];
-            pt.sb0[0] = tau; pt.sb1[0] = lo - tau;
-            pt.sb0[1] = 0.0; pt.sb1[1] = z[2];
-            pt.sa0[0] = tau; pt.sa1[0] = lo - tau + z[0];
-            pt.sa0[1] = 0.0; pt.sa1[1] = z[1];
-            pt.om = rp_aff(0.0, 0.0); pt.om.c[2] = 1.0; pt.om.c[3] = -1.0;
-            pt.W = gw[ia] * gw[ib] * 0.5 * J;
-            fippi_touch_point(Ea, Eb, pa, pb, Va, pt, F);
-          }
-        }
+  const int np = duffy_npts(ncv, n);
+  for (int q = 0; q < np; q++) {
+    duffy_pt(ncv, q, gx, gw, n, pt);
+    fippi_touch_acc(Ea, Eb, pa, pb, Va, pt, *F);
   }
 }
 
@@ -704,48 +741,18 @@ GB_HD_NOINLINE void td_touch_point(const double* Ea, const double* Eb, const int
 
 // Duffy cells of fippi_touch with the full kernel (ncv = 1 or 2); pt index
 // range [p0, npts) in steps of pstride lets a warp split the points.
-GB_HD int td_touch_npts(int ncv, int n) { return ncv == 1 ? 2 * n * n * n : 8 * n * n; }
+GB_HD int td_touch_npts(int ncv, int n) { return duffy_npts(ncv, n); }
 
 GB_HD void td_touch(int ncv, const double* Va, const double* Vb, const int* pa, const int* pb, cx<double> k,
                     const double* gx, const double* gw, int n, int p0, int pstride, cx<double>* MG, cx<double>* T) {
   double Ea[9], Eb[9];
-  for (int i = 0; i < 3; i++)
-    for (int c = 0; c < 3; c++) {
-      Ea[3 * i + c] = pa[i] == 0 ? Va[c] : (pa[i] == 1 ? Va[3 + c] : Va[6 + c]);
-      Eb[3 * i + c] = pb[i] == 0 ? Vb[c] : (pb[i] == 1 ? Vb[3 + c] : Vb[6 + c]);
-    }
+  touch_edges(Va, Vb, pa, pb, Ea, Eb);
   for (int m = 0; m < 9; m++) MG[m] = mk(0.0, 0.0);
   for (int m = 0; m < 10; m++) T[m] = mk(0.0, 0.0);
   const int np = td_touch_npts(ncv, n);
   DuffyPt pt;
   for (int q = p0; q < np; q += pstride) {
-    if (ncv == 1) {
-      const int reg = q / (n * n * n), rem = q % (n * n * n);
-      const int i1 = rem / (n * n), i2 = (rem / n) % n, i3 = rem % n;
-      const double al = gx[i1], be = gx[i2], ga = gx[i3];
-      pt.sa0[0] = pt.sa0[1] = pt.sb0[0] = pt.sb0[1] = 0.0;
-      if (reg == 0) { pt.sa1[0] = 1.0; pt.sa1[1] = al; pt.sb1[0] = be; pt.sb1[1] = be * ga; }
-      else { pt.sb1[0] = 1.0; pt.sb1[1] = al; pt.sa1[0] = be; pt.sa1[1] = be * ga; }
-      pt.om = rp_aff(0.0, 0.0); pt.om.c[3] = be;
-      pt.W = gw[i1] * gw[i2] * gw[i3];
-    } else {
-      const double tx[2] = {0.21132486540518711775, 0.78867513459481288225};
-      const int reg = q / (2 * n * n), rem = q % (2 * n * n);
-      const int ia = rem / (2 * n), ib = (rem / 2) % n, it = rem % 2;
-      const double al = gx[ia], be = gx[ib];
-      double z[3], J, lo;
-      if (reg == 0) { z[0] = 1.0 - al; z[1] = be; z[2] = al; J = 1.0; lo = al; }
-      else if (reg == 1) { z[0] = al; z[1] = 1.0; z[2] = (1.0 - al) * be; J = 1.0 - al; lo = 1.0 - al; }
-      else if (reg == 2) { z[0] = -al; z[1] = (1.0 - al) * be; z[2] = 1.0; J = 1.0 - al; lo = 1.0; }
-      else { z[0] = -al; z[1] = 1.0 - al; z[2] = be; J = 1.0; lo = 1.0; }
-      const double tau = tx[it];
-      pt.sb0[0] = tau; pt.sb1[0] = lo - tau;
-      pt.sb0[1] = 0.0; pt.sb1[1] = z[2];
-      pt.sa0[0] = tau; pt.sa1[0] = lo - tau + z[0];
-      pt.sa0[1] = 0.0; pt.sa1[1] = z[1];
-      pt.om = rp_aff(0.0, 0.0); pt.om.c[2] = 1.0; pt.om.c[3] = -1.0;
-      pt.W = gw[ia] * gw[ib] * 0.5 * J;
-    }
+    duffy_pt(ncv, q, gx, gw, n, pt);
     td_touch_point(Ea, Eb, pa, pb, Va, Vb, k, pt, MG, T);
   }
 }

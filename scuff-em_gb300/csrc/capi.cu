@@ -182,6 +182,28 @@ static __global__ void trace_diag(const cx<T>* X, long long ldx, int n, double* 
   if (threadIdx.x == 0) { out[0] = sr[0]; out[1] = si[0]; }
 }
 
+// sum of log|U(n,n)| over the diagonal of an LU factor; complex entries by
+// their modulus
+template <typename T>
+static __global__ void log_abs_diag(const T* A, long long ld, int n, int cplx, double* out) {
+  __shared__ double sr[1024];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const long long o = (long long)i * (ld + 1);
+    double m;
+    if (cplx) m = hypot((double)A[2 * o], (double)A[2 * o + 1]);
+    else m = fabs((double)A[o]);
+    acc += log(m);
+  }
+  sr[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sr[threadIdx.x] += sr[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sr[0];
+}
+
 }  // namespace gbem
 
 extern "C" {
@@ -839,6 +861,24 @@ gbem_status gbem_lu_trace(gbem_matrix* M, const gbem_matrix* B, int ncols, doubl
 
 gbem_status gbem_lu_trace_host(gbem_matrix* M, const void* B, int ldb, int ncols, double* trace) {
   return trace_impl(M, B, ldb, ncols, true, trace);
+}
+
+gbem_status gbem_lu_log_abs_det(gbem_matrix* M, double* logdet) {
+  if (!M || !logdet) { set_error("gbem_lu_log_abs_det: NULL argument"); return GBEM_EINVAL; }
+  if (!M->factored) { set_error("gbem_lu_log_abs_det: matrix is not factored"); return GBEM_EINVAL; }
+  CHECK_CUDA(cudaSetDevice(M->g->device), "cudaSetDevice");
+  cudaStream_t s = M->stream;
+  double* d_out = nullptr;
+  CHECK_CUDA(cudaMallocAsync((void**)&d_out, sizeof(double), s), "gbem_lu_log_abs_det alloc");
+  if (M->dtype == GBEM_C64) log_abs_diag<float><<<1, 1024, 0, s>>>((const float*)M->d, M->ld, M->N, 1, d_out);
+  else log_abs_diag<double><<<1, 1024, 0, s>>>((const double*)M->d, M->ld, M->N, M->dtype == GBEM_C128, d_out);
+  stats_launch(ST_OTHER);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(logdet, d_out, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d_out, s);
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = e2;
+  return e == cudaSuccess ? GBEM_OK : cuda_status(e, "gbem_lu_log_abs_det");
 }
 
 gbem_status gbem_lu_solve_noalloc(gbem_matrix* M, char trans, int nrhs, void* B, int ldb) {

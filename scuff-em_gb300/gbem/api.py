@@ -104,6 +104,13 @@ class HMatrix:
         self.ipiv, self.info = ipiv, info.value
         return info.value
 
+    def LogAbsDet(self):
+        """log|det M| of this factored matrix: sum of log|U(n,n)| over its LU
+        factor's diagonal (GetLNDetMInvMInf, CasimirIntegrand.cc:50-63)."""
+        v = ctypes.c_double()
+        check(lib().gbem_lu_log_abs_det(self._h, ctypes.byref(v)))
+        return v.value
+
     def TraceMInvdM(self, dM, ncols=None):
         """Tr over the first ncols diagonal entries of M^-1 dM for this
         factored matrix and dM (an HMatrix of the same size and type, or an
@@ -160,6 +167,7 @@ class RWGGeometry:
         n = ctypes.c_int()
         check(lib().gbem_geometry_num_bfs(h, ctypes.byref(n)))
         self.TotalBFs = n.value
+        self.np_total = int(sum(len(np.asarray(d["P"])) for d in surfaces))
 
     @classmethod
     def from_scuffgeo(cls, path, device=0):

@@ -45,6 +45,7 @@ from gbem.mesh import icosphere, read_msh, write_msh  # noqa: E402
 from oracle import oracle  # noqa: E402
 
 REFDUMP = os.path.join(REPO, "oracle", "_ref", "refdump")
+CAS3D = os.path.join(REPO, "oracle", "_ref", "scuff-cas3D")
 
 
 def run(args, cwd):
@@ -273,11 +274,43 @@ def cache_fixture(tmp):
     np.savez_compressed(os.path.join(HERE, "ref_fippi_cache_s1_mesh.npz"), V=V, P=P)
 
 
+def casimir_fixture(tmp):
+    """The reference's own Casimir integrand (scuff-cas3D, unchanged:
+    GetCasimirIntegrand, applications/scuff-cas3D/CasimirIntegrand.cc:243-480)
+    for two PEC icospheres (subdivision 3, radius 1, centres 3 apart) at the
+    20 Gauss-Laguerre nodes x_j scaled by 1/g, for g = 1 (surface gap) and
+    g = 3 (centre gap): energy and z-force integrands per xi, read from its
+    .byXi file (ref_pec2_s3_casimir.npz)."""
+    V3, P3 = icosphere(3)
+    write_msh(os.path.join(tmp, "s3.msh"), V3, P3)
+    geo = os.path.join(tmp, "pec2_s3.scuffgeo")
+    # one mesh file for both bodies, so the reference treats the second as the
+    # first's mate and assembles one T block
+    with open(geo, "w") as f:
+        f.write("OBJECT a\n  MESHFILE s3.msh\nENDOBJECT\n\nOBJECT b\n  MESHFILE s3.msh\n"
+                "  DISPLACED 0.0 0.0 3.0\nENDOBJECT\n")
+    x, _ = np.polynomial.laguerre.laggauss(20)
+    xi = np.concatenate([x / 1.0, x / 3.0])
+    with open(os.path.join(tmp, "xi.txt"), "w") as f:
+        f.write("".join("%.17g\n" % v for v in xi))
+    # the driver reads extra options from stdin when stdin is not a terminal
+    # (libhrutil/ProcessOptions.cc:238), so stdin is closed
+    r = subprocess.run([CAS3D, "--geometry", os.path.basename(geo), "--XiFile", "xi.txt", "--Energy", "--ZForce"],
+                       cwd=tmp, stdin=subprocess.DEVNULL, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("scuff-cas3D failed: %s %s" % (r.stdout, r.stderr))
+    rows = [ln.split() for ln in open(os.path.join(tmp, "pec2_s3.byXi")) if ln.strip() and not ln.startswith("#")]
+    got = np.array([[float(t) for t in r_[1:4]] for r_ in rows])
+    assert np.allclose(got[:, 0], xi, rtol=1e-6), "xi order"
+    np.savez_compressed(os.path.join(HERE, "ref_pec2_s3_casimir.npz"), xi=xi, gap=np.repeat([1.0, 3.0], 20),
+                        energy=got[:, 1], zforce=got[:, 2], laguerre_x=x)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=oracle.reference_tree(),
                     help="reference source tree (default: SCUFF_REF, or a 'reference' checkout beside the repo)")
-    ap.add_argument("--only", choices=["gradients", "torque", "mie", "cache"],
+    ap.add_argument("--only", choices=["gradients", "torque", "mie", "cache", "casimir"],
                     help="regenerate one group of fixtures only")
     a = ap.parse_args()
     if a.only == "mie":
@@ -285,9 +318,10 @@ def main():
         return
     if not os.path.exists(REFDUMP):
         sys.exit("build the reference first: make -C oracle/ref REF=%s" % a.ref)
-    if a.only in ("gradients", "torque", "cache"):
+    if a.only in ("gradients", "torque", "cache", "casimir"):
         with tempfile.TemporaryDirectory() as tmp:
-            {"gradients": gradient_fixtures, "torque": torque_fixtures, "cache": cache_fixture}[a.only](tmp)
+            {"gradients": gradient_fixtures, "torque": torque_fixtures, "cache": cache_fixture,
+             "casimir": casimir_fixture}[a.only](tmp)
         return
     rng = np.random.default_rng(0)
     with tempfile.TemporaryDirectory() as tmp:
@@ -308,6 +342,7 @@ def main():
         gradient_fixtures(tmp)
         torque_fixtures(tmp)
         cache_fixture(tmp)
+        casimir_fixture(tmp)
     mie_tables(a.ref)
 
 
