@@ -11,8 +11,10 @@ solve the 4 right-hand sides and refine to 1e-10 relative residual.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbem|reference]
 
 Prints one JSON line.  --impl reference times the CPU implementation of the
-path (the oracle port of the reference's algorithm; the reference binary
-built from its sources does not exist on the GPU host) on all host cores.
+path on all host cores (the oracle port of the reference's assembly and
+LAPACK's zgetrf/zgetrs; the reference binary built from its sources does not
+exist on the GPU host): one full-size solve cut into W + K slices, each step
+a real part of it (oracle/cpu_solve.py).
 """
 from __future__ import annotations
 
@@ -41,6 +43,17 @@ PLANE_WAVES = [((1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1)), ((1, 0, 0), (0, 0
 # launches of a factorisation, the 11 smallest estimated from the last captured
 # one's bytes per entry (the capture's summary is kept under profiles/)
 TC_TRAFFIC_BYTES_PER_LAUNCH = 1.45e9
+# nominal GB300 CUDA-core rates (the measured-peaks file has HBM and bf16 only)
+FP32_PEAK_TFLOPS = 75.0
+FP64_PEAK_TFLOPS = 1.25
+
+
+def far_ppr(G):
+    """Far (panel pair, region) units of a one-surface dielectric geometry:
+    unordered panel pairs times 2 regions, less the near pairs (rRel <= 4)."""
+    npan = G.np_total
+    near = sum(G.near_counts())
+    return 2 * (npan * (npan + 1) // 2 - near)
 
 
 def workload(subdiv):
@@ -120,47 +133,102 @@ def lu_update_flops(N, w=256):
     return tot
 
 
-def cpu_sample(cores):
-    """Oracle port on the host cores, bounded sample: assembly of the
-    subdivision-2 dielectric sphere (N = 960) scaled by the edge-pair count
-    ratio (7680/480)^2, plus LAPACK zgetrf at N = 3840 scaled by (15360/3840)^3."""
-    from oracle import oracle
-    import scipy.linalg as sl
-    V, P = workload(2)
-    S = oracle.Surface(V, P)
-    eps = [1.0, 2.25 + 0.01j]
-    t0 = time.perf_counter()
-    oracle.assemble([S], [(0, 1)], [False], 2.0, eps, [1.0, 1.0])
-    t_asm = time.perf_counter() - t0
-    rng = np.random.default_rng(0)
-    n_lu = 3840
-    A = rng.standard_normal((n_lu, n_lu)) + 1j * rng.standard_normal((n_lu, n_lu))
-    t0 = time.perf_counter()
-    sl.lu_factor(A, overwrite_a=True, check_finite=False)
-    t_lu = time.perf_counter() - t0
-    t_solve = (7680.0 / 480.0) ** 2 * t_asm + (15360.0 / n_lu) ** 3 * t_lu
-    return {"value": 1.0 / t_solve, "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": "oracle assembly of the N=960 sphere (%.2f s) x256 + zgetrf N=3840 (%.2f s) x64 "
-                      "-> %.1f s per N=15360 solve" % (t_asm, t_lu, t_solve)}
+CONFIG_WORKLOAD = "dielectric icosphere s=%d, N=%d, eps=2.25+0.01i, kR=2, %d plane-wave RHS"
+
+
+def bench_config(subdiv, N, nrhs, world=1):
+    """The workload dict both arms print (identical keys and values)."""
+    return {"workload": CONFIG_WORKLOAD % (subdiv, N, nrhs),
+            "l2": "inputs larger than L2 (C64 matrix %.2f GB, C128 %.2f GB)" % (N * N * 8 / 1e9, N * N * 16 / 1e9),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count()
+
+
+def cpu_sample(cores, subdiv=4):
+    """A bounded sample of the CPU solve at full size (oracle assembly,
+    LAPACK LU; oracle/cpu_solve.py): one column stripe holding 1/64 of the
+    upper triangle's edge pairs (assembled cold once to fill the near-pair
+    memo, then timed warm) and the LU's first panel steps up to 1/16 of its
+    flops, each scaled by its fraction of one solve."""
+    from oracle.cpu_solve import SlicedSolve, cpu_model
+    job = SlicedSolve(subdiv=subdiv, warm=False)
+    eb = job.stripe_bounds(64)
+    j = 32  # a stripe in the middle of the column range
+    job.assemble(eb[j], eb[j + 1])
+    job.M[:] = 0
+    ta, fa = job.assemble(eb[j], eb[j + 1])
+    kb = job.panel_bounds(16)
+    tl, fl = job.factor(kb[0], kb[1])
+    t_solve = ta / fa + tl / fl
+    return {"value": 1.0 / t_solve, "unit": "solves/s", "cores": cores, "kind": "port", "cpu": cpu_model(),
+            "sample": "N=%d at full size: assembly stripe of %.4f of the edge pairs, warm (%.2f s), LU panel steps "
+                      "%d-%d = %.4f of the LU flops (%.2f s, blocked zgetrf on a seeded random matrix), scaled "
+                      "-> %.1f s per solve" % (job.N, fa, ta, kb[0], kb[1], fl, tl, t_solve)}
 
 
 def run_reference(args):
-    cores = os.cpu_count()
+    """The reference's CPU path on all host cores (oracle assembly with
+    OpenMP, LAPACK LU from OpenBLAS): one full-size solve cut into W + K
+    slices.  Every step assembles a column stripe holding 1/(W+K) of the
+    upper triangle's edge pairs (warm: the near-pair integrals are memoised
+    in the set-up, as the reference's FIPPI cache holds them after the first
+    frequency); the K timed steps also run the whole LU, K runs of panel steps
+    of about equal flops, and the last one the 4-RHS solve.  Solves/s =
+    1 / (assembly time scaled by the timed stripes' pair fraction + LU time +
+    solve time).  ms_per_step is the mean wall time of a timed step."""
     if int(os.environ.get("RANK", "0")) != 0:
         return
-    vals = []
-    for _ in range(max(1, args.steps)):
-        vals.append(cpu_sample(cores))
-    v = statistics.median([c["value"] for c in vals])
-    cb = dict(vals[-1])
-    cb["value"] = v
-    print(json.dumps({"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
-                      "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+    # OpenMP threads of the assembly sleep, not spin, while OpenBLAS runs
+    os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
+    from oracle.cpu_solve import SlicedSolve, cpu_model
+    cores = cpu_threads()
+    t0 = time.perf_counter()
+    job = SlicedSolve(subdiv=args.subdiv)
+    t_setup = time.perf_counter() - t0
+    W, K = max(0, args.warmup), max(1, args.steps)
+    eb = job.stripe_bounds(W + K)
+    kb = job.panel_bounds(K)
+    t_asm = f_asm = t_lu = f_lu = t_sol = 0.0
+    steps_s = []
+    for j in range(W + K):
+        s0 = time.perf_counter()
+        ta, fa = job.assemble(eb[j], eb[j + 1])
+        if j >= W:
+            i = j - W
+            tl, fl = job.factor(kb[i], kb[i + 1])
+            t_lu += tl
+            f_lu += fl
+            if i == K - 1:
+                t_sol = job.solve()
+            t_asm += ta
+            f_asm += fa
+            steps_s.append(time.perf_counter() - s0)
+    T_asm = t_asm / f_asm
+    T = T_asm + t_lu / f_lu + t_sol
+    v = 1.0 / T
+    ms_step = 1000.0 * statistics.mean(steps_s)
+    cb = {"value": v, "unit": "solves/s", "cores": cores, "kind": "port", "cpu": cpu_model(),
+          "sample": "one N=%d solve in %d slices: timed steps assembled %.3f of the edge pairs (%.1f s, warm) and "
+                    "ran the whole LU (%.1f s, blocked zgetrf on a seeded random matrix, %d panels of 256) and the "
+                    "4-RHS zgetrs (%.2f s); solve time %.1f s = assembly %.1f + LU %.1f + solve %.2f; set-up "
+                    "(near-pair memo of %d pairs, random matrix) %.1f s untimed"
+                    % (job.N, W + K, f_asm, t_asm, t_lu, job.lu.npanels, t_sol, T, T_asm, t_lu / f_lu, t_sol,
+                       job.near_pairs, t_setup)}
+    print(json.dumps({"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus, "steps": K,
+                      "warmup": W, "ms_per_step": ms_step, "higher_is_better": True,
                       "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
                       "impl": "reference", "cpu_baseline": cb,
                       "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                      "config": {"workload": "dielectric icosphere s=4, N=15360, eps=2.25+0.01i, kR=2, 4 RHS",
-                                 "impl_note": "oracle port of the reference algorithm, OpenMP + LAPACK"}}))
+                      "config": bench_config(args.subdiv, job.N, 4, args.gpus),
+                      "method": "oracle port of the reference's assembly (OpenMP) + LAPACK zgetrf/zgetrs "
+                                "(OpenBLAS), FP64",
+                      "stages_s_per_solve": {"assembly_warm": T_asm, "lu": t_lu / f_lu, "solve": t_sol}}))
 
 
 def batch_jobs(seed=0):
@@ -222,6 +290,7 @@ def main():
     ap.add_argument("--subdiv", type=int, default=4)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fp64-reps", type=int, default=5, help="plain FP64 solves timed (median reported)")
     ap.add_argument("--workload", default="solve", choices=["solve", "batch"],
                     help="solve: the headline N=15360 mixed solve; batch: a frequency-sweep / multi-geometry batch")
     args = ap.parse_args()
@@ -318,12 +387,9 @@ def main():
     out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "c64+fp64-refine", "data": "synthetic",
-           "config": {"workload": "dielectric icosphere s=%d, N=%d, eps=2.25+0.01i, kR=2, %d plane-wave RHS"
-                                  % (args.subdiv, N, nrhs),
-                      "solve": "mixed: FP32 far field + FP64 near field -> C64, split-BF16 tensor-core LU, "
-                               "FP64 refinement to 1e-10",
-                      "l2": "inputs larger than L2 (C64 matrix %.2f GB)" % (N * N * 8 / 1e9),
-                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "config": bench_config(args.subdiv, N, nrhs, world),
+           "method": "mixed: float-float far field + FP64 near field -> C64, split-BF16 tensor-core LU, "
+                     "FP64 refinement to 1e-10",
            "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "solves/s",
                    "h2d_bytes_per_step": int(N * nrhs * 16), "d2h_bytes_per_step": int(N * nrhs * 16)},
            "refine_sweeps": iters, "final_rel_residual": final_res, "cold_first_solve_s": cold_s,
@@ -348,23 +414,57 @@ def main():
                            "launches_per_step": n_upd, "peak_kind": peak_kind,
                            "note": "algorithmic complex flops 8mnk; the split-BF16 form issues 3x that on the "
                                    "tensor pipe"}
+    # the assembly's far field (ppair + stamp kernels): far (panel pair,
+    # region) units per second, their algorithmic FP32 flops (3600 per unit:
+    # 36 kernel samples x 100) against the FP32 pipe, and the HBM traffic
+    # the stage must make (the C64 matrix written once, panel tables read)
+    far_ms = stage_ms[0] / args.steps
+    if far_ms > 0:
+        ppr = far_ppr(G)
+        fl = ppr * 3600.0
+        out["roofline_assembly"] = {
+            "kernel": "ppair_kernel + stamp_kernel (far field, float-float)", "bound": "fp32",
+            "panel_pairs_per_s": ppr / (far_ms * 1e-3), "far_ppr": ppr,
+            "achieved_tflops": fl / (far_ms * 1e-3) / 1e12, "peak_tflops": FP32_PEAK_TFLOPS,
+            "frac": fl / (far_ms * 1e-3) / 1e12 / FP32_PEAK_TFLOPS,
+            "peak_kind": "nominal FP32 (no measured FP32 figure in MEASURED_PEAKS.json)",
+            "hbm_gbs": (N * N * 8 + G.np_total * 64 * 8) / (far_ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm_peak,
+            "note": "float-float arithmetic issues ~640 FP32 instructions per sample against the 100-flop "
+                    "convention"}
 
-    # plain FP64 path (same geometry): assemble C128, LU, solve
+    # plain FP64 path (same geometry): assemble C128, LU, solve -- repeated,
+    # with its own stage split
     if not args.no_fp64:
-        M = G.AllocateBEMMatrix()
-        torch.cuda.synchronize()
-        e0.record(stream)
-        G.AssembleBEMMatrix(w, M)
-        M.LUFactorize()
-        X64 = M.LUSolve(B)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        fp64_ms = e0.elapsed_time(e1)
-        del M
+        fp64_ms, X64 = [], None
+        reps = max(1, args.fp64_reps)
+        lib().gbem_stats(1, None, None)
+        for r in range(reps):
+            M = G.AllocateBEMMatrix()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            G.AssembleBEMMatrix(w, M)
+            M.LUFactorize()
+            X64 = M.LUSolve(B)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            fp64_ms.append(e0.elapsed_time(e1))
+            del M
+        lib().gbem_stats(0, stage_ms, stage_n)
+        f64_stage = {names[i]: stage_ms[i] / reps for i in range(7)}
+        t64 = statistics.median(fp64_ms)
+        lu64_ms = f64_stage["lu_panels"] + f64_stage["lu_trailing_update"]
         rel_x = float(np.max(np.linalg.norm(Xmixed - X64, axis=0) / np.linalg.norm(X64, axis=0)))
         p64 = extinction_power(X64, B)
         pmx = extinction_power(Xmixed, B)
-        out["fp64"] = {"value": 1000.0 / fp64_ms, "unit": "solves/s", "ms_per_solve": fp64_ms}
+        out["fp64"] = {"value": 1000.0 / t64, "unit": "solves/s", "ms_per_solve": t64, "ms_all": fp64_ms,
+                       "runs": reps, "stages_ms_per_solve": f64_stage}
+        if lu64_ms > 0:
+            a64 = 8.0 * N ** 3 / 3.0 / (lu64_ms * 1e-3) / 1e12
+            out["fp64"]["roofline_lu"] = {"bound": "fp64", "achieved_tflops": a64, "peak_tflops": FP64_PEAK_TFLOPS,
+                                          "frac": a64 / FP64_PEAK_TFLOPS,
+                                          "peak_kind": "nominal FP64 (no measured FP64 figure in "
+                                                       "MEASURED_PEAKS.json)",
+                                          "kernel": "panel_kernel<double> + gemm_simt<double> (8N^3/3 flops)"}
         out["speedup_vs_fp64"] = out["value"] / out["fp64"]["value"]
         out["accuracy"] = {"rel_err_x_vs_fp64": rel_x,
                            "rel_err_extinction_power_vs_fp64": float(np.max(np.abs(pmx - p64) / np.abs(p64))),
@@ -379,7 +479,7 @@ def main():
         out["accuracy"]["absorbed_power_fp64"] = [float(v) for v in pa64]
     if not args.no_cpu and rank == 0 and world == 1:
         try:
-            out["cpu_baseline"] = cpu_sample(os.cpu_count())
+            out["cpu_baseline"] = cpu_sample(cpu_threads(), args.subdiv)
         except Exception as e:  # the CPU leg is a report, not the measurement
             out["cpu_baseline"] = {"error": str(e)}
     if rank == 0:
