@@ -224,6 +224,29 @@ gbem_status gbem_lu_factor_host(double *ZM, int N, int ld, int *ipiv, int *info)
 gbem_status gbem_lu_solve_host(const double *ZM, int N, int ld, const int *ipiv,
                                char trans, int nrhs, double *B, int ldb);
 
+/* ---- symmetric matrices in packed storage --------------------------------
+ * HMatrix's LHM_SYMMETRIC storage (libs/libhmat/HMatrix.cc:333): the upper
+ * triangle by columns, entry (i, j), i <= j, at i + j (j + 1) / 2, real (F64)
+ * or complex symmetric (C128, A = A^T). */
+/* The diagonal block (ns, ns) of AssembleBEMMatrixBlock
+ * (AssembleBEMMatrix.cc:349-391) into a packed LHM_SYMMETRIC destination, as
+ * scuff-cas3D allocates its T blocks (applications/scuff-cas3D/
+ * CreateSC3Data.cc:110): AP holds NumBFs(ns) (NumBFs(ns) + 1) / 2 entries;
+ * FP64; dtype F64 (imaginary frequency) or C128. */
+gbem_status gbem_assemble_block_packed_host(gbem_geometry *g, int ns, double omega_re, double omega_im,
+                                            const double *eps, const double *mu, void *AP, int dtype);
+/* Replaces HMatrix::LUFactorize for LHM_SYMMETRIC storage
+ * (LBWrappers.cc:159-166: dsptrf_ / zsptrf_ with UPLO = 'U'): Bunch-Kaufman
+ * A = U D U^T in place on the host packed array AP, LAPACK's pivot codes in
+ * ipiv (1-based; a 2 x 2 block at k-1, k has ipiv[k-1] = ipiv[k] < 0) and
+ * its INFO (k > 0: D(k,k) exactly zero, GBEM_ESINGULAR). */
+gbem_status gbem_sp_factor_host(void *AP, int N, int dtype, int *ipiv, int *info);
+/* Replaces the LHM_SYMMETRIC branch of HMatrix::LUSolve (LBWrappers.cc:
+ * 175-236: dsptrs_ / zsptrs_ 'U'): solves A X = B in place on the host
+ * column-major B (N x nrhs, ldb) with the factor and pivots of
+ * gbem_sp_factor_host. */
+gbem_status gbem_sp_solve_host(const void *AP, int N, int dtype, const int *ipiv, int nrhs, void *B, int ldb);
+
 /* ---- mixed-precision solve ----------------------------------------------- */
 /* One BEM solve in the mixed form: assemble the matrix with an FP32 far
  * field and FP64 near field into C64, factor it in complex FP32 with pivoting

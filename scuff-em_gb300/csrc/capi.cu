@@ -863,6 +863,109 @@ gbem_status gbem_lu_trace_host(gbem_matrix* M, const void* B, int ldb, int ncols
   return trace_impl(M, B, ldb, ncols, true, trace);
 }
 
+// ---- symmetric matrices in packed storage (LHM_SYMMETRIC) ----------------
+gbem_status gbem_assemble_block_packed_host(gbem_geometry* g, int ns, double omega_re, double omega_im,
+                                            const double* eps, const double* mu, void* AP, int dtype) {
+  if (!g || !AP || ns < 0 || ns >= (int)g->S.size() || (dtype != GBEM_C128 && dtype != GBEM_F64)) {
+    set_error("gbem_assemble_block_packed_host: bad arguments (dtype C128 or F64)");
+    return GBEM_EINVAL;
+  }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  CHECK_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+  cudaStream_t s = g->stream;
+  const int n = surface_bfs(g, ns);
+  const size_t es = esize(dtype), np = (size_t)n * (n + 1) / 2;
+  void *full = nullptr, *pk = nullptr;
+  cudaError_t e = cudaMallocAsync(&full, (size_t)n * n * es, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&pk, np * es, s);
+  if (e != cudaSuccess) st = cuda_status(e, "packed assembly alloc");
+  BlockSel sel{ns, ns, 0, 0};
+  if (st == GBEM_OK) st = assemble_into(g, omega_re, omega_im, eps, mu, GBEM_PREC_FP64, full, n, dtype, &sel);
+  if (st == GBEM_OK) st = sp_pack_device(full, n, n, dtype, pk, s);
+  if (st == GBEM_OK) {
+    e = cudaMemcpyAsync(AP, pk, np * es, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "packed assembly download");
+  }
+  if (full) cudaFreeAsync(full, s);
+  if (pk) cudaFreeAsync(pk, s);
+  cudaStreamSynchronize(s);
+  return st;
+}
+
+gbem_status gbem_sp_factor_host(void* AP, int N, int dtype, int* ipiv, int* info) {
+  if (!AP || N <= 0 || (dtype != GBEM_C128 && dtype != GBEM_F64)) {
+    set_error("gbem_sp_factor_host: bad arguments (N > 0, dtype C128 or F64)");
+    return GBEM_EINVAL;
+  }
+  const size_t es = esize(dtype), np = (size_t)N * (N + 1) / 2;
+  cudaStream_t s;
+  CHECK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+  void* dAP = nullptr;
+  int* dpiv = nullptr;
+  gbem_status st = GBEM_OK;
+  int h_info = 0;
+  cudaError_t e = cudaMallocAsync(&dAP, np * es, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&dpiv, sizeof(int) * N, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dAP, AP, np * es, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) st = cuda_status(e, "gbem_sp_factor_host upload");
+  if (st == GBEM_OK) st = sp_factor_device(dAP, N, dtype, dpiv, &h_info, s);
+  if (st == GBEM_OK) {
+    e = cudaMemcpyAsync(AP, dAP, np * es, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && ipiv) e = cudaMemcpyAsync(ipiv, dpiv, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "gbem_sp_factor_host download");
+    if (info) *info = h_info;
+  }
+  if (dAP) cudaFreeAsync(dAP, s);
+  if (dpiv) cudaFreeAsync(dpiv, s);
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (st == GBEM_OK && h_info > 0) { set_error("sptrf: D(%d,%d) is exactly zero", h_info, h_info); return GBEM_ESINGULAR; }
+  return st;
+}
+
+gbem_status gbem_sp_solve_host(const void* AP, int N, int dtype, const int* ipiv, int nrhs, void* B, int ldb) {
+  if (!AP || !ipiv || !B || N <= 0 || nrhs <= 0 || ldb < N || (dtype != GBEM_C128 && dtype != GBEM_F64)) {
+    set_error("gbem_sp_solve_host: bad arguments (dtype C128 or F64)");
+    return GBEM_EINVAL;
+  }
+  for (int k = 0; k < N; k++) {
+    const int c = ipiv[k];
+    if (c == 0 || c > N || c < -N || (c < 0 && !((k > 0 && ipiv[k - 1] == c) || (k + 1 < N && ipiv[k + 1] == c)))) {
+      set_error("gbem_sp_solve_host: ipiv[%d] = %d is not a pivot code of gbem_sp_factor_host", k, c);
+      return GBEM_EINVAL;
+    }
+  }
+  const size_t es = esize(dtype), np = (size_t)N * (N + 1) / 2;
+  cudaStream_t s;
+  CHECK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+  void *dAP = nullptr, *dB = nullptr;
+  int* dpiv = nullptr;
+  gbem_status st = GBEM_OK;
+  cudaError_t e = cudaMallocAsync(&dAP, np * es, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&dpiv, sizeof(int) * N, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dB, (size_t)N * nrhs * es, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dAP, AP, np * es, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dpiv, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dB, (size_t)N * es, B, (size_t)ldb * es, (size_t)N * es, nrhs, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) st = cuda_status(e, "gbem_sp_solve_host upload");
+  if (st == GBEM_OK) st = sp_solve_device(dAP, N, dtype, dpiv, nrhs, dB, N, s);
+  if (st == GBEM_OK) {
+    e = cudaMemcpy2DAsync(B, (size_t)ldb * es, dB, (size_t)N * es, (size_t)N * es, nrhs, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) st = cuda_status(e, "gbem_sp_solve_host download");
+  }
+  if (dAP) cudaFreeAsync(dAP, s);
+  if (dpiv) cudaFreeAsync(dpiv, s);
+  if (dB) cudaFreeAsync(dB, s);
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  return st;
+}
+
 gbem_status gbem_lu_log_abs_det(gbem_matrix* M, double* logdet) {
   if (!M || !logdet) { set_error("gbem_lu_log_abs_det: NULL argument"); return GBEM_EINVAL; }
   if (!M->factored) { set_error("gbem_lu_log_abs_det: matrix is not factored"); return GBEM_EINVAL; }

@@ -176,6 +176,13 @@ gbem_status lu_solve_static_scratch(const void* dA, int N, int ld, int dtype, co
                                     void* hB, int ldb, cudaStream_t s);
 int lu_solve_noalloc_max_n(int dtype);
 
+// sptrf.cu: symmetric matrices in LAPACK's upper packed storage
+// (Bunch-Kaufman A = U D U^T, dsptrf/zsptrf semantics); dtype F64 or C128
+gbem_status sp_factor_device(void* dAP, int N, int dtype, int* dipiv, int* h_info, cudaStream_t s);
+gbem_status sp_solve_device(const void* dAP, int N, int dtype, const int* dipiv, int nrhs, void* dB, int ldb,
+                            cudaStream_t s);
+gbem_status sp_pack_device(const void* dA, int lda, int n, int dtype, void* dAP, cudaStream_t s);
+
 // per-stage device timing and launch counts (process-wide; see gbem_stats)
 enum Stage { ST_FAR = 0, ST_NEAR = 1, ST_PANEL = 2, ST_GEMM = 3, ST_SOLVE = 4, ST_RESID = 5, ST_OTHER = 6, ST_N = 8 };
 void stats_launch(int stage, int n = 1);

@@ -258,6 +258,19 @@ class RWGGeometry:
                                              mu.ctypes.data, M.ctypes.data, M.shape[0], RowOffset, ColOffset, dt))
         return M
 
+    def AssembleBEMMatrixBlockPacked(self, ns, Omega, real=False):
+        """The diagonal block (ns, ns) in HMatrix's packed LHM_SYMMETRIC
+        storage (upper triangle by columns, (i, j) at i + j (j+1)/2), as
+        scuff-cas3D keeps its T blocks (CreateSC3Data.cc:110): a 1-D float64
+        (real=True) or complex128 array of n (n + 1) / 2 entries."""
+        n = self.NumBFs(ns)
+        AP = np.zeros(n * (n + 1) // 2, dtype=np.float64 if real else np.complex128)
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        check(lib().gbem_assemble_block_packed_host(self._h, ns, Omega.real, Omega.imag, eps.ctypes.data,
+                                                    mu.ctypes.data, AP.ctypes.data, F64 if real else C128))
+        return AP
+
     def AssembleBEMMatrixBlockGradient(self, nsa, nsb, Omega, real=False, components=(0, 1, 2)):
         """GradM[mu] = dM_block/dx_mu for a rigid displacement of surface nsa
         (AssembleBEMMatrixBlock's GradM); returns a list of three host arrays
@@ -392,6 +405,40 @@ class RWGGeometry:
         if st not in (_lib.GBEM_OK, _lib.GBEM_ENOCONV):
             check(st)
         return X, it.value, res.value
+
+
+def packed_dtype(AP):
+    if AP.dtype == np.float64:
+        return F64
+    if AP.dtype == np.complex128:
+        return C128
+    raise ValueError("packed arrays are float64 or complex128")
+
+
+def SymmetricLUFactorize(AP, N):
+    """HMatrix::LUFactorize for LHM_SYMMETRIC storage (dsptrf/zsptrf 'U',
+    LBWrappers.cc:159-166) on the GPU: factors the packed array AP in place
+    and returns (ipiv, info) with LAPACK's pivot codes."""
+    AP = np.asarray(AP)
+    if not AP.flags.c_contiguous or AP.size != N * (N + 1) // 2:
+        raise ValueError("AP must be a contiguous packed array of N (N + 1) / 2 entries")
+    ipiv = np.zeros(N, dtype=np.int32)
+    info = ctypes.c_int()
+    st = lib().gbem_sp_factor_host(AP.ctypes.data, N, packed_dtype(AP), ipiv.ctypes.data, ctypes.byref(info))
+    if st not in (_lib.GBEM_OK, _lib.GBEM_ESINGULAR):
+        check(st)
+    return ipiv, info.value
+
+
+def SymmetricLUSolve(AP, N, ipiv, B):
+    """HMatrix::LUSolve for LHM_SYMMETRIC storage (dsptrs/zsptrs 'U'): X with
+    A X = B for the packed factor of SymmetricLUFactorize."""
+    B = np.asarray(B)
+    vec = B.ndim == 1
+    X = np.array(B.reshape(N, -1), dtype=AP.dtype, order="F", copy=True)
+    ip = np.ascontiguousarray(ipiv, dtype=np.int32)
+    check(lib().gbem_sp_solve_host(AP.ctypes.data, N, packed_dtype(AP), ip.ctypes.data, X.shape[1], X.ctypes.data, N))
+    return X[:, 0] if vec else X
 
 
 def PreloadCache(path):

@@ -20,7 +20,7 @@ BUILD = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(REPO, "include")]
-CUDA_UNITS = ["assemble.cu", "lu.cu", "gemm_tc.cu", "capi.cu", "fippi_cache.cu"]
+CUDA_UNITS = ["assemble.cu", "lu.cu", "gemm_tc.cu", "capi.cu", "fippi_cache.cu", "sptrf.cu"]
 CXX_UNITS = ["geometry.cpp"]
 
 

@@ -57,3 +57,42 @@ def device_columns(M, cols):
         dst = out.ctypes.data + j * M.N * es
         assert rt.cudaMemcpy(ctypes.c_void_p(dst), ctypes.c_void_p(src), M.N * es, 2) == 0  # DeviceToHost
     return out
+
+
+def lapack_sp(AP, N, B=None):
+    """LAPACK's own dsptrf/zsptrf and dsptrs/zsptrs ('U') from the OpenBLAS
+    scipy ships (the routines HMatrix::LUFactorize/LUSolve call for packed
+    symmetric storage): returns (factor, ipiv, info[, X])."""
+    import ctypes
+    from oracle.cpu_solve import _openblas
+    L, pre = _openblas()
+    t = "z" if np.iscomplexobj(AP) else "d"
+    F = np.array(AP, copy=True)
+    ipiv = np.zeros(N, dtype=np.int32)
+    info = ctypes.c_int(0)
+    n = ctypes.c_int(N)
+    getattr(L, pre + t + "sptrf_")(b"U", ctypes.byref(n), F.ctypes.data_as(ctypes.c_void_p),
+                                   ipiv.ctypes.data_as(ctypes.c_void_p), ctypes.byref(info))
+    if B is None:
+        return F, ipiv, info.value
+    X = np.array(B, dtype=F.dtype, order="F", copy=True).reshape(N, -1, order="F")
+    info2 = ctypes.c_int(0)
+    getattr(L, pre + t + "sptrs_")(b"U", ctypes.byref(n), ctypes.byref(ctypes.c_int(X.shape[1])),
+                                   F.ctypes.data_as(ctypes.c_void_p), ipiv.ctypes.data_as(ctypes.c_void_p),
+                                   X.ctypes.data_as(ctypes.c_void_p), ctypes.byref(n), ctypes.byref(info2))
+    return F, ipiv, info.value, X
+
+
+def pack_upper(A):
+    """HMatrix's LHM_SYMMETRIC packing of a square array's upper triangle."""
+    n = A.shape[0]
+    return np.concatenate([A[:j + 1, j] for j in range(n)])
+
+
+def unpack_upper(AP, n):
+    A = np.zeros((n, n), dtype=AP.dtype)
+    o = 0
+    for j in range(n):
+        A[:j + 1, j] = AP[o:o + j + 1]
+        o += j + 1
+    return A
