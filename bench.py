@@ -231,21 +231,38 @@ def run_reference(args):
                       "stages_s_per_solve": {"assembly_warm": T_asm, "lu": t_lu / f_lu, "solve": t_sol}}))
 
 
-def batch_jobs(seed=0):
-    """A synthetic batch in the shape of the batching workload: icospheres of
-    radius 0.5-1.5 at subdivisions 2-3, eps ~ U[1.5, 4] + i U[0, 0.1], each
-    swept over log-spaced kR in [0.1, 5], two plane waves per solve."""
+def batch_geometries(seed=0):
+    """The batching workload's 48 geometries, seed 0: 24 icospheres of radius
+    U[0.5, 1.5] at subdivisions 2, 3, 4 in turn (320-5120 panels) and 24
+    rounded cubes of side 1 with U[600, 3000] panels (seeded jittered
+    triangulations), each with eps ~ U[1.5, 4] + i U[0, 0.1].  Returns
+    [(RWGGeometry, characteristic radius, description)]."""
     from gbem import RWGGeometry, mesh
     from gbem.api import Material
     rng = np.random.default_rng(seed)
-    jobs = []
-    for g in range(8):
-        s = 2 + g % 2
-        R = rng.uniform(0.5, 1.5)
-        V, P = mesh.icosphere(s, radius=R)
+    out = []
+    for j in range(48):
         eps = complex(rng.uniform(1.5, 4.0), rng.uniform(0.0, 0.1))
-        G = RWGGeometry([{"V": V, "P": P, "material": Material(eps)}])
-        for kR in np.geomspace(0.1, 5.0, 4):
+        if j % 2 == 0:
+            s = 2 + (j // 2) % 3
+            R = float(rng.uniform(0.5, 1.5))
+            V, P = mesh.icosphere(s, radius=R)
+            desc = "icosphere s=%d R=%.3f" % (s, R)
+        else:
+            npan = int(rng.uniform(600, 3000))
+            V, P = mesh.rounded_cube(npan, side=1.0, seed=int(rng.integers(1 << 30)))
+            R = 0.5
+            desc = "rounded cube %d panels" % len(P)
+        out.append((RWGGeometry([{"V": V, "P": P, "material": Material(eps)}]), R, desc))
+    return out
+
+
+def batch_jobs(geoms, nfreq=16):
+    """Every geometry swept over nfreq log-spaced kR in [0.1, 5] (omega =
+    kR / R), two plane waves (+z incidence, x and y polarisation) per solve."""
+    jobs = []
+    for G, R, _ in geoms:
+        for kR in np.geomspace(0.1, 5.0, nfreq):
             w = kR / R
             B = np.stack([G.AssembleRHSVector(w, e, n) for e, n in PLANE_WAVES[:2]], axis=1)
             jobs.append((G, w, B))
@@ -253,32 +270,111 @@ def batch_jobs(seed=0):
 
 
 def run_batch(args):
-    """Batch throughput: the same jobs one at a time and as one batch of up to
-    four concurrent solves (gbem_solve_mixed_batch).  A 'step' is the whole
-    batch; value = solves/s of the batched form."""
-    import time
+    """Batch throughput on the batching workload (48 geometries x 16
+    frequencies = 768 mixed solves, N 960-15360): one step = the whole batch
+    through gbem_solve_mixed_batch (up to four concurrent solves); the same
+    jobs one at a time are timed once for comparison."""
     from gbem import solve_mixed_batch
-    jobs = batch_jobs()
-    for _ in range(max(args.warmup, 3) // 3):
+    geoms = batch_geometries()
+    jobs = batch_jobs(geoms)
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.warmup)):
         solve_mixed_batch(jobs, max_concurrent=4)
-    t_seq, t_bat = [], []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        for G, w, B in jobs:
-            G.solve_mixed(w, B)
-        t_seq.append(time.perf_counter() - t0)
+    t_warm = time.perf_counter() - t0
+    t_bat = []
+    for _ in range(max(1, args.steps)):
         t0 = time.perf_counter()
         out = solve_mixed_batch(jobs, max_concurrent=4)
         t_bat.append(time.perf_counter() - t0)
-    ns = [G.TotalBFs for G, _, _ in jobs]
-    print(json.dumps({"metric": "batched mixed solves/s (frequency sweeps of 8 geometries)", "value": len(jobs) / min(t_bat),
-                      "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-                      "ms_per_step": 1e3 * min(t_bat), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    t0 = time.perf_counter()
+    for G, w, B in jobs:
+        G.solve_mixed(w, B)
+    t_seq = time.perf_counter() - t0
+    ns = sorted(G.TotalBFs for G, _, _ in geoms)
+    buckets = {}
+    for n in ns:
+        b = "%d-%d" % ((n // 1024) * 1024, (n // 1024) * 1024 + 1023)
+        buckets[b] = buckets.get(b, 0) + 1
+    print(json.dumps({"metric": "batched mixed solves/s (48 geometries x 16 frequencies)",
+                      "value": len(jobs) / statistics.median(t_bat), "unit": "solves/s", "n_gpus": 1,
+                      "steps": len(t_bat), "warmup": max(1, args.warmup), "ms_per_step": 1e3 * statistics.median(t_bat),
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                       "dtype": "c64+fp64-refine", "data": "synthetic",
-                      "config": {"workload": "8 dielectric icospheres (s=2,3; R 0.5-1.5) x 4 kR in [0.1, 5], 2 RHS",
-                                 "N_range": [min(ns), max(ns)], "jobs": len(jobs), "max_concurrent": 4},
-                      "sequential_solves_per_s": len(jobs) / min(t_seq),
+                      "config": {"workload": "24 icospheres (R 0.5-1.5, s=2,3,4) + 24 rounded cubes (600-3000 panels), "
+                                             "eps U[1.5,4]+iU[0,0.1], 16 kR in [0.1,5], 2 RHS, seed 0",
+                                 "N_range": [ns[0], ns[-1]], "geometries_per_1024_bucket": buckets,
+                                 "jobs": len(jobs), "max_concurrent": 4},
+                      "sequential_solves_per_s": len(jobs) / t_seq, "first_pass_s_incl_near_tables": t_warm,
                       "max_refine_sweeps": max(o[1] for o in out), "max_residual": max(o[2] for o in out)}))
+
+
+def run_large(args):
+    """The large workload: dielectric icosphere s=5 (20480 panels, N = 61440,
+    a 30 GB complex64 matrix), eps = 12+0.05i, kR = 4, 8 plane waves
+    (+-x, +-y, +-z incidence, two polarisations each, the first 8); mixed
+    solve with FP64 refinement.  Prints solves/s and the EMT powers."""
+    import torch
+    from gbem import RWGGeometry, mesh
+    from gbem.api import Material
+    V, P = mesh.icosphere(5)
+    G = RWGGeometry([{"V": V, "P": P, "material": Material(12 + 0.05j)}])
+    w = 4.0
+    waves = []
+    for d in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)):
+        pols = [p for p in ((1, 0, 0), (0, 1, 0), (0, 0, 1)) if np.dot(p, d) == 0]
+        waves += [(p, d) for p in pols]
+    waves = waves[:8]
+    B = np.stack([G.AssembleRHSVector(w, e, n) for e, n in waves], axis=1)
+    t0 = time.perf_counter()
+    X, it, res = G.solve_mixed(w, B)
+    cold = time.perf_counter() - t0
+    ts, its = [], []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        X, it, res = G.solve_mixed(w, B)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+        its.append(it)
+    pabs, pscat = G.GetPFT(w, X, RHS=B, precision="mixed")
+    t = statistics.median(ts)
+    print(json.dumps({"metric": "mixed solves/s at N=61440", "value": 1.0 / t, "unit": "solves/s", "n_gpus": 1,
+                      "steps": len(ts), "warmup": 1, "ms_per_step": 1e3 * t, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "c64+fp64-refine", "data": "synthetic",
+                      "config": {"workload": "dielectric icosphere s=5, N=%d, eps=12+0.05i, kR=4, 8 plane-wave RHS"
+                                             % G.TotalBFs},
+                      "cold_first_solve_s": cold, "refine_sweeps": its, "final_rel_residual": res,
+                      "absorbed_power": [float(v) for v in pabs], "scattered_power": [float(v) for v in pscat]}))
+
+
+def run_casimir(args):
+    """The Casimir workload: two PEC icospheres (s=3, N = 3840 real), centres
+    3 apart; energy and z-force integrands at the 20 Gauss-Laguerre
+    frequencies xi = x_j / g (g = 1, the surface gap), and the integrated
+    energy and force (sum of weights x integrand).  One step = the 20-point
+    sweep."""
+    from gbem import mesh
+    from gbem.casimir import CasimirIntegrand, laguerre_xi
+    V, P = mesh.icosphere(3)
+    cas = CasimirIntegrand([{"V": V, "P": P, "material": None}, {"V": V + [0.0, 0.0, 3.0], "P": P, "material": None}])
+    xi, wt = laguerre_xi(20, 1.0)
+    for _ in range(max(1, args.warmup)):
+        cas(float(xi[0]))
+    ts = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        vals = [cas(float(x)) for x in xi]
+        ts.append(time.perf_counter() - t0)
+    E = np.array([v[0] for v in vals])
+    F = np.array([v[1] for v in vals])
+    t = statistics.median(ts)
+    print(json.dumps({"metric": "Casimir integrand points/s (two PEC spheres, N=3840)", "value": len(xi) / t,
+                      "unit": "xi/s", "n_gpus": 1, "steps": len(ts), "warmup": max(1, args.warmup),
+                      "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                      "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": "2 PEC icospheres s=3, centre gap 3, 20 Gauss-Laguerre xi, surface gap 1"},
+                      "xi": [float(x) for x in xi], "energy_integrand": E.tolist(), "zforce_integrand": F.tolist(),
+                      "energy": float(np.dot(wt, E)), "zforce": float(np.dot(wt, F))}))
 
 
 def main():
@@ -291,13 +387,18 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fp64-reps", type=int, default=5, help="plain FP64 solves timed (median reported)")
-    ap.add_argument("--workload", default="solve", choices=["solve", "batch"],
-                    help="solve: the headline N=15360 mixed solve; batch: a frequency-sweep / multi-geometry batch")
+    ap.add_argument("--workload", default="solve", choices=["solve", "batch", "large", "casimir"],
+                    help="solve: the headline N=15360 mixed solve; batch: 48 geometries x 16 frequencies; "
+                         "large: the N=61440 sphere; casimir: the two-sphere Casimir sweep")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "large":
+        return run_large(args)
+    if args.workload == "casimir":
+        return run_casimir(args)
 
     import ctypes
     import torch
