@@ -259,6 +259,17 @@ gbem_status gbem_solve_mixed(gbem_geometry *g, double omega_re, double omega_im,
                              const double *B, int ldb, double *X, int ldx,
                              double tol, int max_iter, int *iters, double *resid);
 
+/* The FP64 solve by mixed-precision refinement (the gbem_solve_refined of the
+ * replacement's C ABI; the reference solves with zgetrf/zgetrs on the FP64
+ * matrix, LBWrappers.cc:151-236): the matrix is assembled in FP64
+ * (complex128), its complex64 rounding is factored (tensor-core LU), and x
+ * is refined with FP64 residuals against the complex128 matrix until
+ * ||b - M x|| <= tol ||b||, so x is the FP64 solve's to that tolerance.
+ * Arguments as gbem_solve_mixed. */
+gbem_status gbem_solve_refined(gbem_geometry *g, double omega_re, double omega_im, const double *eps,
+                               const double *mu, int nrhs, const double *B, int ldb, double *X, int ldx,
+                               double tol, int max_iter, int *iters, double *resid);
+
 /* A batch of independent mixed-precision solves (frequency sweeps and
  * multi-geometry jobs of uneven N; no counterpart in the reference, whose
  * drivers loop over frequencies and geometries one solve at a time).  Up to
@@ -350,6 +361,19 @@ gbem_status gbem_cache_lookup_stats(const gbem_geometry *g, long long *hits, lon
 gbem_status gbem_vertex_vjp_matrix(gbem_geometry *g, double omega_re, double omega_im, const double *eps,
                                    const double *mu, int nrhs, const double *lam, int ldl, const double *x,
                                    int ldx, double rel_step, double *grad);
+/* gbem_vertex_vjp_matrix for one region's matrix alone, with the signs of an
+ * exterior region (KK = i mu w GC0, KN = NK = -i k GC1, NN = -i eps w GC0):
+ * region 0 gives the matrix of the EMT scattered power's quadratic form
+ * (gbem_power_emt), whose explicit shape derivative this contracts. */
+gbem_status gbem_vertex_vjp_region(gbem_geometry *g, double omega_re, double omega_im, const double *eps,
+                                   const double *mu, int region, int nrhs, const double *lam, int ldl,
+                                   const double *x, int ldx, double rel_step, double *grad);
+/* Gradient of gbem_power_emt's scattered power with respect to the solution
+ * vectors: G[:, r] = dP_r/dRe KN[:, r] + i dP_r/dIm KN[:, r] (FP64; host
+ * N x nrhs complex128; nrhs <= 8).  No reference counterpart (the shape
+ * derivative of absorbed power). */
+gbem_status gbem_power_emt_grad(gbem_geometry *g, double omega_re, double omega_im, const double *eps,
+                                const double *mu, int nrhs, const double *KN, int ldkn, double *G, int ldg);
 /* grad[3 v + c] = Re sum_w sum_i conj(gb_iw) d b_iw/dV_vc for the plane-wave
  * right-hand sides of gbem_rhs_planewave (E0: 6 doubles, nhat: 3 per wave). */
 gbem_status gbem_vertex_vjp_rhs_planewave(gbem_geometry *g, double omega_re, double omega_im, const double *eps,

@@ -1082,6 +1082,25 @@ static RegionArgs region_args(const Block& b, double wr, double wi, const double
   return ra;
 }
 
+// One region's contribution with the signs of an exterior region
+// (KK = i mu w GC0, KN = NK = -i k GC1, NN = -i eps w GC0): the matrix of the
+// EMT power's quadratic form.  nreg = 0 when the block does not see region R.
+static RegionArgs single_region_args(const Block& b, const RegionArgs& ra, int R, double wr, double wi,
+                                     const double* eps, const double* mu) {
+  RegionArgs rb;
+  memset(&rb, 0, sizeof rb);
+  for (int r = 0; r < ra.nreg; r++) {
+    if (b.reg[r] != R) continue;
+    const cx<double> I = cxd(0.0, 1.0), w = cxd(wr, wi);
+    rb.k[0] = ra.k[r];
+    rb.pf1[0] = I * cxd(mu[2 * R], mu[2 * R + 1]) * w;
+    rb.pfc[0] = cxd(-1.0, 0.0);
+    rb.pf3[0] = (-1.0) * (I * cxd(eps[2 * R], eps[2 * R + 1]) * w);
+    rb.nreg = 1;
+  }
+  return rb;
+}
+
 gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int precision,
                             void* dM, int ld, int dtype, cudaStream_t s, const BlockSel* only, int only_region) {
   if ((precision == GBEM_PREC_FP64 && dtype != GBEM_C128) || (precision == GBEM_PREC_MIXED && dtype != GBEM_C64)) {
@@ -1123,22 +1142,8 @@ gbem_status assemble_device(Geometry* g, double wr, double wi, const double* eps
     if (only && !(b.sa == std::min(only->nsa, only->nsb) && b.sb == std::max(only->nsa, only->nsb))) continue;
     RegionArgs ra = region_args(b, wr, wi, eps, mu);
     if (only_region >= 0) {
-      // one region's contribution with the sign of an exterior region:
-      // KK = i mu w GC0, KN = NK = -i k GC1, NN = -i eps w GC0
-      RegionArgs rb;
-      memset(&rb, 0, sizeof rb);
-      for (int r = 0; r < ra.nreg; r++) {
-        if (b.reg[r] != only_region) continue;
-        const int R = b.reg[r];
-        const cx<double> I = cxd(0.0, 1.0), w = cxd(wr, wi);
-        rb.k[0] = ra.k[r];
-        rb.pf1[0] = I * cxd(mu[2 * R], mu[2 * R + 1]) * w;
-        rb.pfc[0] = cxd(-1.0, 0.0);
-        rb.pf3[0] = (-1.0) * (I * cxd(eps[2 * R], eps[2 * R + 1]) * w);
-        rb.nreg = 1;
-      }
-      if (rb.nreg == 0) continue;
-      ra = rb;
+      ra = single_region_args(b, ra, only_region, wr, wi, eps, mu);
+      if (ra.nreg == 0) continue;
     }
     {
       StatTimer tn(ST_NEAR, s);
@@ -1914,7 +1919,7 @@ static int total_vertices(const Geometry* g) {
 
 gbem_status vertex_vjp_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int nrhs,
                               const void* d_lam, int ldl, const void* d_x, int ldx, double* d_grad, double rel_step,
-                              cudaStream_t s) {
+                              cudaStream_t s, int only_region) {
   gbem_status st = upload_geometry(g);
   if (st == GBEM_OK) st = upload_vjp_tables(g);
   if (st != GBEM_OK) return st;
@@ -1929,7 +1934,11 @@ gbem_status vertex_vjp_device(Geometry* g, double wr, double wi, const double* e
     if (b.nreg == 0) continue;
     const Surface& A = g->S[b.sa];
     const Surface& B = g->S[b.sb];
-    const RegionArgs ra = region_args(b, wr, wi, eps, mu);
+    RegionArgs ra = region_args(b, wr, wi, eps, mu);
+    if (only_region >= 0) {
+      ra = single_region_args(b, ra, only_region, wr, wi, eps, mu);
+      if (ra.nreg == 0) continue;
+    }
     VjpFarArgs fa;
     fa.t = t; fa.offa = A.panel_offset; fa.offb = B.panel_offset; fa.npa = A.np; fa.npb = B.np;
     fa.bpe_a = A.pec ? 1 : 2; fa.bpe_b = B.pec ? 1 : 2; fa.sym = b.sym ? 1 : 0;

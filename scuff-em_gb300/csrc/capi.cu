@@ -162,6 +162,36 @@ static __global__ void emt_quadform(const cx<TM>* M, long long ld, int N, const 
     for (int r = 0; r < nrhs; r++) part[((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 8 + r] = red[r][0];
 }
 
+// Gradient of the EMT scattered power with respect to the solution vector:
+// P = 1/2 c^H H c with c = D x (D = 1 on K rows, -ZVAC on N rows) and
+// H = S - i T, S_ij = alpha_ij Re M0_ij (alpha: KK -ZVAC, NN 1/ZVAC),
+// T_ij = beta_ij Im M0_ij (beta: KN -1, NK +1), the form of emt_quadform;
+// out = dP/dRe x + i dP/dIm x = D H D x.  One thread per row.
+static __global__ void emt_grad(const cx<double>* M, long long ld, int N, const signed char* type, const cx<double>* X,
+                                long long ldx, int nrhs, cx<double>* out, long long ldo) {
+  const double ZV = 376.73031346177;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int ti = type[i];
+  double gr[8] = {0, 0, 0, 0, 0, 0, 0, 0}, gi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int j = 0; j < N; j++) {
+    const cx<double> m = M[i + (long long)j * ld];
+    const int tj = type[j];
+    const double s = (!ti && !tj) ? -ZV * m.re : ((ti && tj) ? m.re / ZV : 0.0);
+    const double t = (!ti && tj) ? -m.im : ((ti && !tj) ? m.im : 0.0);
+    const double dj = tj ? -ZV : 1.0;
+    for (int r = 0; r < nrhs; r++) {
+      const cx<double> xj = X[j + (long long)r * ldx];
+      const double cr = dj * xj.re, ci = dj * xj.im;
+      // (s - i t) (cr + i ci)
+      gr[r] += s * cr + t * ci;
+      gi[r] += s * ci - t * cr;
+    }
+  }
+  const double di = ti ? -ZV : 1.0;
+  for (int r = 0; r < nrhs; r++) out[i + (long long)r * ldo] = mk(di * gr[r], di * gi[r]);
+}
+
 namespace gbem {
 template <typename T>
 static __global__ void trace_diag(const cx<T>* X, long long ldx, int n, double* out) {
@@ -494,9 +524,29 @@ gbem_status gbem_power_emt(gbem_geometry* g, double omega_re, double omega_im, c
   return GBEM_OK;
 }
 
+static gbem_status vertex_vjp_impl(gbem_geometry* g, double omega_re, double omega_im, const double* eps,
+                                   const double* mu, int region, int nrhs, const double* lam, int ldl, const double* x,
+                                   int ldx, double rel_step, double* grad);
+
 gbem_status gbem_vertex_vjp_matrix(gbem_geometry* g, double omega_re, double omega_im, const double* eps,
                                    const double* mu, int nrhs, const double* lam, int ldl, const double* x, int ldx,
                                    double rel_step, double* grad) {
+  return vertex_vjp_impl(g, omega_re, omega_im, eps, mu, -1, nrhs, lam, ldl, x, ldx, rel_step, grad);
+}
+
+gbem_status gbem_vertex_vjp_region(gbem_geometry* g, double omega_re, double omega_im, const double* eps,
+                                   const double* mu, int region, int nrhs, const double* lam, int ldl, const double* x,
+                                   int ldx, double rel_step, double* grad) {
+  if (!g || region < 0 || region >= g->nregions) {
+    set_error("gbem_vertex_vjp_region: region out of range");
+    return GBEM_EINVAL;
+  }
+  return vertex_vjp_impl(g, omega_re, omega_im, eps, mu, region, nrhs, lam, ldl, x, ldx, rel_step, grad);
+}
+
+static gbem_status vertex_vjp_impl(gbem_geometry* g, double omega_re, double omega_im, const double* eps,
+                                   const double* mu, int region, int nrhs, const double* lam, int ldl, const double* x,
+                                   int ldx, double rel_step, double* grad) {
   if (!g || !eps || !mu || !lam || !x || !grad || nrhs <= 0 || ldl < g->N || ldx < g->N || !(rel_step > 0.0)) {
     set_error("gbem_vertex_vjp_matrix: bad arguments");
     return GBEM_EINVAL;
@@ -515,13 +565,60 @@ gbem_status gbem_vertex_vjp_matrix(gbem_geometry* g, double omega_re, double ome
     e = cudaMemcpy2DAsync(dX, (size_t)N * 16, x, (size_t)ldx * 16, (size_t)N * 16, nrhs, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(dG, 0, sizeof(double) * 3 * (size_t)nv, s);
   st = cuda_status(e, "gbem_vertex_vjp_matrix setup");
-  if (st == GBEM_OK) st = vertex_vjp_device(g, omega_re, omega_im, eps, mu, nrhs, dL, N, dX, N, (double*)dG, rel_step, s);
+  if (st == GBEM_OK)
+    st = vertex_vjp_device(g, omega_re, omega_im, eps, mu, nrhs, dL, N, dX, N, (double*)dG, rel_step, s, region);
   if (st == GBEM_OK) {
     e = cudaMemcpyAsync(grad, dG, sizeof(double) * 3 * (size_t)nv, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     st = cuda_status(e, "gbem_vertex_vjp_matrix");
   }
   cudaFreeAsync(dL, s); cudaFreeAsync(dX, s); cudaFreeAsync(dG, s);
+  cudaStreamSynchronize(s);
+  return st;
+}
+
+gbem_status gbem_power_emt_grad(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
+                                int nrhs, const double* KN, int ldkn, double* G, int ldg) {
+  if (!g || !eps || !mu || !KN || !G || nrhs <= 0 || nrhs > 8 || ldkn < g->N || ldg < g->N) {
+    set_error("gbem_power_emt_grad: bad arguments (1 <= nrhs <= 8)");
+    return GBEM_EINVAL;
+  }
+  for (const Surface& S : g->S)
+    if (S.reg_ext != 0) {
+      set_error("gbem_power_emt_grad: every surface must face the exterior region 0");
+      return GBEM_ENOTSUP;
+    }
+  gbem_status st = ensure_stream(g);
+  if (st != GBEM_OK) return st;
+  const int N = g->N;
+  cudaStream_t s = g->stream;
+  std::vector<signed char> type(N);
+  for (const Surface& S : g->S)
+    for (int e = 0; e < S.ne; e++) {
+      if (S.pec) type[S.bf_offset + e] = 0;
+      else { type[S.bf_offset + 2 * e] = 0; type[S.bf_offset + 2 * e + 1] = 1; }
+    }
+  void *dM = nullptr, *dX = nullptr, *dT = nullptr, *dG = nullptr;
+  cudaError_t e = cudaMallocAsync(&dM, (size_t)N * N * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dX, (size_t)N * nrhs * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dG, (size_t)N * nrhs * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dT, (size_t)N, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(dX, (size_t)N * 16, KN, (size_t)ldkn * 16, (size_t)N * 16, nrhs, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dT, type.data(), N, cudaMemcpyHostToDevice, s);
+  st = cuda_status(e, "gbem_power_emt_grad setup");
+  if (st == GBEM_OK) st = assemble_device(g, omega_re, omega_im, eps, mu, GBEM_PREC_FP64, dM, N, GBEM_C128, s, nullptr, 0);
+  if (st == GBEM_OK) {
+    emt_grad<<<(N + 127) / 128, 128, 0, s>>>((const cx<double>*)dM, N, N, (const signed char*)dT,
+                                            (const cx<double>*)dX, N, nrhs, (cx<double>*)dG, N);
+    stats_launch(ST_OTHER);
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(G, (size_t)ldg * 16, dG, (size_t)N * 16, (size_t)N * 16, nrhs, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    st = cuda_status(e, "gbem_power_emt_grad");
+  }
+  cudaFreeAsync(dM, s); cudaFreeAsync(dX, s); cudaFreeAsync(dT, s); cudaFreeAsync(dG, s);
   cudaStreamSynchronize(s);
   return st;
 }
@@ -1091,9 +1188,15 @@ __global__ void colnorm2(const double2* a, int N, int nrhs, double* out) {
   if (threadIdx.x == 0) out[r] = red[0];
 }
 
+// fp64_matrix: the matrix is assembled in FP64 (complex128), factored as its
+// complex64 rounding, and the refinement residuals are taken against the
+// complex128 matrix itself, so the solution converges to the FP64 solve's;
+// otherwise the mixed assembly (float-float far field, complex64) is both
+// factored and refined against.
 static gbem_status solve_mixed_impl(gbem_geometry* g, double omega_re, double omega_im, const double* eps,
                                     const double* mu, int nrhs, const void* B, int ldb, bool b_host, void* X, int ldx,
-                                    bool x_host, double tol, int max_iter, int* iters, double* resid) {
+                                    bool x_host, double tol, int max_iter, int* iters, double* resid,
+                                    bool fp64_matrix = false) {
   if (!g || !B || !X || nrhs <= 0 || nrhs > 64 || ldb < g->N || ldx < g->N) {
     set_error("gbem_solve_mixed: bad arguments");
     return GBEM_EINVAL;
@@ -1130,9 +1233,21 @@ static gbem_status solve_mixed_impl(gbem_geometry* g, double omega_re, double om
   void* dY = w; w += (size_t)N * 8 * 8;
   void* part = w;
   cudaError_t e = cudaSuccess;
-  st = gbem_assemble(g, omega_re, omega_im, eps, mu, GBEM_PREC_MIXED, M);
+  gbem_matrix* M128 = nullptr;
+  if (fp64_matrix) {
+    st = gbem_matrix_create(g, GBEM_C128, &M128);
+    if (st == GBEM_OK) st = gbem_assemble(g, omega_re, omega_im, eps, mu, GBEM_PREC_FP64, M128);
+    if (st == GBEM_OK) {
+      const size_t nn = (size_t)N * N;
+      to_c64<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>((const double2*)M128->d, (float2*)F->d, nn);
+      stats_launch(ST_OTHER);
+      e = cudaGetLastError();
+    }
+  } else {
+    st = gbem_assemble(g, omega_re, omega_im, eps, mu, GBEM_PREC_MIXED, M);
+    if (st == GBEM_OK) e = cudaMemcpyAsync(F->d, M->d, (size_t)N * N * 8, cudaMemcpyDeviceToDevice, s);
+  }
   if (st == GBEM_OK) {
-    e = cudaMemcpyAsync(F->d, M->d, (size_t)N * N * 8, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess)
       e = cudaMemcpy2DAsync(dB, (size_t)N * 16, B, (size_t)ldb * 16, (size_t)N * 16, nrhs,
                             b_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s);
@@ -1165,8 +1280,10 @@ static gbem_status solve_mixed_impl(gbem_geometry* g, double omega_re, double om
     stats_launch(ST_OTHER);
     {
       StatTimer t(ST_RESID, s);
-      st = residual_device(M->d, N, GBEM_C64, N, (const double*)dX, N, (const double*)dB, N, nrhs, (double*)dR, N,
-                           part, s);
+      st = fp64_matrix ? residual_device(M128->d, N, GBEM_C128, N, (const double*)dX, N, (const double*)dB, N, nrhs,
+                                         (double*)dR, N, part, s)
+                       : residual_device(M->d, N, GBEM_C64, N, (const double*)dX, N, (const double*)dB, N, nrhs,
+                                         (double*)dR, N, part, s);
     }
     if (st != GBEM_OK) break;
     colnorm2<<<nrhs, 256, 0, s>>>((const double2*)dR, N, nrhs, dn);
@@ -1185,6 +1302,7 @@ static gbem_status solve_mixed_impl(gbem_geometry* g, double omega_re, double om
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) st = cuda_status(e, "gbem_solve_mixed download");
   }
+  if (M128) gbem_matrix_destroy(M128);
   if (iters) *iters = it;
   if (resid) *resid = rel;
   if (st == GBEM_OK && rel > tol) {
@@ -1198,6 +1316,13 @@ gbem_status gbem_solve_mixed(gbem_geometry* g, double omega_re, double omega_im,
                              int nrhs, const double* B, int ldb, double* X, int ldx, double tol, int max_iter, int* iters,
                              double* resid) {
   return solve_mixed_impl(g, omega_re, omega_im, eps, mu, nrhs, B, ldb, true, X, ldx, true, tol, max_iter, iters, resid);
+}
+
+gbem_status gbem_solve_refined(gbem_geometry* g, double omega_re, double omega_im, const double* eps, const double* mu,
+                               int nrhs, const double* B, int ldb, double* X, int ldx, double tol, int max_iter,
+                               int* iters, double* resid) {
+  return solve_mixed_impl(g, omega_re, omega_im, eps, mu, nrhs, B, ldb, true, X, ldx, true, tol, max_iter, iters, resid,
+                          true);
 }
 
 gbem_status gbem_solve_mixed_batch(int njobs, gbem_batch_job* jobs, int max_concurrent) {

@@ -144,9 +144,11 @@ void free_geometry_device(Geometry* g);
 // adjoint contractions (device arrays, complex128 column-major): grad (3 per
 // vertex, surfaces in order) += Re sum conj(lam) dM/dV x, and
 // += Re sum conj(gb) db/dV for nw plane waves (E0: 6 doubles, nh: 3 per wave)
+// only_region >= 0: that region's contribution alone, with the signs of an
+// exterior region (the matrix of the EMT power's quadratic form)
 gbem_status vertex_vjp_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int nrhs,
                               const void* d_lam, int ldl, const void* d_x, int ldx, double* d_grad, double rel_step,
-                              cudaStream_t s);
+                              cudaStream_t s, int only_region = -1);
 gbem_status rhs_vjp_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, int nw,
                            const double* E0, const double* nh, const void* d_gb, int ldg, double* d_grad, cudaStream_t s);
 int geometry_total_vertices(const Geometry* g);

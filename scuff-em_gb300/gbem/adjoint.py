@@ -71,8 +71,12 @@ class _Scatter(torch.autograd.Function):
         elif precision == "mixed":
             x = geo.solve_mixed(Omega, b)[0]
             solve = lambda B: geo.solve_mixed(Omega, B)[0]  # noqa: E731
+        elif precision == "refined":
+            # the FP64 solution by mixed-precision refinement against the FP64 matrix
+            x = geo.solve_refined(Omega, b)[0]
+            solve = lambda B: geo.solve_refined(Omega, B)[0]  # noqa: E731
         else:
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+            raise ValueError("precision must be 'fp64', 'mixed' or 'refined'")
         ctx.geo, ctx.solve, ctx.Omega, ctx.waves, ctx.rel_step = geo, solve, Omega, waves, rel_step
         ctx.x = x
         ctx.vdevice, ctx.vdtype = V.device, V.dtype
@@ -95,6 +99,59 @@ def scatter(V, topology, Omega, waves, precision="fp64", rel_step=1e-4):
     region, differentiable with respect to the vertex tensor V (nv x 3)."""
     return _Scatter.apply(V, topology, complex(Omega), [(tuple(E0), tuple(nh)) for E0, nh in waves], precision,
                           rel_step)
+
+
+class _ScatteredPower(torch.autograd.Function):
+    """EMT scattered power of the solutions x (one value per column) as a
+    function of x and of the vertices V (the exterior region's matrix in its
+    quadratic form depends on V)."""
+
+    @staticmethod
+    def forward(ctx, x, V, topology, Omega, rel_step):
+        geo = topology.geometry(V.detach().cpu().numpy())
+        xn = x.detach().resolve_conj().cpu().numpy().astype(np.complex128)
+        _, ps = geo.GetPFT(Omega, xn)
+        ctx.geo, ctx.Omega, ctx.rel_step, ctx.x = geo, Omega, rel_step, xn
+        ctx.vdevice, ctx.vdtype = V.device, V.dtype
+        return torch.from_numpy(np.asarray(ps, dtype=np.float64)).to(x.device)
+
+    @staticmethod
+    def backward(ctx, gp):
+        geo, x = ctx.geo, ctx.x
+        w = gp.detach().cpu().numpy().astype(np.float64)
+        gx = geo.ScatteredPowerGrad(ctx.Omega, x) * w[None, :]
+        # explicit part: P = 1/2 sum Re(w_ij M0_ij) with M0 the exterior
+        # region's matrix; w = conj(l1) x1^T + conj(l2) x2^T with c = D x
+        # (D = 1 on K rows, -ZVAC on N rows):
+        #   l1 = p c, x1 = q c, l2 = p' conj(c), x2 = q' conj(c),
+        #   p = (1, 1/ZVAC), q = (-ZVAC/2, 1/2), p' = (1, -1/ZVAC), q' = (-ZVAC/2, -1/2) on (K, N) rows
+        nrow = np.asarray(geo.basis_types()) == 1
+        d = np.where(nrow, -ZVAC, 1.0)[:, None]
+        c = d * x
+        p = np.where(nrow, 1.0 / ZVAC, 1.0)[:, None]
+        q = np.where(nrow, 0.5, -0.5 * ZVAC)[:, None]
+        pp = np.where(nrow, -1.0 / ZVAC, 1.0)[:, None]
+        qq = np.where(nrow, -0.5, -0.5 * ZVAC)[:, None]
+        lam = np.concatenate([p * c * w[None, :], pp * np.conj(c) * w[None, :]], axis=1)
+        xx = np.concatenate([q * c, qq * np.conj(c)], axis=1)
+        gV = 0.5 * geo.VertexVJPRegion(ctx.Omega, 0, lam, xx, rel_step=ctx.rel_step)
+        return (torch.from_numpy(gx), torch.from_numpy(gV).to(device=ctx.vdevice, dtype=ctx.vdtype), None, None,
+                None)
+
+
+def scattered_power(x, V, topology, Omega, rel_step=1e-4):
+    """EMT scattered power per column of x (the reference's default power
+    method, GetPFT with EMT, EMTPFT.cc:642-700), differentiable with respect
+    to x and to the vertex tensor V."""
+    return _ScatteredPower.apply(x, V, topology, complex(Omega), rel_step)
+
+
+def absorbed_power(x, b, V, topology, Omega, rel_step=1e-4):
+    """Absorbed power per column: extinction minus scattered power (the
+    reference's EMT split, EMTPFT.cc:305-392), differentiable with respect to
+    the solutions, the right-hand sides and the vertices."""
+    types = topology.geometry(V.detach().cpu().numpy()).basis_types()
+    return extinction_power(x, b, types) - scattered_power(x, V, topology, Omega, rel_step)
 
 
 def extinction_power(x, b, types):

@@ -344,6 +344,31 @@ class RWGGeometry:
         check(lib().gbem_geometry_num_vertices(self._h, ctypes.byref(n)))
         return n.value
 
+    def VertexVJPRegion(self, Omega, region, lam, x, rel_step=1e-4):
+        """VertexVJP for one region's matrix alone, with exterior-region signs
+        (gbem_vertex_vjp_region; region 0: the EMT power's matrix)."""
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        lam = np.asfortranarray(np.asarray(lam, dtype=np.complex128).reshape(self.TotalBFs, -1))
+        x = np.asfortranarray(np.asarray(x, dtype=np.complex128).reshape(self.TotalBFs, -1))
+        if lam.shape != x.shape:
+            raise ValueError("lam and x need the same shape")
+        g = np.zeros((self.NumVertices, 3))
+        check(lib().gbem_vertex_vjp_region(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data, region,
+                                           x.shape[1], lam.ctypes.data, self.TotalBFs, x.ctypes.data, self.TotalBFs,
+                                           float(rel_step), g.ctypes.data))
+        return g
+
+    def ScatteredPowerGrad(self, Omega, KN):
+        """dP_scat/dRe KN + i dP_scat/dIm KN per column (gbem_power_emt_grad)."""
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        KN = np.asfortranarray(np.asarray(KN, dtype=np.complex128).reshape(self.TotalBFs, -1))
+        G = np.zeros_like(KN, order="F")
+        check(lib().gbem_power_emt_grad(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data, KN.shape[1],
+                                        KN.ctypes.data, self.TotalBFs, G.ctypes.data, self.TotalBFs))
+        return G
+
     def VertexVJP(self, Omega, lam, x, rel_step=1e-4):
         """Re sum conj(lam) (dM/dV) x over the columns of lam and x (N x nrhs):
         the adjoint contraction with the vertex derivatives of the full BEM
@@ -390,6 +415,22 @@ class RWGGeometry:
                 t[off + 1:off + 2 * ne:2] = 1
                 off += 2 * ne
         return t
+
+    def solve_refined(self, Omega, B, tol=1e-12, max_iter=20):
+        """The FP64 solve by refinement (gbem_solve_refined): FP64 matrix,
+        complex64 tensor-core LU of its rounding, FP64 residuals against the
+        FP64 matrix.  Returns (X, iterations, relative residual)."""
+        eps, mu = self.eps_mu(Omega)
+        Omega = complex(Omega)
+        B = np.asfortranarray(np.asarray(B, dtype=np.complex128).reshape(self.TotalBFs, -1))
+        X = np.zeros_like(B, order="F")
+        it, res = ctypes.c_int(), ctypes.c_double()
+        st = lib().gbem_solve_refined(self._h, Omega.real, Omega.imag, eps.ctypes.data, mu.ctypes.data, B.shape[1],
+                                      B.ctypes.data, self.TotalBFs, X.ctypes.data, self.TotalBFs, tol, max_iter,
+                                      ctypes.byref(it), ctypes.byref(res))
+        if st not in (_lib.GBEM_OK, _lib.GBEM_ENOCONV):
+            check(st)
+        return X, it.value, res.value
 
     def solve_mixed(self, Omega, B, tol=1e-10, max_iter=10):
         """Mixed-precision solve (FP32 far field, complex-FP32 LU, FP64
