@@ -1028,12 +1028,28 @@ gbem_status gbem_sp_solve_host(const void* AP, int N, int dtype, const int* ipiv
     set_error("gbem_sp_solve_host: bad arguments (dtype C128 or F64)");
     return GBEM_EINVAL;
   }
-  for (int k = 0; k < N; k++) {
-    const int c = ipiv[k];
-    if (c == 0 || c > N || c < -N || (c < 0 && !((k > 0 && ipiv[k - 1] == c) || (k + 1 < N && ipiv[k + 1] == c)))) {
-      set_error("gbem_sp_solve_host: ipiv[%d] = %d is not a pivot code of gbem_sp_factor_host", k, c);
+  // the solve walks the pivot codes downwards (1 x 1 steps, or 2 x 2 steps
+  // over k-1, k) and upwards (k, k+1): both walks must stay inside [0, N)
+  for (int k = 0; k < N; k++)
+    if (ipiv[k] == 0 || ipiv[k] > N || ipiv[k] < -N) {
+      set_error("gbem_sp_solve_host: ipiv[%d] = %d is not a pivot code of gbem_sp_factor_host", k, ipiv[k]);
       return GBEM_EINVAL;
     }
+  for (int k = N - 1; k >= 0;) {
+    if (ipiv[k] > 0) { k -= 1; continue; }
+    if (k < 1 || ipiv[k - 1] != ipiv[k]) {
+      set_error("gbem_sp_solve_host: ipiv[%d] = %d opens a 2 x 2 block without its partner", k, ipiv[k]);
+      return GBEM_EINVAL;
+    }
+    k -= 2;
+  }
+  for (int k = 0; k < N;) {
+    if (ipiv[k] > 0) { k += 1; continue; }
+    if (k + 1 >= N || ipiv[k + 1] != ipiv[k]) {
+      set_error("gbem_sp_solve_host: ipiv[%d] = %d opens a 2 x 2 block without its partner", k, ipiv[k]);
+      return GBEM_EINVAL;
+    }
+    k += 2;
   }
   const size_t es = esize(dtype), np = (size_t)N * (N + 1) / 2;
   cudaStream_t s;
