@@ -136,9 +136,12 @@ def lu_update_flops(N, w=256):
 CONFIG_WORKLOAD = "dielectric icosphere s=%d, N=%d, eps=2.25+0.01i, kR=2, %d plane-wave RHS"
 
 
-def bench_config(subdiv, N, nrhs, world=1):
+def bench_config(subdiv, N, nrhs, world=1, pec=False):
     """The workload dict both arms print (identical keys and values)."""
-    return {"workload": CONFIG_WORKLOAD % (subdiv, N, nrhs),
+    wl = CONFIG_WORKLOAD % (subdiv, N, nrhs)
+    if pec:
+        wl = "PEC icosphere s=%d, N=%d, kR=2, %d plane-wave RHS" % (subdiv, N, nrhs)
+    return {"workload": wl,
             "l2": "inputs larger than L2 (C64 matrix %.2f GB, C128 %.2f GB)" % (N * N * 8 / 1e9, N * N * 16 / 1e9),
             "parallelism": "replicas" if world > 1 else "single GPU"}
 
@@ -384,6 +387,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbem", choices=["gbem", "reference"])
     ap.add_argument("--subdiv", type=int, default=4)
+    ap.add_argument("--pec", action="store_true",
+                    help="a PEC sphere instead of the dielectric one (N = 30 * 4^s; for profiling runs)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fp64-reps", type=int, default=5, help="plain FP64 solves timed (median reported)")
@@ -391,6 +396,8 @@ def main():
                     help="solve: the headline N=15360 mixed solve; batch: 48 geometries x 16 frequencies; "
                          "large: the N=61440 sphere; casimir: the two-sphere Casimir sweep")
     args = ap.parse_args()
+    if args.pec:
+        args.no_fp64 = True  # the accuracy report assumes the dielectric's K/N interleaving
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
@@ -414,7 +421,7 @@ def main():
     from gbem._lib import check, lib
 
     V, P = workload(args.subdiv)
-    G = RWGGeometry([{"V": V, "P": P, "material": Material(2.25 + 0.01j)}], device=local)
+    G = RWGGeometry([{"V": V, "P": P, "material": None if args.pec else Material(2.25 + 0.01j)}], device=local)
     N = G.TotalBFs
     w = 2.0
     stream = torch.cuda.current_stream()
@@ -488,7 +495,7 @@ def main():
     out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "c64+fp64-refine", "data": "synthetic",
-           "config": bench_config(args.subdiv, N, nrhs, world),
+           "config": bench_config(args.subdiv, N, nrhs, world, args.pec),
            "method": "mixed: float-float far field + FP64 near field -> C64, split-BF16 tensor-core LU, "
                      "FP64 refinement to 1e-10",
            "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "solves/s",

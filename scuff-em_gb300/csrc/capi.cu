@@ -3,6 +3,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <map>
+#include <complex>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -1204,6 +1205,167 @@ __global__ void colnorm2(const double2* a, int N, int nrhs, double* out) {
   if (threadIdx.x == 0) out[r] = red[0];
 }
 
+__global__ void c64_to_c128(const float2* a, double2* b, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = make_double2((double)a[i].x, (double)a[i].y);
+}
+__global__ void add_c128(double2* x, const double2* d, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) { x[i].x += d[i].x; x[i].y += d[i].y; }
+}
+
+// GMRES-based refinement, for matrices whose conditioning defeats plain
+// refinement with the complex64 factor (kappa(A) u_f >~ 1: low frequencies,
+// fine meshes).  Each outer step solves the correction equation A d = r,
+// r = b - A x from the FP64 residual, by restarted GMRES(m) on the
+// left-preconditioned system (LU)^-1 A d = (LU)^-1 r (Carson & Higham's
+// GMRES-IR): products with A as in the residual (double-float accumulation
+// on a complex64 matrix, FP64 on a complex128 one), the preconditioner by the
+// complex64 triangular solves, the Krylov basis and the small Hessenberg
+// problems on the host in FP64.  All right-hand sides advance together.
+static gbem_status gmres_refine(const void* dA, int adtype, gbem_matrix* F, int N, int nrhs, const double2* dB,
+                                double2* dX, double2* dR, float2* dD, void* dY, void* part, const std::vector<double>& bn,
+                                double tol, int max_outer, int* iters, double* rel_out, cudaStream_t s) {
+  typedef std::complex<double> C;
+  const int m = 40;
+  const size_t nel = (size_t)N * nrhs;
+  const unsigned nb = (unsigned)((nel + 255) / 256);
+  double2 *dV = nullptr, *dW = nullptr, *dZ = nullptr;
+  double* dn = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&dV, nel * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&dW, nel * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&dZ, nel * 16, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&dn, sizeof(double) * nrhs, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dZ, 0, nel * 16, s);
+  gbem_status st = cuda_status(e, "GMRES workspace");
+  std::vector<C> V((size_t)(m + 1) * nel), w(nel), H((size_t)(m + 1) * m * nrhs), g((size_t)(m + 1) * nrhs);
+  std::vector<C> cs((size_t)m * nrhs), sn((size_t)m * nrhs);
+  std::vector<double> rn(nrhs);
+  // z = (LU)^-1 v for the nrhs columns of the device array src (complex128)
+  auto precond = [&](const double2* src, std::vector<C>& out) -> gbem_status {
+    to_c64<<<nb, 256, 0, s>>>(src, dD, nel);
+    stats_launch(ST_OTHER);
+    gbem_status q = lu_solve_device(F->d, N, N, GBEM_C64, F->d_perm, 'N', nrhs, dD, N, dY, s);
+    if (q != GBEM_OK) return q;
+    c64_to_c128<<<nb, 256, 0, s>>>(dD, dW, nel);
+    stats_launch(ST_OTHER);
+    cudaError_t ee = cudaMemcpyAsync(out.data(), dW, nel * 16, cudaMemcpyDeviceToHost, s);
+    if (ee == cudaSuccess) ee = cudaStreamSynchronize(s);
+    return cuda_status(ee, "GMRES preconditioner");
+  };
+  auto residual_norms = [&](double* rel) -> gbem_status {
+    gbem_status q = residual_device(dA, N, adtype, N, (const double*)dX, N, (const double*)dB, N, nrhs, (double*)dR, N,
+                                    part, s);
+    if (q != GBEM_OK) return q;
+    colnorm2<<<nrhs, 256, 0, s>>>(dR, N, nrhs, dn);
+    stats_launch(ST_OTHER);
+    cudaError_t ee = cudaMemcpyAsync(rn.data(), dn, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s);
+    if (ee == cudaSuccess) ee = cudaStreamSynchronize(s);
+    if (ee != cudaSuccess) return cuda_status(ee, "GMRES residual");
+    *rel = 0.0;
+    for (int r = 0; r < nrhs; r++) *rel = std::fmax(*rel, std::sqrt(rn[r] / (bn[r] > 0 ? bn[r] : 1.0)));
+    return GBEM_OK;
+  };
+  double rel = *rel_out;
+  for (int outer = 0; st == GBEM_OK && outer < max_outer && rel > tol; outer++) {
+    // preconditioned residual, the first Krylov vector of every column
+    std::vector<C> z(nel);
+    st = precond(dR, z);
+    if (st != GBEM_OK) break;
+    std::vector<double> beta(nrhs);
+    for (int c = 0; c < nrhs; c++) {
+      double nz = 0.0;
+      for (int i = 0; i < N; i++) nz += std::norm(z[(size_t)c * N + i]);
+      beta[c] = std::sqrt(nz);
+      for (int i = 0; i < N; i++) V[(size_t)c * N + i] = beta[c] > 0 ? z[(size_t)c * N + i] / beta[c] : C(0.0);
+      for (int j = 0; j <= m; j++) g[(size_t)c * (m + 1) + j] = 0.0;
+      g[(size_t)c * (m + 1)] = beta[c];
+    }
+    int kmax = 0;
+    for (int j = 0; j < m; j++) {
+      // w = (LU)^-1 A v_j: A v_j = -(0 - A v_j) by the residual kernel
+      e = cudaMemcpyAsync(dV, V.data() + (size_t)j * nel, nel * 16, cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) { st = cuda_status(e, "GMRES upload"); break; }
+      st = residual_device(dA, N, adtype, N, (const double*)dV, N, (const double*)dZ, N, nrhs, (double*)dW, N, part, s);
+      if (st != GBEM_OK) break;
+      std::vector<C>& wv = w;
+      // dW = -A v_j; precondition it (dW is overwritten by the result)
+      e = cudaMemcpyAsync(dV, dW, nel * 16, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) { st = cuda_status(e, "GMRES copy"); break; }
+      st = precond(dV, wv);
+      if (st != GBEM_OK) break;
+      bool all_small = true;
+      for (int c = 0; c < nrhs; c++) {
+        C* wc = wv.data() + (size_t)c * N;
+        for (int i = 0; i < N; i++) wc[i] = -wc[i];
+        C* Hc = H.data() + (size_t)c * (m + 1) * m;  // column-major (m+1) x m
+        // modified Gram-Schmidt against v_0 .. v_j
+        for (int i = 0; i <= j; i++) {
+          const C* vi = V.data() + (size_t)i * nel + (size_t)c * N;
+          C h = 0.0;
+          for (int q = 0; q < N; q++) h += std::conj(vi[q]) * wc[q];
+          Hc[i + (size_t)j * (m + 1)] = h;
+          for (int q = 0; q < N; q++) wc[q] -= h * vi[q];
+        }
+        double hn = 0.0;
+        for (int q = 0; q < N; q++) hn += std::norm(wc[q]);
+        hn = std::sqrt(hn);
+        Hc[j + 1 + (size_t)j * (m + 1)] = hn;
+        C* vn = V.data() + (size_t)(j + 1) * nel + (size_t)c * N;
+        for (int q = 0; q < N; q++) vn[q] = hn > 0 ? wc[q] / hn : C(0.0);
+        // Givens rotations on column j of H and on g
+        C* csc = cs.data() + (size_t)c * m;
+        C* snc = sn.data() + (size_t)c * m;
+        C* gc = g.data() + (size_t)c * (m + 1);
+        for (int i = 0; i < j; i++) {
+          const C a = Hc[i + (size_t)j * (m + 1)], b = Hc[i + 1 + (size_t)j * (m + 1)];
+          Hc[i + (size_t)j * (m + 1)] = std::conj(csc[i]) * a + std::conj(snc[i]) * b;
+          Hc[i + 1 + (size_t)j * (m + 1)] = -snc[i] * a + csc[i] * b;
+        }
+        const C a = Hc[j + (size_t)j * (m + 1)], b = Hc[j + 1 + (size_t)j * (m + 1)];
+        const double den = std::sqrt(std::norm(a) + std::norm(b));
+        csc[j] = den > 0 ? a / den : C(1.0);
+        snc[j] = den > 0 ? b / den : C(0.0);
+        Hc[j + (size_t)j * (m + 1)] = den;
+        Hc[j + 1 + (size_t)j * (m + 1)] = 0.0;
+        gc[j + 1] = -snc[j] * gc[j];
+        gc[j] = std::conj(csc[j]) * gc[j];
+        if (std::abs(gc[j + 1]) > 1e-7 * beta[c]) all_small = false;
+      }
+      kmax = j + 1;
+      if (all_small) break;
+    }
+    if (st != GBEM_OK) break;
+    // d = V y with H y = g (upper triangular, kmax x kmax), per column
+    std::vector<C> d(nel, C(0.0));
+    for (int c = 0; c < nrhs; c++) {
+      C* Hc = H.data() + (size_t)c * (m + 1) * m;
+      C* gc = g.data() + (size_t)c * (m + 1);
+      std::vector<C> y(kmax);
+      for (int i = kmax - 1; i >= 0; i--) {
+        C t = gc[i];
+        for (int k = i + 1; k < kmax; k++) t -= Hc[i + (size_t)k * (m + 1)] * y[k];
+        const C piv = Hc[i + (size_t)i * (m + 1)];
+        y[i] = std::abs(piv) > 0 ? t / piv : C(0.0);
+      }
+      for (int i = 0; i < kmax; i++) {
+        const C* vi = V.data() + (size_t)i * nel + (size_t)c * N;
+        for (int q = 0; q < N; q++) d[(size_t)c * N + q] += y[i] * vi[q];
+      }
+    }
+    e = cudaMemcpyAsync(dV, d.data(), nel * 16, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) { st = cuda_status(e, "GMRES correction"); break; }
+    add_c128<<<nb, 256, 0, s>>>(dX, dV, nel);
+    stats_launch(ST_OTHER);
+    st = residual_norms(&rel);
+    ++*iters;
+  }
+  cudaFreeAsync(dV, s); cudaFreeAsync(dW, s); cudaFreeAsync(dZ, s); cudaFreeAsync(dn, s);
+  cudaStreamSynchronize(s);
+  *rel_out = rel;
+  return st;
+}
+
 // fp64_matrix: the matrix is assembled in FP64 (complex128), factored as its
 // complex64 rounding, and the refinement residuals are taken against the
 // complex128 matrix itself, so the solution converges to the FP64 solve's;
@@ -1282,8 +1444,9 @@ static gbem_status solve_mixed_impl(gbem_geometry* g, double omega_re, double om
     if (e != cudaSuccess) st = cuda_status(e, "norm");
   }
   int it = 0;
-  double rel = 1.0;
+  double rel = 1.0, prev_rel = 2.0;
   size_t nel = (size_t)N * nrhs;
+  bool stalled = false;
   while (st == GBEM_OK && it < max_iter) {
     to_c64<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>((const double2*)dR, (float2*)dD, nel);
     stats_launch(ST_OTHER);
@@ -1311,6 +1474,15 @@ static gbem_status solve_mixed_impl(gbem_geometry* g, double omega_re, double om
     rel = 0;
     for (int r = 0; r < nrhs; r++) rel = std::fmax(rel, std::sqrt(rn[r] / (bn[r] > 0 ? bn[r] : 1.0)));
     if (rel <= tol) break;
+    // plain refinement contracts by ~kappa u_f per sweep; when that is not
+    // well below one (or the residual grows) it will not reach tol
+    if (it >= 2 && !(rel < 0.2 * prev_rel)) { stalled = true; break; }
+    prev_rel = rel;
+  }
+  if (st == GBEM_OK && rel > tol && (stalled || it >= max_iter)) {
+    const void* dA = fp64_matrix ? M128->d : M->d;
+    st = gmres_refine(dA, fp64_matrix ? GBEM_C128 : GBEM_C64, F, N, nrhs, (const double2*)dB, (double2*)dX,
+                      (double2*)dR, (float2*)dD, dY, part, bn, tol, max_iter, &it, &rel, s);
   }
   if (st == GBEM_OK) {
     e = cudaMemcpy2DAsync(X, (size_t)ldx * 16, dX, (size_t)N * 16, (size_t)N * 16, nrhs,

@@ -370,8 +370,10 @@ static int g_tc_mode = -1;  // -1 unknown, 0 disabled, 1 enabled
 
 void tc_gemm_set_enabled(int on) { g_tc_mode = on ? 1 : 0; }
 
+// max_ctas > 0 caps the persistent grid (the rest of the SMs stay free for
+// kernels that run beside this one on another stream)
 bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long lda, const cx<float>* B, long long ldb,
-                    int m, int n, int k, void* ws, size_t ws_bytes, cudaStream_t s, cudaError_t* err) {
+                    int m, int n, int k, void* ws, size_t ws_bytes, cudaStream_t s, cudaError_t* err, int max_ctas) {
   *err = cudaSuccess;
   if (g_tc_mode < 0) {
     const char* e = getenv("GBEM_LU_TC");
@@ -408,7 +410,8 @@ bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long l
   }
   const int mt = (m + tc::BM - 1) / tc::BM, ntn = (2 * n + tc::BN - 1) / tc::BN;
   const int ntiles = mt * ntn;
-  tc_gemm_kernel<<<std::min(ntiles, nsm), 320, tc::SMEM_BYTES, s>>>(ma, mb, C, ldc, m, n, Kp / tc::BK, mt, ntiles);
+  const int grid = std::min(ntiles, max_ctas > 0 ? std::min(max_ctas, nsm) : nsm);
+  tc_gemm_kernel<<<grid, 320, tc::SMEM_BYTES, s>>>(ma, mb, C, ldc, m, n, Kp / tc::BK, mt, ntiles);
   *err = cudaGetLastError();
   return *err == cudaSuccess;
 }

@@ -129,3 +129,47 @@ def test_batch_matches_individual_solves():
     for (X, it, res), Xr in zip(out, ref):
         assert res <= 1e-10 and it >= 1
         assert np.abs(X - Xr).max() <= 1e-12 * np.abs(Xr).max()
+
+
+def test_refined_solve_is_the_fp64_solve():
+    """gbem_solve_refined: FP64 matrix, tensor-core LU of its complex64
+    rounding, FP64 residuals against the FP64 matrix -- the FP64 solve's
+    solution to the refinement tolerance."""
+    import scipy.linalg as sl
+    from gbem import RWGGeometry, mesh
+    from gbem.api import Material
+    V, P = mesh.icosphere(2)
+    G = RWGGeometry([{"V": V, "P": P, "material": Material(2.25 + 0.01j)}])
+    w = 2.0
+    B = np.stack([G.AssembleRHSVector(w, e, n) for e, n in [((1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, -1))]], axis=1)
+    X, it, res = G.solve_refined(w, B, tol=1e-13)
+    assert res <= 1e-13
+    M64 = G.AssembleBEMMatrix(w).numpy()
+    X64 = sl.solve(M64, B)
+    assert np.abs(X - X64).max() / np.abs(X64).max() < 1e-11
+
+
+def test_gmres_refinement_on_an_ill_conditioned_matrix():
+    """At low frequency the PMCHWT matrix of a fine jittered mesh is
+    ill-conditioned enough that plain refinement with the complex64 factor
+    diverges (the batching workload's second geometry, a seeded rounded cube
+    of 2700 panels, N = 8100, at kR = 0.1); the solve switches to GMRES-based
+    refinement preconditioned by the same factor and reaches the tolerance,
+    against the FP64 solution."""
+    from gbem import RWGGeometry, mesh
+    from gbem.api import Material
+    rng = np.random.default_rng(0)  # the batching workload's draws, seed 0
+    rng.uniform(1.5, 4.0), rng.uniform(0.0, 0.1), rng.uniform(0.5, 1.5)
+    eps = complex(rng.uniform(1.5, 4.0), rng.uniform(0.0, 0.1))
+    npan = int(rng.uniform(600, 3000))
+    V, P = mesh.rounded_cube(npan, side=1.0, seed=int(rng.integers(1 << 30)))
+    G = RWGGeometry([{"V": V, "P": P, "material": Material(eps)}])
+    w = 0.1 / 0.5
+    B = np.stack([G.AssembleRHSVector(w, e, n) for e, n in [((1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1))]], axis=1)
+    X, it, res = G.solve_mixed(w, B, tol=1e-10, max_iter=12)
+    print("rounded cube N=%d kR=0.1: sweeps %d, residual %.2e" % (G.TotalBFs, it, res))
+    assert res <= 1e-10
+    M = G.AssembleBEMMatrix(w)
+    assert M.LUFactorize() == 0
+    X64 = M.LUSolve(B)
+    assert np.abs(X - X64).max() / np.abs(X64).max() < 1e-5
