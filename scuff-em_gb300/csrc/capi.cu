@@ -1444,45 +1444,71 @@ static gbem_status solve_mixed_impl(gbem_geometry* g, double omega_re, double om
     if (e != cudaSuccess) st = cuda_status(e, "norm");
   }
   int it = 0;
-  double rel = 1.0, prev_rel = 2.0;
+  double rel = 1.0;
   size_t nel = (size_t)N * nrhs;
-  bool stalled = false;
-  while (st == GBEM_OK && it < max_iter) {
-    to_c64<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>((const double2*)dR, (float2*)dD, nel);
-    stats_launch(ST_OTHER);
-    {
-      StatTimer t(ST_SOLVE, s);
-      st = lu_solve_device(F->d, N, N, GBEM_C64, F->d_perm, 'N', nrhs, dD, N, dY, s);
+  const void* dA = fp64_matrix ? M128->d : M->d;
+  const int adt = fp64_matrix ? GBEM_C128 : GBEM_C64;
+  // refinement sweeps x <- x + (LU)^-1 r, r = b - A x in FP64, until rel <=
+  // tol; false when the sweeps stop contracting: plain refinement contracts
+  // by ~kappa(A) u_f per sweep, and when that is not well below one (or the
+  // residual grows) it will not reach tol
+  auto refine = [&](int max_sweeps) -> bool {
+    double prev = 2.0;
+    for (int sw = 0; st == GBEM_OK && sw < max_sweeps; sw++) {
+      to_c64<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>((const double2*)dR, (float2*)dD, nel);
+      stats_launch(ST_OTHER);
+      {
+        StatTimer t(ST_SOLVE, s);
+        st = lu_solve_device(F->d, N, N, GBEM_C64, F->d_perm, 'N', nrhs, dD, N, dY, s);
+      }
+      if (st != GBEM_OK) break;
+      add_c64<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>((double2*)dX, (const float2*)dD, nel);
+      stats_launch(ST_OTHER);
+      {
+        StatTimer t(ST_RESID, s);
+        st = residual_device(dA, N, adt, N, (const double*)dX, N, (const double*)dB, N, nrhs, (double*)dR, N, part, s);
+      }
+      if (st != GBEM_OK) break;
+      colnorm2<<<nrhs, 256, 0, s>>>((const double2*)dR, N, nrhs, dn);
+      stats_launch(ST_OTHER);
+      e = cudaMemcpyAsync(rn.data(), dn, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) { st = cuda_status(e, "refinement"); break; }
+      it++;
+      rel = 0;
+      for (int r = 0; r < nrhs; r++) rel = std::fmax(rel, std::sqrt(rn[r] / (bn[r] > 0 ? bn[r] : 1.0)));
+      if (rel <= tol) return true;
+      if (sw >= 1 && !(rel < 0.2 * prev)) return false;
+      prev = rel;
     }
-    if (st != GBEM_OK) break;
-    add_c64<<<(unsigned)((nel + 255) / 256), 256, 0, s>>>((double2*)dX, (const float2*)dD, nel);
-    stats_launch(ST_OTHER);
-    {
-      StatTimer t(ST_RESID, s);
-      st = fp64_matrix ? residual_device(M128->d, N, GBEM_C128, N, (const double*)dX, N, (const double*)dB, N, nrhs,
-                                         (double*)dR, N, part, s)
-                       : residual_device(M->d, N, GBEM_C64, N, (const double*)dX, N, (const double*)dB, N, nrhs,
-                                         (double*)dR, N, part, s);
+    return rel <= tol;
+  };
+  bool ok = refine(max_iter);
+  if (st == GBEM_OK && !ok) {
+    // the split-BF16 factor is too coarse for this matrix: factor it again
+    // with exact FP32 trailing updates (backward error ~1e-7 instead of
+    // ~1e-4) and restart the refinement from x = 0
+    if (fp64_matrix) {
+      const size_t nn = (size_t)N * N;
+      to_c64<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>((const double2*)M128->d, (float2*)F->d, nn);
+      stats_launch(ST_OTHER);
+      e = cudaGetLastError();
+    } else {
+      e = cudaMemcpyAsync(F->d, M->d, (size_t)N * N * 8, cudaMemcpyDeviceToDevice, s);
     }
-    if (st != GBEM_OK) break;
-    colnorm2<<<nrhs, 256, 0, s>>>((const double2*)dR, N, nrhs, dn);
-    stats_launch(ST_OTHER);
-    e = cudaMemcpyAsync(rn.data(), dn, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) { st = cuda_status(e, "refinement"); break; }
-    it++;
-    rel = 0;
-    for (int r = 0; r < nrhs; r++) rel = std::fmax(rel, std::sqrt(rn[r] / (bn[r] > 0 ? bn[r] : 1.0)));
-    if (rel <= tol) break;
-    // plain refinement contracts by ~kappa u_f per sweep; when that is not
-    // well below one (or the residual grows) it will not reach tol
-    if (it >= 2 && !(rel < 0.2 * prev_rel)) { stalled = true; break; }
-    prev_rel = rel;
-  }
-  if (st == GBEM_OK && rel > tol && (stalled || it >= max_iter)) {
-    const void* dA = fp64_matrix ? M128->d : M->d;
-    st = gmres_refine(dA, fp64_matrix ? GBEM_C128 : GBEM_C64, F, N, nrhs, (const double2*)dB, (double2*)dX,
-                      (double2*)dR, (float2*)dD, dY, part, bn, tol, max_iter, &it, &rel, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dX, 0, nel * 16, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dR, dB, nel * 16, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) st = cuda_status(e, "refactor");
+    if (st == GBEM_OK) {
+      tc_gemm_thread_off(1);
+      st = gbem_lu_factor(F, nullptr, &info);
+      tc_gemm_thread_off(0);
+    }
+    if (st == GBEM_OK) ok = refine(max_iter);
+    // then GMRES-based refinement preconditioned by that factor
+    if (st == GBEM_OK && !ok)
+      st = gmres_refine(dA, adt, F, N, nrhs, (const double2*)dB, (double2*)dX, (double2*)dR, (float2*)dD, dY, part, bn,
+                        tol, max_iter, &it, &rel, s);
   }
   if (st == GBEM_OK) {
     e = cudaMemcpy2DAsync(X, (size_t)ldx * 16, dX, (size_t)N * 16, (size_t)N * 16, nrhs,

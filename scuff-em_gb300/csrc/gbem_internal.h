@@ -178,6 +178,10 @@ gbem_status lu_solve_static_scratch(const void* dA, int N, int ld, int dtype, co
                                     void* hB, int ldb, cudaStream_t s);
 int lu_solve_noalloc_max_n(int dtype);
 
+// gemm_tc.cu: keep the calling host thread's LU factorisations off the
+// split-BF16 tensor-core updates (exact FP32 SIMT updates instead)
+void tc_gemm_thread_off(int off);
+
 // sptrf.cu: symmetric matrices in LAPACK's upper packed storage
 // (Bunch-Kaufman A = U D U^T, dsptrf/zsptrf semantics); dtype F64 or C128
 gbem_status sp_factor_device(void* dAP, int N, int dtype, int* dipiv, int* h_info, cudaStream_t s);

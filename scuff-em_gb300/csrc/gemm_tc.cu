@@ -367,19 +367,19 @@ size_t tc_gemm_ws_bytes(int m, int n, int k) {
 }
 
 static int g_tc_mode = -1;  // -1 unknown, 0 disabled, 1 enabled
+static thread_local int tl_tc_off = 0;  // this host thread's LU takes the FP32 SIMT updates
 
 void tc_gemm_set_enabled(int on) { g_tc_mode = on ? 1 : 0; }
+void tc_gemm_thread_off(int off) { tl_tc_off = off; }
 
-// max_ctas > 0 caps the persistent grid (the rest of the SMs stay free for
-// kernels that run beside this one on another stream)
 bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long lda, const cx<float>* B, long long ldb,
-                    int m, int n, int k, void* ws, size_t ws_bytes, cudaStream_t s, cudaError_t* err, int max_ctas) {
+                    int m, int n, int k, void* ws, size_t ws_bytes, cudaStream_t s, cudaError_t* err) {
   *err = cudaSuccess;
   if (g_tc_mode < 0) {
     const char* e = getenv("GBEM_LU_TC");
     g_tc_mode = (e && e[0] == '0') ? 0 : 1;
   }
-  if (g_tc_mode == 0) return false;
+  if (g_tc_mode == 0 || tl_tc_off) return false;
   if (m <= 0 || n <= 0 || k <= 0) return true;
   int Kp = pad64(6 * k);
   size_t need = ((size_t)m + 2 * (size_t)n) * Kp * 2;
@@ -410,8 +410,7 @@ bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long l
   }
   const int mt = (m + tc::BM - 1) / tc::BM, ntn = (2 * n + tc::BN - 1) / tc::BN;
   const int ntiles = mt * ntn;
-  const int grid = std::min(ntiles, max_ctas > 0 ? std::min(max_ctas, nsm) : nsm);
-  tc_gemm_kernel<<<grid, 320, tc::SMEM_BYTES, s>>>(ma, mb, C, ldc, m, n, Kp / tc::BK, mt, ntiles);
+  tc_gemm_kernel<<<std::min(ntiles, nsm), 320, tc::SMEM_BYTES, s>>>(ma, mb, C, ldc, m, n, Kp / tc::BK, mt, ntiles);
   *err = cudaGetLastError();
   return *err == cudaSuccess;
 }

@@ -29,8 +29,7 @@ namespace gbem {
 
 // tensor-core trailing update (gemm_tc.cu); returns false if unavailable
 bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long lda, const cx<float>* B,
-                    long long ldb, int m, int n, int k, void* ws, size_t ws_bytes, cudaStream_t s, cudaError_t* err,
-                    int max_ctas = 0);
+                    long long ldb, int m, int n, int k, void* ws, size_t ws_bytes, cudaStream_t s, cudaError_t* err);
 size_t tc_gemm_ws_bytes(int m, int n, int k);
 int tc_gemm_error(bool reset);
 
@@ -1112,12 +1111,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   if (sizeof(T) == 4) tcb = tc_gemm_ws_bytes(N, N, w);
   const size_t dinv_bytes = (size_t)((N + 31) / 32) * 1024 * esz;
   const size_t swap_bytes = sizeof(int) * (4 * 256 + 16);
-  // look-ahead (complex FP32 with cluster leaves): the trailing update's tail
-  // runs on a second stream, beside the next panel, with its own operand scratch
-  const char* la_env = getenv("GBEM_LU_LOOKAHEAD");
-  const bool lookahead = sizeof(T) == 4 && leaf_cl && tcb && !(la_env && la_env[0] == '0') && N > 2 * w;
-  const size_t tcb2 = lookahead ? tcb : 0;
-  size_t total = need + tcb + 1024 + dinv_bytes + 256 + swap_bytes + 256 + tcb2 + 1024;
+  size_t total = need + tcb + 1024 + dinv_bytes + 256 + swap_bytes + 256;
   if (*ws_bytes < total) {
     if (*ws) cudaFree(*ws);
     *ws = nullptr;
@@ -1136,27 +1130,6 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   cx<T>* dinv = (cx<T>*)(((uintptr_t)tcws + tcb + 255) & ~(uintptr_t)255);
   int* swap_mv = (int*)(((uintptr_t)((unsigned char*)dinv + dinv_bytes) + 255) & ~(uintptr_t)255);
   int* swap_n = swap_mv + 4 * 256;
-  void* tcws2 = lookahead ? (void*)(((uintptr_t)(swap_n + 16) + 1023) & ~(uintptr_t)1023) : nullptr;
-  cudaStream_t s2 = nullptr;
-  cudaEvent_t ev_u12 = nullptr, ev_tail = nullptr;
-  bool tail_pending = false;
-  if (lookahead) {
-    e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_u12, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_tail, cudaEventDisableTiming);
-    if (e != cudaSuccess) return cuda_status(e, "look-ahead stream");
-  }
-  // the persistent tail update leaves one leaf cluster's SMs free
-  const int tail_ctas = std::max(1, nsm - std::max(leaf_cl, 16));
-  struct LookaheadGuard {
-    cudaStream_t s, s2;
-    cudaEvent_t a, b;
-    ~LookaheadGuard() {
-      if (s2) { cudaStreamSynchronize(s2); cudaStreamDestroy(s2); }
-      if (a) cudaEventDestroy(a);
-      if (b) cudaEventDestroy(b);
-    }
-  } guard{s, s2, ev_u12, ev_tail};
   DinvState ds;
   ds.dinv = (cx<float>*)dinv;
   ds.made.assign((N + 31) / 32, 0);
@@ -1188,13 +1161,6 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
         stats_launch(ST_PANEL, 1);
         e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(512), args, sm, s);
         if (e != cudaSuccess) return cuda_status(e, "panel_kernel");
-      }
-      // the previous step's tail update (other stream) must finish before
-      // this panel's interchanges touch the columns it writes
-      if (tail_pending) {
-        e = cudaStreamWaitEvent(s, ev_tail, 0);
-        if (e != cudaSuccess) return cuda_status(e, "look-ahead wait");
-        tail_pending = false;
       }
       // interchanges to the left and right of the panel
       swap_compose<<<1, 256, 0, s>>>(d_ipiv, c0, c0 + wc, swap_mv, swap_n);
@@ -1250,38 +1216,12 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
         trsm_kernel<T><<<(nrest + 31) / 32, 256, tsm, s>>>(A, ld, c0, wc, cb, N);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
     }
+    StatTimer tg(ST_GEMM, s);
     cx<T>* C = A + cb + (long long)cb * ld;
     const cx<T>* L21 = A + cb + (long long)c0 * ld;
     const cx<T>* U12 = A + c0 + (long long)cb * ld;
     bool done = false;
-    if (lookahead && nrest > wc) {
-      // the next panel's columns now, the rest beside the next panel
-      const int w1 = wc;
-      {
-        StatTimer tg(ST_GEMM, s);
-        done = tc_gemm_update((cx<float>*)C, ld, (const cx<float>*)L21, ld, (const cx<float>*)U12, ld, nrest, w1, wc,
-                              tcws, tcb, s, &e);
-        if (e != cudaSuccess) return cuda_status(e, "tensor-core update");
-        if (done) stats_launch(ST_GEMM, 3);
-      }
-      if (done) {
-        e = cudaEventRecord(ev_u12, s);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, ev_u12, 0);
-        if (e != cudaSuccess) return cuda_status(e, "look-ahead event");
-        StatTimer tg2(ST_GEMM, s2);
-        const bool d2 = tc_gemm_update((cx<float>*)(C + (long long)w1 * ld), ld, (const cx<float>*)L21, ld,
-                                       (const cx<float>*)(U12 + (long long)w1 * ld), ld, nrest, nrest - w1, wc, tcws2,
-                                       tcb2, s2, &e, tail_ctas);
-        if (e != cudaSuccess || !d2) return cuda_status(e != cudaSuccess ? e : cudaErrorInvalidValue, "tail update");
-        stats_launch(ST_GEMM, 3);
-        e = cudaEventRecord(ev_tail, s2);
-        if (e != cudaSuccess) return cuda_status(e, "look-ahead event");
-        tail_pending = true;
-        continue;
-      }
-    }
-    StatTimer tg(ST_GEMM, s);
-    if (sizeof(T) == 4 && !done) {
+    if (sizeof(T) == 4) {
       done = tc_gemm_update((cx<float>*)C, ld, (const cx<float>*)L21, ld, (const cx<float>*)U12, ld, nrest, nrest, wc,
                             tcws, tcb, s, &e);
       if (e != cudaSuccess) return cuda_status(e, "tensor-core update");
@@ -1293,10 +1233,6 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
       stats_launch(ST_GEMM);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "gemm");
     }
-  }
-  if (tail_pending) {
-    e = cudaStreamWaitEvent(s, ev_tail, 0);
-    if (e != cudaSuccess) return cuda_status(e, "look-ahead wait");
   }
   e = cudaMemcpyAsync(h_info, d_info, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
