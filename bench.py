@@ -38,11 +38,11 @@ ZVAC = 376.73031346177
 METRIC = "BEM solves/s at N=15360, mixed-prec vs FP64 on one GB300 @<=1e-6 rel err"
 PLANE_WAVES = [((1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1)), ((1, 0, 0), (0, 0, -1)), ((0, 1, 0), (0, 0, -1))]
 
-# DRAM read + write bytes per trailing-update launch at N = 15360, measured by
-# ncu (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass) over 48 of the 59
-# launches of a factorisation, the 11 smallest estimated from the last captured
-# one's bytes per entry (the capture's summary is kept under profiles/)
-TC_TRAFFIC_BYTES_PER_LAUNCH = 1.45e9
+# DRAM read + write bytes per trailing-update launch at N = 15360: one ncu
+# capture (dram__bytes_read/write.sum) of the first trailing update of the
+# N = 7680 PEC sphere -- 16.4 B per updated complex64 entry -- scaled by the
+# entries each of the 59 updates writes (summary under profiles/)
+TC_TRAFFIC_BYTES_PER_LAUNCH = 1.28e9
 # nominal GB300 CUDA-core rates (the measured-peaks file has HBM and bf16 only)
 FP32_PEAK_TFLOPS = 75.0
 FP64_PEAK_TFLOPS = 1.25
