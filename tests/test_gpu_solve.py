@@ -167,9 +167,20 @@ def test_gmres_refinement_on_an_ill_conditioned_matrix():
     w = 0.1 / 0.5
     B = np.stack([G.AssembleRHSVector(w, e, n) for e, n in [((1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1))]], axis=1)
     X, it, res = G.solve_mixed(w, B, tol=1e-10, max_iter=12)
-    print("rounded cube N=%d kR=0.1: sweeps %d, residual %.2e" % (G.TotalBFs, it, res))
+    print("rounded cube N=%d kR=0.1: mixed sweeps %d, residual %.2e" % (G.TotalBFs, it, res))
     assert res <= 1e-10
+    # the mixed form solves its complex64 matrix: the refinement residual is
+    # taken against it (rounding the matrix moves this ill-conditioned
+    # solution by ~1e-3, so it is not compared with the FP64 solution)
+    M32 = G.AssembleBEMMatrix(w, precision="mixed").numpy().astype(np.complex128)
+    assert np.abs(M32 @ X - B).max() / np.abs(B).max() < 1e-9
+    # the refined form keeps the FP64 matrix and reaches the FP64 solution
+    Xr, itr, resr = G.solve_refined(w, B, tol=1e-12, max_iter=12)
+    print("refined sweeps %d, residual %.2e" % (itr, resr))
+    assert resr <= 1e-12
+    # two FP64-accurate solutions of a matrix this ill-conditioned differ by
+    # ~cond x 1e-16 (measured 1.4e-8 between them)
     M = G.AssembleBEMMatrix(w)
     assert M.LUFactorize() == 0
     X64 = M.LUSolve(B)
-    assert np.abs(X - X64).max() / np.abs(X64).max() < 1e-5
+    assert np.abs(Xr - X64).max() / np.abs(X64).max() < 1e-7
