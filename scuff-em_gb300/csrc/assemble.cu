@@ -314,6 +314,51 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// every lane ends with the warp's totals
+__device__ __forceinline__ void fippi_warp_sum(Fippi& F) {
+#pragma unroll
+  for (int m = 0; m < 9; m++) {
+    F.RM1[m] = warp_sum(F.RM1[m]);
+    F.R1[m] = warp_sum(F.R1[m]);
+    F.R2[m] = warp_sum(F.R2[m]);
+  }
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    F.XM[m] = warp_sum(F.XM[m]);
+    F.XX[m] = warp_sum(F.XX[m]);
+  }
+}
+
+__device__ __forceinline__ void cx_warp_sum(cx<double>* v, int n) {
+  for (int m = 0; m < n; m++) { v[m].re = warp_sum(v[m].re); v[m].im = warp_sum(v[m].im); }
+}
+
+// the static integrals of one near pair by the whole warp (lanes over the
+// rule's points, shuffle-reduced: every lane ends with the totals)
+__device__ void fippi_warp(const DevNear& d, const double* Va, const double* Vb, const double* sgx, const double* sgw,
+                           int n, int lane, Fippi& F) {
+  fippi_zero(&F);
+  if (d.ncv == 0) {
+    double A[3], B[3], Ap[3], Bp[3], dV[3], a2;
+    fippi_far_setup(Va, Vb, A, B, Ap, Bp, dV, &a2);
+    for (int q = lane; q < n * n * n; q += 32) {
+      const int i1 = q / (n * n), j = (q / n) % n, l = q % n;
+      const double u = sgx[i1];
+      fippi_far_acc(A, B, Ap, Bp, dV, a2, u, u * sgx[j], sgx[l], sgw[i1] * sgw[j] * sgw[l] * u, F);
+    }
+  } else {
+    double Ea[9], Eb[9];
+    touch_edges(Va, Vb, d.perm_a, d.perm_b, Ea, Eb);
+    const int np = duffy_npts(d.ncv, n);
+    DuffyPt pt;
+    for (int q = lane; q < np; q += 32) {
+      duffy_pt(d.ncv, q, sgx, sgw, n, pt);
+      fippi_touch_acc(Ea, Eb, d.perm_a, d.perm_b, Va, pt, F);
+    }
+  }
+  fippi_warp_sum(F);
+}
+
 __global__ void __launch_bounds__(FIPPI_THREADS) fippi_kernel(const DevNear* near, const int* list, int n,
                                                                const double* pv, Fippi* out) {
   __shared__ double sgx[N_FIP], sgw[N_FIP];
@@ -347,17 +392,7 @@ __global__ void __launch_bounds__(FIPPI_THREADS) fippi_kernel(const DevNear* nea
       fippi_touch_acc(Ea, Eb, d.perm_a, d.perm_b, Va, pt, F);
     }
   }
-#pragma unroll
-  for (int m = 0; m < 9; m++) {
-    F.RM1[m] = warp_sum(F.RM1[m]);
-    F.R1[m] = warp_sum(F.R1[m]);
-    F.R2[m] = warp_sum(F.R2[m]);
-  }
-#pragma unroll
-  for (int m = 0; m < 3; m++) {
-    F.XM[m] = warp_sum(F.XM[m]);
-    F.XX[m] = warp_sum(F.XX[m]);
-  }
+  fippi_warp_sum(F);
   if (lane == 0) out[i] = F;
 }
 
@@ -1562,7 +1597,7 @@ gbem_status rhs_planewave_device(Geometry* g, double wr, double wi, const double
 //  vjp_far_kernel   far pairs (rRel > 4), one thread per pair: reverse-mode
 //                   derivative of the 6x6-rule integrals (adjoint.cuh), the
 //                   edge-length factors La Lb included.
-//  vjp_near_kernel  near and common-vertex pairs, one thread per (pair,
+//  vjp_near_kernel  near and common-vertex pairs, one warp per (pair,
 //                   vertex, coordinate) -- one vertex per pair follows from
 //                   translation invariance: central differences of the FP64
 //                   near-pair evaluation (static integrals recomputed for the
@@ -1682,10 +1717,13 @@ __global__ void __launch_bounds__(128) vjp_far_kernel(VjpFarArgs a, RegionArgs r
 
 // Re sum over regions and (Qa, Qb) of the pair's weighted values at the given
 // vertex positions -- the arithmetic of self_kernel, near_kernel and
-// td_touch_kernel for one pair in one thread (the static integrals at the
-// adjoint's 8-point rule), with the edge lengths taken from the positions
+// td_touch_kernel for one pair by one warp (the static integrals at the
+// adjoint's 8-point rule; the point sums of the static integrals, of the
+// self and touching Helmholtz integrals dealt to the lanes and reduced), with
+// the edge lengths taken from the positions.  Every lane returns the value.
 __device__ double near_pair_energy(const DevNear& d, const double* Va, const double* Vb, const double* sgA,
-                                   const double* sgB, const RegionArgs& ra, const cx<double> W[3][9]) {
+                                   const double* sgB, const RegionArgs& ra, const cx<double> W[3][9], int lane,
+                                   const double* sgx8, const double* sgw8) {
   const bool self = d.pa == d.pb;
   double fac[9];
   for (int ja = 0; ja < 3; ja++)
@@ -1714,7 +1752,8 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
     cx<double> H0[9], H1[9];
     if (self) {
       cx<double> MG[9], MP[9];
-      self_moments(Va, k, c_gx16, c_gw16, NT_SELF, MG, 0, 1);
+      self_moments(Va, k, c_gx16, c_gw16, NT_SELF, MG, lane, 32);
+      cx_warp_sum(MG, 9);
       for (int m = 0; m < 9; m++) MP[m] = mk(0.0, 0.0);
       for (int m = 0; m < 9; m++) {
         double c[9], dd[9];
@@ -1729,8 +1768,7 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
       cx<double> T[10];
       if (!sw) {
         if (!haveF) {
-          if (d.ncv == 0) fippi_far(Va, Vb, c_gx8, c_gw8, N_FIP_ADJ, &F);
-          else fippi_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, c_gx8, c_gw8, N_FIP_ADJ, &F);
+          fippi_warp(d, Va, Vb, sgx8, sgw8, N_FIP_ADJ, lane, F);
           haveF = true;
         }
         pair_moments<double, 1>(g, k, c_lo64, 6, MG, MP);
@@ -1739,7 +1777,9 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
       } else if (d.ncv == 0) {
         pair_moments<double, 0>(g, k, c_ho, HO_N * HO_N, MG, MP);
       } else {
-        td_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, k, c_gx12, c_gw12, N_TD, 0, 1, MG, T);
+        td_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, k, c_gx12, c_gw12, N_TD, lane, 32, MG, T);
+        cx_warp_sum(MG, 9);
+        cx_warp_sum(T, 10);
         for (int m = 0; m < 9; m++) MP[m] = mk(0.0, 0.0);
         td = true;
       }
@@ -1767,12 +1807,17 @@ struct VjpNearArgs {
 };
 
 __global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs ra) {
-  // 15 threads per pair: vertices 1..5 of the pair's six slots (panel a's
-  // vertex 0 follows from the others)
-  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long pair = tid / 15;
-  if (pair >= a.nnear) return;
-  const int dir = (int)(tid % 15), v = 1 + dir / 3, c = dir % 3;
+  // 15 warps per pair: vertices 1..5 of the pair's six slots (panel a's
+  // vertex 0 follows from the others) x 3 coordinates; each warp evaluates
+  // its two displaced pairs with the lanes over the cubature points
+  __shared__ double sgx[N_FIP_ADJ], sgw[N_FIP_ADJ];
+  if (threadIdx.x < N_FIP_ADJ) { sgx[threadIdx.x] = c_gx8[threadIdx.x]; sgw[threadIdx.x] = c_gw8[threadIdx.x]; }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long pair = wid / 15;
+  if (pair >= a.nnear) return;  // whole warps
+  const int dir = (int)(wid % 15), v = 1 + dir / 3, c = dir % 3;
   const VjpTables& t = a.t;
   const DevNear d = a.near[pair];
   const bool self = d.pa == d.pb;
@@ -1803,11 +1848,13 @@ __global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs
       if (t.pvi[3 * d.pa + q] == gv) Va[3 * q + c] += dv;
       if (t.pvi[3 * d.pb + q] == gv) Vb[3 * q + c] += dv;
     }
-    E[s] = near_pair_energy(d, Va, Vb, sgA, sgB, ra, W);
+    E[s] = near_pair_energy(d, Va, Vb, sgA, sgB, ra, W, lane, sgx, sgw);
   }
   const double dE = (E[0] - E[1]) / (2.0 * h);
-  atomicAdd(&t.grad[3 * (size_t)gv + c], dE);
-  atomicAdd(&t.grad[3 * (size_t)g0 + c], -dE);
+  if (lane == 0) {
+    atomicAdd(&t.grad[3 * (size_t)gv + c], dE);
+    atomicAdd(&t.grad[3 * (size_t)g0 + c], -dE);
+  }
 }
 
 struct RhsVjpArgs {
@@ -1950,7 +1997,7 @@ gbem_status vertex_vjp_device(Geometry* g, double wr, double wi, const double* e
       VjpNearArgs na;
       na.t = t; na.near = db->near; na.nnear = db->nnear; na.bpe_a = fa.bpe_a; na.bpe_b = fa.bpe_b;
       na.rel_step = rel_step;
-      const long long n = 15LL * db->nnear;
+      const long long n = 15LL * 32 * db->nnear;  // one warp per (pair, displaced coordinate)
       vjp_near_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(na, ra);
       stats_launch(ST_OTHER);
     }
