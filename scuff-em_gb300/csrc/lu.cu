@@ -263,6 +263,9 @@ struct LeafArgs {
   int pc0, pc1;  // the enclosing panel's columns: the leaf's interchanges are applied to all of them
   int* ipiv;     // 0-based global pivot rows
   int* info;
+  // register leaves only: first apply the 16-column leaf just left of this
+  // one, U12 = L11^-1 A12 (rows c0-16 .. c0-1, stored) and A22 -= L21 U12
+  int fuse;
 };
 
 __global__ void __launch_bounds__(512) leaf_kernel(LeafArgs a) {
@@ -452,6 +455,43 @@ __global__ void __launch_bounds__(NT, 1) leaf_kernel_reg(LeafArgs a) {
   bool pend = false;
   int pd = 0, pp = 0;
   cx<float> xd = mk(0.0f, 0.0f), xp = xd;
+  __shared__ __align__(16) cx<float> u12[LEAF_W][LEAF_W + 1];
+  if (a.fuse) {
+    // the previous leaf's block row: U12 = L11^-1 A12 (L11 unit lower), every
+    // CTA for itself, then A22 -= L21 U12 on this CTA's rows
+    __shared__ __align__(16) cx<float> l11[LEAF_W][LEAF_W + 1];
+    const int lc = a.c0 - LEAF_W;
+    for (int q = tid; q < LEAF_W * LEAF_W; q += NT) {
+      const int i = q % LEAF_W, j = q / LEAF_W;
+      l11[i][j] = a.A[(lc + i) + (long long)(lc + j) * a.ld];
+      u12[i][j] = j < w ? a.A[(lc + i) + (long long)(a.c0 + j) * a.ld] : mk(0.0f, 0.0f);
+    }
+    __syncthreads();
+    if (tid < w) {
+      for (int i = 1; i < LEAF_W; i++) {
+        cx<float> acc = u12[i][tid];
+        for (int kk = 0; kk < i; kk++) acc = acc - l11[i][kk] * u12[kk][tid];
+        u12[i][tid] = acc;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < RT; t++) {
+      const int r = tid + t * NT;
+      if (r < nr) {
+        cx<float> l[LEAF_W];
+#pragma unroll
+        for (int i = 0; i < LEAF_W; i++) l[i] = a.A[(m0 + r) + (long long)(lc + i) * a.ld];
+#pragma unroll
+        for (int kk = 0; kk < LEAF_W; kk++) {
+          cx<float> acc = R[t][kk];
+#pragma unroll
+          for (int i = 0; i < LEAF_W; i++) acc = acc - l[i] * u12[i][kk];
+          R[t][kk] = acc;
+        }
+      }
+    }
+  }
   // candidates of column 0
   unsigned cvb = 0u;
   int crow = -1;
@@ -579,7 +619,8 @@ __global__ void __launch_bounds__(NT, 1) leaf_kernel_reg(LeafArgs a) {
     colp[pp] = xd;
     colp[pd] = xp;
   }
-  // no CTA leaves while another may still read its shared memory
+  // no CTA leaves while another may still read its shared memory (and every
+  // CTA has read A12 before it is overwritten with U12)
   cl.sync();
 #pragma unroll
   for (int t = 0; t < RT; t++) {
@@ -589,6 +630,11 @@ __global__ void __launch_bounds__(NT, 1) leaf_kernel_reg(LeafArgs a) {
       for (int k = 0; k < LEAF_W; k++)
         if (k < w) a.A[(m0 + r) + (long long)(a.c0 + k) * a.ld] = R[t][k];
   }
+  if (a.fuse && rank == 0)
+    for (int q = tid; q < LEAF_W * w; q += NT) {
+      const int i = q % LEAF_W, j = q / LEAF_W;
+      a.A[(a.c0 - LEAF_W + i) + (long long)(a.c0 + j) * a.ld] = u12[i][j];
+    }
 }
 
 // Row interchanges outside a panel, in two steps.  swap_compose (one CTA)
@@ -924,7 +970,19 @@ static int leaf_cluster_size(int N, int smem_optin) {
   return 0;
 }
 
+// The lowest recursion level's U12 solve and update inside the right leaf
+// (LeafArgs::fuse); GBEM_LU_FUSE=0 launches them as separate kernels.
+static bool leaf_fusion() {
+  static int f = -1;
+  if (f < 0) {
+    const char* e = getenv("GBEM_LU_FUSE");
+    f = (e && e[0] == '0') ? 0 : 1;
+  }
+  return f == 1;
+}
+
 static cudaError_t leaf_launch_shape(const LeafArgs& la, int CL, int shape, cudaStream_t s) {
+  if (la.fuse && la.Rr > 1024) return cudaErrorInvalidValue;  // register leaves only
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(CL);
   cfg.blockDim = dim3(shape == 1024 ? 1024 : 512);
@@ -980,6 +1038,7 @@ static int leaf_shape(const LeafArgs& la, int CL, cudaStream_t s) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     LeafArgs t = la;
+    t.fuse = 0;  // the scratch holds rows c0.. only
     t.ld = rows;
     t.A = scr - la.c0 - (long long)la.pc0 * rows;  // element (r, c) of the panel at scr[(r - c0) + (c - pc0) rows]
     t.ipiv = sp;
@@ -1011,11 +1070,11 @@ static int leaf_shape(const LeafArgs& la, int CL, cudaStream_t s) {
 }
 
 static cudaError_t leaf_launch(cx<float>* A, long long ld, int N, int c0, int w, int pc0, int pc1, int* ipiv, int* info,
-                               int CL, cudaStream_t s) {
+                               int CL, cudaStream_t s, int fuse = 0) {
   const int m = N - c0;
   LeafArgs la;
   la.A = A; la.ld = ld; la.N = N; la.c0 = c0; la.w = w; la.Rr = (m + CL - 1) / CL; la.ipiv = ipiv; la.info = info;
-  la.pc0 = pc0; la.pc1 = pc1;
+  la.pc0 = pc0; la.pc1 = pc1; la.fuse = fuse;
   return leaf_launch_shape(la, CL, leaf_shape(la, CL, s), s);
 }
 
@@ -1049,6 +1108,11 @@ static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, in
   cudaError_t e = rec_panel(A, ld, N, c, h, pc0, pc1, ipiv, info, CL, tcws, tcb, ds, s, launches);
   if (e != cudaSuccess) return e;
   const int wr = w - h, m2 = N - c - h;
+  if (h == LEAF_W && wr <= LEAF_W && leaf_fusion() && (m2 + CL - 1) / CL <= 1024) {
+    // lowest level: the right leaf applies the left one's U12 and update itself
+    ++*launches;
+    return leaf_launch(A, ld, N, c + h, wr, pc0, pc1, ipiv, info, CL, s, 1);
+  }
   const bool dm = ds && h % 32 == 0 && c % 32 == 0;
   const unsigned make = dm ? dinv_make_mask(ds, c, h) : 0u;
   if (dm)
@@ -1488,6 +1552,17 @@ __global__ void __launch_bounds__(256) trsv_coop(const cx<T>* A, long long lda, 
   }
 }
 
+// CTAs of the triangular solves: GBEM_TRSV_CTAS caps the grid (default: one
+// per SM, fewer when N is small)
+static int trsv_ctas() {
+  static int c = -1;
+  if (c < 0) {
+    const char* e = getenv("GBEM_TRSV_CTAS");
+    c = e ? std::max(0, atoi(e)) : 0;
+  }
+  return c;
+}
+
 template <typename T>
 static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, char trans, int nrhs, cx<T>* B, int ldb,
                               cx<T>* Y, cudaStream_t s) {
@@ -1517,6 +1592,7 @@ static gbem_status solve_impl(const cx<T>* A, int N, int ld, const int* d_perm, 
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trsv_coop<T, true>, 256, dsm);
       // 4 threads per row; one CTA per SM is enough to keep the reads in flight
       int G = std::max(1, std::min(nsm * std::max(per, 1), std::min(nsm, (4 * N + 255) / 256)));
+      if (trsv_ctas() > 0) G = std::max(1, std::min(G, trsv_ctas()));
       int Nn = N, bsn = bs, nrn = nr;
       const cx<T>* Ac = A;
       long long ldl = ld;
