@@ -1771,11 +1771,15 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
           fippi_warp(d, Va, Vb, sgx8, sgw8, N_FIP_ADJ, lane, F);
           haveF = true;
         }
-        pair_moments<double, 1>(g, k, c_lo64, 6, MG, MP);
+        pair_moments_part<double, true>(g, k, c_lo64, 6, lane, 32, MG, MP);
+        cx_warp_sum(MG, 9);
+        cx_warp_sum(MP, 9);
         add_taylor_terms(F, k, MG, MP);
         desing = true;
       } else if (d.ncv == 0) {
-        pair_moments<double, 0>(g, k, c_ho, HO_N * HO_N, MG, MP);
+        pair_moments_part<double, false>(g, k, c_ho, HO_N * HO_N, lane, 32, MG, MP);
+        cx_warp_sum(MG, 9);
+        cx_warp_sum(MP, 9);
       } else {
         td_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, k, c_gx12, c_gw12, N_TD, lane, 32, MG, T);
         cx_warp_sum(MG, 9);

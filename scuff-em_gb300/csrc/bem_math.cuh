@@ -185,6 +185,32 @@ GB_HD void pair_moments(const PairGeom<T>& g, cx<T> k, const T* rule, int npts, 
   }
 }
 
+// pair_moments with the npts x npts samples dealt out: this call adds the
+// samples q = p0, p0 + pstride, ... (q = i npts + j); the caller sums the
+// partial moments of all p0 (one lane each).
+template <typename T, bool DESING>
+GB_HD void pair_moments_part(const PairGeom<T>& g, cx<T> k, const T* rule, int npts, int p0, int pstride, cx<T>* MG,
+                             cx<T>* MP) {
+  for (int m = 0; m < 9; m++) { MG[m] = mk((T)0, (T)0); MP[m] = mk((T)0, (T)0); }
+  for (int q = p0; q < npts * npts; q += pstride) {
+    const int i = q / npts, j = q - i * npts;
+    const T u = rule[3 * i], v = rule[3 * i + 1], wi = rule[3 * i + 2];
+    const T up = rule[3 * j], vp = rule[3 * j + 1], wj = rule[3 * j + 2];
+    T R[3];
+    for (int c = 0; c < 3; c++) R[c] = g.D0[c] + u * g.Aa[c] + v * g.Ba[c] - up * g.Ab[c] - vp * g.Bb[c];
+    const T r2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+    cx<T> phi, psi;
+    if constexpr (DESING) desing_pp(r2, k, wj, &phi, &psi);
+    else helmholtz_pp(r2, k, wj, &phi, &psi);
+    const T a[3] = {wi, wi * u, wi * v}, b[3] = {(T)1, up, vp};
+    for (int al = 0; al < 3; al++)
+      for (int be = 0; be < 3; be++) {
+        MG[3 * al + be] = MG[3 * al + be] + (a[al] * b[be]) * phi;
+        MP[3 * al + be] = MP[3 * al + be] + (a[al] * b[be]) * psi;
+      }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Combination coefficients for one (Qa, Qb) choice.  ja, jb = local vertex
 // index of Q in each panel (mesh order).  Computed in double from the
