@@ -278,6 +278,7 @@ def run_batch(args):
     through gbem_solve_mixed_batch (up to four concurrent solves); the same
     jobs one at a time are timed once for comparison."""
     from gbem import solve_mixed_batch
+    from gbem.api import LUTuning
     geoms = batch_geometries()
     jobs = batch_jobs(geoms)
     t0 = time.perf_counter()
@@ -308,6 +309,7 @@ def run_batch(args):
                                  "N_range": [ns[0], ns[-1]], "geometries_per_1024_bucket": buckets,
                                  "jobs": len(jobs), "max_concurrent": 4},
                       "sequential_solves_per_s": len(jobs) / t_seq, "first_pass_s_incl_near_tables": t_warm,
+                      "lu_tuning": LUTuning(0),
                       "max_refine_sweeps": max(o[1] for o in out), "max_residual": max(o[2] for o in out)}))
 
 

@@ -194,6 +194,13 @@ gbem_status gbem_lu_trace_host(gbem_matrix *M, const void *B, int ldb, int ncols
  * pivot is exactly zero. */
 gbem_status gbem_lu_log_abs_det(gbem_matrix *M, double *logdet);
 
+/* The LU tuning choices made so far on device `device` (no reference
+ * counterpart; LAPACK has no tunables here), as JSON: the register leaf's
+ * threads per 64-row bucket of rows per CTA, and the complex-FP32 panel width
+ * per 1024-row bucket of N.  Writes at most cap bytes including the
+ * terminating NUL; returns GBEM_EINVAL if the text does not fit. */
+gbem_status gbem_lu_tuning(int device, char *buf, int cap);
+
 /* gbem_lu_solve without any device allocation.  No counterpart in the
  * reference (HMatrix::LUSolve runs LAPACK on host memory).  Same arguments
  * and results as gbem_lu_solve for complex128 and complex64 matrices; a real

@@ -1080,6 +1080,15 @@ gbem_status gbem_sp_solve_host(const void* AP, int N, int dtype, const int* ipiv
   return st;
 }
 
+gbem_status gbem_lu_tuning(int device, char* buf, int cap) {
+  if (!buf || cap <= 0) { set_error("gbem_lu_tuning: NULL or empty buffer"); return GBEM_EINVAL; }
+  CHECK_CUDA(cudaSetDevice(device), "cudaSetDevice");
+  const std::string j = lu_tuning_json();
+  if ((int)j.size() + 1 > cap) { set_error("gbem_lu_tuning: %d bytes needed", (int)j.size() + 1); return GBEM_EINVAL; }
+  memcpy(buf, j.c_str(), j.size() + 1);
+  return GBEM_OK;
+}
+
 gbem_status gbem_lu_log_abs_det(gbem_matrix* M, double* logdet) {
   if (!M || !logdet) { set_error("gbem_lu_log_abs_det: NULL argument"); return GBEM_EINVAL; }
   if (!M->factored) { set_error("gbem_lu_log_abs_det: matrix is not factored"); return GBEM_EINVAL; }

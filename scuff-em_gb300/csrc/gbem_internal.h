@@ -177,6 +177,8 @@ gbem_status residual_device(const void* dA, int lda, int dtype, int N, const dou
 gbem_status lu_solve_static_scratch(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs,
                                     void* hB, int ldb, cudaStream_t s);
 int lu_solve_noalloc_max_n(int dtype);
+// the LU tuning tables of the current device, as JSON
+std::string lu_tuning_json();
 
 // gemm_tc.cu: keep the calling host thread's LU factorisations off the
 // split-BF16 tensor-core updates (exact FP32 SIMT updates instead)

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <mutex>
+#include <string>
 #include <vector>
 #include "bem_math.cuh"
 #include "gbem_internal.h"
@@ -1000,6 +1001,12 @@ static cudaError_t leaf_launch_shape(const LeafArgs& la, int CL, int shape, cuda
   return cudaLaunchKernelEx(&cfg, leaf_kernel, la);
 }
 
+// Tuning tables, per device: the register leaf's shape per 64-row bucket of
+// rows per CTA, and the complex-FP32 panel width per 1024-row bucket of N.
+static std::mutex g_tune_mu;
+static std::vector<std::pair<long long, int>> g_leaf_tuned;   // (device * 1024 + bucket, threads)
+static std::vector<std::pair<long long, int>> g_panel_tuned;  // (device * 1024 + bucket, width)
+
 // Leaf shape autotuner.  For 512 < rows per CTA <= 1024 the leaf exists in
 // two register shapes, 1024 threads x 1 row and 512 threads x 2 rows, whose
 // order depends on the row count (45.7 vs 49.8 us for the latter at 960
@@ -1015,8 +1022,8 @@ static int leaf_shape(const LeafArgs& la, int CL, cudaStream_t s) {
     forced = e ? (atoi(e) == 1024 ? 1024 : 512) : 0;
   }
   if (forced) return forced;
-  static std::mutex mu;
-  static std::vector<std::pair<long long, int>> tuned;  // (device * 1024 + bucket, shape)
+  std::mutex& mu = g_tune_mu;
+  std::vector<std::pair<long long, int>>& tuned = g_leaf_tuned;
   int dev = 0;
   cudaGetDevice(&dev);
   const long long key = (long long)dev * 1024 + (la.Rr - 1) / 64;
@@ -1143,7 +1150,68 @@ static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, in
 
 template <typename T>
 static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info, cudaStream_t s, void** ws,
-                               size_t* ws_bytes) {
+                               size_t* ws_bytes, int force_w = 0);
+
+// Panel width of the complex-FP32 LU with cluster leaves, per device and
+// 1024-row bucket of N: 256 or 128, whichever factors a scratch copy of the
+// bucket's first matrix faster (2 runs each; 1024 <= N <= 8192 -- at N = 15360
+// 256 was measured best, and a scratch copy there would take 1.9 GB).
+// GBEM_LU_PANEL=128 or 256 fixes it.
+static int panel_width_c64(cx<float>* A, int N, int ld, cudaStream_t s, void** ws, size_t* ws_bytes) {
+  static int forced = -1;
+  if (forced < 0) {
+    const char* e = getenv("GBEM_LU_PANEL");
+    forced = e ? (atoi(e) == 128 ? 128 : 256) : 0;
+  }
+  if (forced) return forced;
+  if (N < 1024 || N > 8192) return 256;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const long long key = (long long)dev * 1024 + N / 1024;
+  {
+    std::lock_guard<std::mutex> l(g_tune_mu);
+    for (auto& t : g_panel_tuned)
+      if (t.first == key) return t.second;
+  }
+  int best = 256;
+  cx<float>* scr = nullptr;
+  int* sp = nullptr;
+  if (cudaMallocAsync((void**)&scr, sizeof(cx<float>) * (size_t)N * N, s) == cudaSuccess &&
+      cudaMallocAsync((void**)&sp, sizeof(int) * (size_t)N, s) == cudaSuccess) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float tbest = 1e30f;
+    for (int w : {256, 128}) {
+      float tw = 1e30f;
+      for (int rep = 0; rep < 2; rep++) {
+        int info = 0;
+        cudaMemcpy2DAsync(scr, (size_t)N * sizeof(cx<float>), A, (size_t)ld * sizeof(cx<float>),
+                          (size_t)N * sizeof(cx<float>), N, cudaMemcpyDeviceToDevice, s);
+        cudaEventRecord(e0, s);
+        const gbem_status st = factor_impl<float>(scr, N, N, sp, &info, s, ws, ws_bytes, w);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 1e30f;
+        if (st == GBEM_OK) cudaEventElapsedTime(&ms, e0, e1);
+        tw = std::min(tw, ms);
+      }
+      if (tw < tbest) { tbest = tw; best = w; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  cudaGetLastError();
+  if (scr) cudaFreeAsync(scr, s);
+  if (sp) cudaFreeAsync(sp, s);
+  std::lock_guard<std::mutex> l(g_tune_mu);
+  g_panel_tuned.emplace_back(key, best);
+  return best;
+}
+
+template <typename T>
+static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info, cudaStream_t s, void** ws,
+                               size_t* ws_bytes, int force_w) {
   int dev = 0, nsm = 0, smem_optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -1159,7 +1227,9 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   }
   // complex FP32: recursive panels with cluster leaves where the leaf rows fit
   const int leaf_cl = sizeof(T) == 4 ? leaf_cluster_size(N, smem_optin) : 0;
-  if (leaf_cl) w = 256;
+  if (leaf_cl)
+    w = force_w ? force_w
+                : (sizeof(T) == 4 ? panel_width_c64((cx<float>*)A, N, ld, s, ws, ws_bytes) : 256);
   if (w > N) w = std::max(1, N);
   R = std::max(R, 1);
   size_t smem = std::min((size_t)(R * panel_stride(w) + w) * esz, smem_cap);
@@ -1306,6 +1376,33 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     return GBEM_ETIMEOUT;
   }
   return GBEM_OK;
+}
+
+// The tuning tables as JSON (for the calling device), for reports.
+std::string lu_tuning_json() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> l(g_tune_mu);
+  std::string out = "{\"leaf_threads_by_rows_per_cta\": {";
+  bool first = true;
+  for (auto& t : g_leaf_tuned)
+    if (t.first / 1024 == dev) {
+      const long long b = t.first % 1024;
+      out += (first ? "" : ", ") + std::string("\"") + std::to_string(64 * b + 1) + "-" + std::to_string(64 * b + 64) +
+             "\": " + std::to_string(t.second);
+      first = false;
+    }
+  out += "}, \"panel_width_by_N\": {";
+  first = true;
+  for (auto& t : g_panel_tuned)
+    if (t.first / 1024 == dev) {
+      const long long b = t.first % 1024;
+      out += (first ? "" : ", ") + std::string("\"") + std::to_string(1024 * b) + "-" + std::to_string(1024 * b + 1023) +
+             "\": " + std::to_string(t.second);
+      first = false;
+    }
+  out += "}}";
+  return out;
 }
 
 gbem_status lu_factor_device(void* dA, int N, int ld, int dtype, int* d_ipiv, int* h_info, cudaStream_t s, void** ws,

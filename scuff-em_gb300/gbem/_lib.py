@@ -19,7 +19,7 @@ STATUS_NAMES = {0: "GBEM_OK", 1: "GBEM_EINVAL", 2: "GBEM_ENOMEM", 3: "GBEM_ECUDA
 
 #: every symbol include/gbem.h declares
 EXPORTS = [
-    "gbem_vertex_vjp_region", "gbem_power_emt_grad", "gbem_solve_refined", "gbem_lu_log_abs_det", "gbem_assemble_block_packed_host", "gbem_sp_factor_host", "gbem_sp_solve_host",
+    "gbem_vertex_vjp_region", "gbem_power_emt_grad", "gbem_solve_refined", "gbem_lu_log_abs_det", "gbem_lu_tuning", "gbem_assemble_block_packed_host", "gbem_sp_factor_host", "gbem_sp_solve_host",
     "gbem_last_error", "gbem_version", "gbem_geometry_create", "gbem_geometry_destroy", "gbem_geometry_num_bfs",
     "gbem_geometry_edges", "gbem_geometry_near_counts", "gbem_matrix_create", "gbem_matrix_destroy",
     "gbem_matrix_device_ptr", "gbem_matrix_download", "gbem_matrix_upload", "gbem_assemble", "gbem_assemble_host",
@@ -80,6 +80,7 @@ def lib():
             "gbem_stats": ([I, P, P], I), "gbem_geometry_set_stream": ([P, P], I),
             "gbem_lu_solve_noalloc": ([P, ctypes.c_char, I, P, I], I),
             "gbem_lu_log_abs_det": ([P, P], I),
+            "gbem_lu_tuning": ([I, P, I], I),
             "gbem_solve_refined": ([P, D, D, P, P, I, P, I, P, I, D, I, P, P], I),
             "gbem_vertex_vjp_region": ([P, D, D, P, P, I, I, P, I, P, I, D, P], I),
             "gbem_power_emt_grad": ([P, D, D, P, P, I, P, I, P, I], I),

