@@ -1315,7 +1315,13 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
       StatTimer tt(ST_PANEL, s);
       const int h = wc / 2;
       const size_t hsm = (size_t)(2 * h + 32) * 33 * esz;
-      trsm_blocked<T><<<(nrest + 31) / 32, 256, hsm, s>>>(A, ld, c0, h, cb, N, dinv, dinv_make_mask(&ds, c0, h));
+      // blocks the recursion left uninverted (the last one): inverted once
+      // here rather than by every CTA of the wide solves below
+      if (dinv_make_mask(&ds, c0, wc)) {
+        tri_inv_blocks<T><<<wc / 32, 256, 0, s>>>(A, ld, c0, dinv);
+        stats_launch(ST_PANEL);
+      }
+      trsm_blocked<T><<<(nrest + 31) / 32, 256, hsm, s>>>(A, ld, c0, h, cb, N, dinv, 0u);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
       stats_launch(ST_PANEL);
       cx<float>* B2 = (cx<float>*)(A + (c0 + h) + (long long)cb * ld);
@@ -1328,7 +1334,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
         gemm_simt<float><<<dim3((h + 63) / 64, (nrest + 63) / 64), 256, 0, s>>>(B2, ld, L21h, ld, X1, ld, h, nrest, h);
         stats_launch(ST_PANEL);
       }
-      trsm_blocked<T><<<(nrest + 31) / 32, 256, hsm, s>>>(A, ld, c0 + h, h, cb, N, dinv, dinv_make_mask(&ds, c0 + h, h));
+      trsm_blocked<T><<<(nrest + 31) / 32, 256, hsm, s>>>(A, ld, c0 + h, h, cb, N, dinv, 0u);
       stats_launch(ST_PANEL);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
       split = true;
