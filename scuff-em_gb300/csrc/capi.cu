@@ -71,6 +71,15 @@ static void stats_collect() {
 gbem_status rhs_planewave_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, const double* E0,
                                  const double* nh, void* d_rhs, cudaStream_t s);
 
+bool pdl_enabled() {
+  static int p = -1;
+  if (p < 0) {
+    const char* e = getenv("GBEM_PDL");
+    p = (e && e[0] == '0') ? 0 : 1;
+  }
+  return p == 1;
+}
+
 cudaError_t allow_max_smem_raw(const void* kernel) {
   static std::mutex mu;
   static std::vector<std::pair<int, const void*>> done;

@@ -214,4 +214,32 @@ template <typename K> inline cudaError_t allow_max_smem(K* kernel) { return allo
 void set_error(const char* fmt, ...);
 gbem_status cuda_status(cudaError_t e, const char* what);
 
+// Programmatic dependent launch for the LU's chains of small kernels: a kernel
+// launched with launch_pdl may be scheduled while the previous kernel of the
+// stream still runs (that kernel's CTAs call pdl_trigger once resident), and
+// it calls pdl_wait -- which returns once the previous grid has completed and
+// its memory is visible -- before its first access to global memory.  That
+// hides the launch latency between dependent kernels.  pdl_wait is a no-op in
+// a kernel launched without the attribute.  GBEM_PDL=0 turns the attribute off.
+bool pdl_enabled();
+#ifdef __CUDACC__
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+#endif
+
 }  // namespace gbem

@@ -136,6 +136,8 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16* hi, __nv_bflo
 // padded past 6k) is written with contiguous 8-byte stores.
 __global__ void __launch_bounds__(256) pack_a(const cx<float>* A, long long lda, int m, int k, int Kp,
                                               __nv_bfloat16* out) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ cx<float> t[256][17];
   const int i0 = blockIdx.x * 16;
   for (int q = threadIdx.x; q < 16 * k; q += blockDim.x) {
@@ -169,6 +171,8 @@ __global__ void __launch_bounds__(256) pack_a(const cx<float>* A, long long lda,
 }
 
 __global__ void pack_b(const cx<float>* B, long long ldb, int k, int n, int Kp, __nv_bfloat16* out) {
+  pdl_wait();
+  pdl_trigger();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= (long long)k * n) return;
   int kk = (int)(t % k), j = (int)(t / k);
@@ -184,6 +188,8 @@ __global__ void pack_b(const cx<float>* B, long long ldb, int k, int n, int Kp, 
 }
 
 __global__ void zero_pad(__nv_bfloat16* out, long long rows, int K6, int Kp) {
+  pdl_wait();
+  pdl_trigger();
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   int w = Kp - K6;
   if (w <= 0 || t >= rows * w) return;
@@ -199,6 +205,8 @@ __global__ void __launch_bounds__(320, 1) tc_gemm_kernel(const __grid_constant__
                                                           const __grid_constant__ CUtensorMap mapB, cx<float>* C,
                                                           long long ldc, int m, int n, int kblocks, int mt,
                                                           int ntiles) {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   uintptr_t base = ((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023;
   unsigned char* tiles = (unsigned char*)base;
@@ -388,11 +396,11 @@ bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long l
   __nv_bfloat16* pb = pa + (size_t)m * Kp;
   if (k > 256) return false;
   long long tb = (long long)k * n;
-  pack_a<<<(unsigned)((m + 15) / 16), 256, 0, s>>>(A, lda, m, k, Kp, pa);
-  pack_b<<<(unsigned)((tb + 255) / 256), 256, 0, s>>>(B, ldb, k, n, Kp, pb);
+  launch_pdl(pack_a, dim3((unsigned)((m + 15) / 16)), dim3(256), 0, s, A, lda, m, k, Kp, pa);
+  launch_pdl(pack_b, dim3((unsigned)((tb + 255) / 256)), dim3(256), 0, s, B, ldb, k, n, Kp, pb);
   if (Kp > 6 * k) {
     long long pw = (long long)(Kp - 6 * k);
-    zero_pad<<<(unsigned)(((long long)2 * n * pw + 255) / 256), 256, 0, s>>>(pb, 2LL * n, 6 * k, Kp);
+    launch_pdl(zero_pad, dim3((unsigned)(((long long)2 * n * pw + 255) / 256)), dim3(256), 0, s, pb, 2LL * n, 6 * k, Kp);
   }
   CUtensorMap ma, mb;
   if (!make_map(&ma, pa, m, Kp, tc::BM) || !make_map(&mb, pb, 2 * n, Kp, tc::BN)) return false;
@@ -410,7 +418,8 @@ bool tc_gemm_update(cx<float>* C, long long ldc, const cx<float>* A, long long l
   }
   const int mt = (m + tc::BM - 1) / tc::BM, ntn = (2 * n + tc::BN - 1) / tc::BN;
   const int ntiles = mt * ntn;
-  tc_gemm_kernel<<<std::min(ntiles, nsm), 320, tc::SMEM_BYTES, s>>>(ma, mb, C, ldc, m, n, Kp / tc::BK, mt, ntiles);
+  launch_pdl(tc_gemm_kernel, dim3(std::min(ntiles, nsm)), dim3(320), (size_t)tc::SMEM_BYTES, s, ma, mb, C, ldc, m, n,
+             Kp / tc::BK, mt, ntiles);
   *err = cudaGetLastError();
   return *err == cudaSuccess;
 }

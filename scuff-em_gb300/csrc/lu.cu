@@ -270,6 +270,8 @@ struct LeafArgs {
 };
 
 __global__ void __launch_bounds__(512) leaf_kernel(LeafArgs a) {
+  pdl_wait();
+  pdl_trigger();
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<float>* rows = reinterpret_cast<cx<float>*>(smem_raw);  // [Rr][LEAF_STRIDE]
@@ -419,6 +421,8 @@ __device__ __forceinline__ void warp_cand(unsigned vb, int row, unsigned& wvb, i
 
 template <int RT, int NT>
 __global__ void __launch_bounds__(NT, 1) leaf_kernel_reg(LeafArgs a) {
+  pdl_wait();
+  pdl_trigger();
   cg::cluster_group cl = cg::this_cluster();
   __shared__ Cand pub[2];
   __shared__ __align__(16) cx<float> prow[2][LEAF_W];
@@ -649,6 +653,8 @@ __global__ void __launch_bounds__(NT, 1) leaf_kernel_reg(LeafArgs a) {
 constexpr int SWAP_HASH = 1024;  // >= 2 x the widest panel (256)
 
 __global__ void __launch_bounds__(256) swap_compose(const int* ipiv, int r0, int r1, int* mv, int* mv_n) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ int psrc[256];
   __shared__ int hkey[SWAP_HASH], hval[SWAP_HASH];
   __shared__ int cnt;
@@ -694,6 +700,8 @@ __global__ void __launch_bounds__(256) swap_compose(const int* ipiv, int r0, int
 template <typename T>
 __global__ void __launch_bounds__(256) swap_apply(cx<T>* A, long long ld, const int* mv, const int* mv_n, int cb, int ce,
                                                   int skip0, int skip1) {
+  pdl_wait();
+  pdl_trigger();
   const int j = cb + (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (j >= ce || (j >= skip0 && j < skip1)) return;  // whole warps leave together
   const int n = *mv_n;
@@ -723,6 +731,8 @@ __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_
 
 template <typename T>
 __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c0, int w, int cb, int ce) {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][33]
   __shared__ __align__(16) cx<T> Lt[2][32][33];    // cp.async targets: element-aligned
@@ -795,6 +805,8 @@ __global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, long long ld, int c
 template <typename T>
 __global__ void __launch_bounds__(256) trsm_blocked(cx<T>* A, long long ld, int c0, int w, int cb, int ce, cx<T>* dinv,
                                                     unsigned make) {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* B = reinterpret_cast<cx<T>*>(smem_raw);  // [w][33]
   cx<T>* Lc = B + w * 33;                          // [w][33]: the column block of L at and below the diagonal
@@ -871,6 +883,8 @@ __global__ void __launch_bounds__(256) trsm_blocked(cx<T>* A, long long ld, int 
 // (w a multiple of 32), one CTA per block, into dinv's slots (see trsm_blocked)
 template <typename T>
 __global__ void __launch_bounds__(256) tri_inv_blocks(const cx<T>* A, long long ld, int c0, cx<T>* dinv) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ cx<T> L[32][33], X[32][33];
   const int r0 = c0 + 32 * blockIdx.x, tid = threadIdx.x;
   for (int q = tid; q < 1024; q += blockDim.x) {
@@ -894,6 +908,8 @@ __global__ void __launch_bounds__(256) tri_inv_blocks(const cx<T>* A, long long 
 template <typename T>
 __global__ void __launch_bounds__(256) gemm_simt(cx<T>* C, long long ldc, const cx<T>* A, long long lda,
                                                  const cx<T>* B, long long ldb, int m, int n, int K) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ cx<T> As[16][64 + 1];
   __shared__ cx<T> Bs[16][64 + 1];
   const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
@@ -988,11 +1004,13 @@ static cudaError_t leaf_launch_shape(const LeafArgs& la, int CL, int shape, cuda
   cfg.gridDim = dim3(CL);
   cfg.blockDim = dim3(shape == 1024 ? 1024 : 512);
   cfg.stream = s;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = CL; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   if (la.Rr <= 1024 && shape == 1024) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<1, 1024>, la);
   if (la.Rr <= 512) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<1, 512>, la);
   if (la.Rr <= 1024) return cudaLaunchKernelEx(&cfg, leaf_kernel_reg<2, 512>, la);
@@ -1123,10 +1141,10 @@ static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, in
   const bool dm = ds && h % 32 == 0 && c % 32 == 0;
   const unsigned make = dm ? dinv_make_mask(ds, c, h) : 0u;
   if (dm)
-    trsm_blocked<float><<<(wr + 31) / 32, 256, (size_t)(2 * h + 32) * 33 * sizeof(cx<float>), s>>>(
+    launch_pdl(trsm_blocked<float>, dim3((wr + 31) / 32), dim3(256), (size_t)(2 * h + 32) * 33 * sizeof(cx<float>), s, 
         A, ld, c, h, c + h, c + w, ds->dinv, make);
   else
-    trsm_kernel<float><<<(wr + 31) / 32, 256, (size_t)h * 33 * sizeof(cx<float>), s>>>(A, ld, c, h, c + h, c + w);
+    launch_pdl(trsm_kernel<float>, dim3((wr + 31) / 32), dim3(256), (size_t)h * 33 * sizeof(cx<float>), s, A, ld, c, h, c + h, c + w);
   ++*launches;
   if (m2 > 0) {
     cx<float>* C = A + (c + h) + (long long)(c + h) * ld;
@@ -1140,7 +1158,7 @@ static cudaError_t rec_panel(cx<float>* A, long long ld, int N, int c, int w, in
       if (done) *launches += 3;
     }
     if (!done) {
-      gemm_simt<float><<<dim3((m2 + 63) / 64, (wr + 63) / 64), 256, 0, s>>>(C, ld, L21, ld, U12, ld, m2, wr, h);
+      launch_pdl(gemm_simt<float>, dim3(dim3((m2 + 63) / 64, (wr + 63) / 64)), dim3(256), 0, s, C, ld, L21, ld, U12, ld, m2, wr, h);
       ++*launches;
     }
   }
@@ -1297,8 +1315,8 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
         if (e != cudaSuccess) return cuda_status(e, "panel_kernel");
       }
       // interchanges to the left and right of the panel
-      swap_compose<<<1, 256, 0, s>>>(d_ipiv, c0, c0 + wc, swap_mv, swap_n);
-      swap_apply<T><<<(unsigned)((32LL * N + 255) / 256), 256, 0, s>>>(A, ld, swap_mv, swap_n, 0, N, c0, c0 + wc);
+      launch_pdl(swap_compose, dim3(1), dim3(256), 0, s, d_ipiv, c0, c0 + wc, swap_mv, swap_n);
+      launch_pdl(swap_apply<T>, dim3((unsigned)((32LL * N + 255) / 256)), dim3(256), 0, s, A, ld, swap_mv, swap_n, 0, N, c0, c0 + wc);
       stats_launch(ST_PANEL, 2);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "row interchanges");
     }
@@ -1318,10 +1336,10 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
       // blocks the recursion left uninverted (the last one): inverted once
       // here rather than by every CTA of the wide solves below
       if (dinv_make_mask(&ds, c0, wc)) {
-        tri_inv_blocks<T><<<wc / 32, 256, 0, s>>>(A, ld, c0, dinv);
+        launch_pdl(tri_inv_blocks<T>, dim3(wc / 32), dim3(256), 0, s, A, ld, c0, dinv);
         stats_launch(ST_PANEL);
       }
-      trsm_blocked<T><<<(nrest + 31) / 32, 256, hsm, s>>>(A, ld, c0, h, cb, N, dinv, 0u);
+      launch_pdl(trsm_blocked<T>, dim3((nrest + 31) / 32), dim3(256), hsm, s, A, ld, c0, h, cb, N, dinv, 0u);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
       stats_launch(ST_PANEL);
       cx<float>* B2 = (cx<float>*)(A + (c0 + h) + (long long)cb * ld);
@@ -1331,10 +1349,10 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
         stats_launch(ST_PANEL, 3);
       } else {
         if (e != cudaSuccess) return cuda_status(e, "tensor-core update");
-        gemm_simt<float><<<dim3((h + 63) / 64, (nrest + 63) / 64), 256, 0, s>>>(B2, ld, L21h, ld, X1, ld, h, nrest, h);
+        launch_pdl(gemm_simt<float>, dim3(dim3((h + 63) / 64, (nrest + 63) / 64)), dim3(256), 0, s, B2, ld, L21h, ld, X1, ld, h, nrest, h);
         stats_launch(ST_PANEL);
       }
-      trsm_blocked<T><<<(nrest + 31) / 32, 256, hsm, s>>>(A, ld, c0 + h, h, cb, N, dinv, 0u);
+      launch_pdl(trsm_blocked<T>, dim3((nrest + 31) / 32), dim3(256), hsm, s, A, ld, c0 + h, h, cb, N, dinv, 0u);
       stats_launch(ST_PANEL);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
       split = true;
@@ -1346,14 +1364,14 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
         make = dinv_make_mask(&ds, c0, wc);  // blocks no recursive solve inverted yet
       } else if (dm) {
         // the grid panel has no recursive solves: invert the panel's blocks first
-        tri_inv_blocks<T><<<wc / 32, 256, 0, s>>>(A, ld, c0, dinv);
+        launch_pdl(tri_inv_blocks<T>, dim3(wc / 32), dim3(256), 0, s, A, ld, c0, dinv);
         stats_launch(ST_PANEL);
       }
       stats_launch(ST_PANEL);
       if (dm)
-        trsm_blocked<T><<<(nrest + 31) / 32, 256, tsm, s>>>(A, ld, c0, wc, cb, N, dinv, make);
+        launch_pdl(trsm_blocked<T>, dim3((nrest + 31) / 32), dim3(256), tsm, s, A, ld, c0, wc, cb, N, dinv, make);
       else
-        trsm_kernel<T><<<(nrest + 31) / 32, 256, tsm, s>>>(A, ld, c0, wc, cb, N);
+        launch_pdl(trsm_kernel<T>, dim3((nrest + 31) / 32), dim3(256), tsm, s, A, ld, c0, wc, cb, N);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "trsm");
     }
     StatTimer tg(ST_GEMM, s);
@@ -1369,7 +1387,7 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
     }
     if (!done) {
       dim3 grid((nrest + 63) / 64, (nrest + 63) / 64);
-      gemm_simt<T><<<grid, 256, 0, s>>>(C, ld, L21, ld, U12, ld, nrest, nrest, wc);
+      launch_pdl(gemm_simt<T>, dim3(grid), dim3(256), 0, s, C, ld, L21, ld, U12, ld, nrest, nrest, wc);
       stats_launch(ST_GEMM);
       if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "gemm");
     }
