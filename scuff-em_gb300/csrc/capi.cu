@@ -1413,7 +1413,8 @@ static gbem_status solve_mixed_impl(gbem_geometry* g, double omega_re, double om
     if (st == GBEM_OK) st = gbem_matrix_create(g, GBEM_C64, &F);
     if (st != GBEM_OK) return st;
     g->mixedM = M; g->mixedF = F;
-    size_t wsb = (size_t)N * nrhs * 16 * 4 + (size_t)N * nrhs * 8 + (size_t)N * 8 * 8 + (size_t)8 * 8 * N * 16 + 4096;
+    size_t wsb = (size_t)N * nrhs * 16 * 4 + (size_t)N * nrhs * 8 + (size_t)N * 8 * 8 +
+                 (size_t)RESID_MAX_SPLIT * 8 * N * 16 + 4096;
     cudaError_t e = cudaMalloc(&g->mixed_ws, wsb);
     if (e != cudaSuccess) return cuda_status(e, "gbem_solve_mixed alloc");
     g->mixed_nrhs = nrhs;

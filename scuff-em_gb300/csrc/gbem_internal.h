@@ -177,6 +177,9 @@ gbem_status residual_device(const void* dA, int lda, int dtype, int N, const dou
 gbem_status lu_solve_static_scratch(const void* dA, int N, int ld, int dtype, const int* d_perm, char trans, int nrhs,
                                     void* hB, int ldb, cudaStream_t s);
 int lu_solve_noalloc_max_n(int dtype);
+// column splits of the FP64 residual: its partial-sum workspace holds
+// RESID_MAX_SPLIT x 8 x N complex128
+constexpr int RESID_MAX_SPLIT = 32;
 // the LU tuning tables of the current device, as JSON
 std::string lu_tuning_json();
 

@@ -1974,7 +1974,13 @@ __global__ void residual_finish(const cx<double>* B, long long ldb, const cx<dou
 
 gbem_status residual_device(const void* dA, int lda, int dtype, int N, const double* dX, int ldx, const double* dB,
                             int ldb, int nrhs, double* dR, int ldr, void* part, cudaStream_t s) {
-  const int nsplit = 8;
+  // column splits: more partial sums put more rows x chunks in flight
+  // (GBEM_RESID_SPLIT, at most RESID_MAX_SPLIT)
+  static int nsplit = -1;
+  if (nsplit < 0) {
+    const char* ev = getenv("GBEM_RESID_SPLIT");
+    nsplit = ev ? std::max(1, std::min(RESID_MAX_SPLIT, atoi(ev))) : 24;
+  }
   int cchunk = (N + nsplit - 1) / nsplit;
   cudaError_t e;
   for (int r0 = 0; r0 < nrhs; r0 += 8) {
