@@ -408,6 +408,10 @@ __device__ void store_near(double* dst, int ja, int jb, cx<double> kk, cx<double
 // over the lanes and the moments reduced with shuffles
 __global__ void __launch_bounds__(128) self_kernel(const DevNear* near, const int* list, int n, const double* pv,
                                                    RegionArgs ra, double* nearval) {
+  // the 1-D rule in shared memory: the lanes read different nodes at once
+  __shared__ double sgx[NT_SELF], sgw[NT_SELF];
+  if (threadIdx.x < NT_SELF) { sgx[threadIdx.x] = c_gx16[threadIdx.x]; sgw[threadIdx.x] = c_gw16[threadIdx.x]; }
+  __syncthreads();
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n) return;  // whole warps exit together
   int i = list[warp];
@@ -421,7 +425,7 @@ __global__ void __launch_bounds__(128) self_kernel(const DevNear* near, const in
     cx<double> k = ra.k[r];
     if (k.re == 0.0 && k.im == 0.0) continue;
     cx<double> MG[9], MP[9];
-    self_moments(V, k, c_gx16, c_gw16, NT_SELF, MG, lane, 32);
+    self_moments(V, k, sgx, sgw, NT_SELF, MG, lane, 32);
     for (int m = 0; m < 9; m++) {
       for (int o = 16; o > 0; o >>= 1) {
         MG[m].re += __shfl_xor_sync(0xffffffff, MG[m].re, o);
@@ -1723,7 +1727,8 @@ __global__ void __launch_bounds__(128) vjp_far_kernel(VjpFarArgs a, RegionArgs r
 // the edge lengths taken from the positions.  Every lane returns the value.
 __device__ double near_pair_energy(const DevNear& d, const double* Va, const double* Vb, const double* sgA,
                                    const double* sgB, const RegionArgs& ra, const cx<double> W[3][9], int lane,
-                                   const double* sgx8, const double* sgw8) {
+                                   const double* sgx8, const double* sgw8, const double* srule6,
+                                   const double* srule16) {
   const bool self = d.pa == d.pb;
   double fac[9];
   for (int ja = 0; ja < 3; ja++)
@@ -1752,7 +1757,7 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
     cx<double> H0[9], H1[9];
     if (self) {
       cx<double> MG[9], MP[9];
-      self_moments(Va, k, c_gx16, c_gw16, NT_SELF, MG, lane, 32);
+      self_moments(Va, k, srule16, srule16 + NT_SELF, NT_SELF, MG, lane, 32);
       cx_warp_sum(MG, 9);
       for (int m = 0; m < 9; m++) MP[m] = mk(0.0, 0.0);
       for (int m = 0; m < 9; m++) {
@@ -1771,7 +1776,7 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
           fippi_warp(d, Va, Vb, sgx8, sgw8, N_FIP_ADJ, lane, F);
           haveF = true;
         }
-        pair_moments_part<double, true>(g, k, c_lo64, 6, lane, 32, MG, MP);
+        pair_moments_part<double, true>(g, k, srule6, 6, lane, 32, MG, MP);
         cx_warp_sum(MG, 9);
         cx_warp_sum(MP, 9);
         add_taylor_terms(F, k, MG, MP);
@@ -1814,8 +1819,11 @@ __global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs
   // 15 warps per pair: vertices 1..5 of the pair's six slots (panel a's
   // vertex 0 follows from the others) x 3 coordinates; each warp evaluates
   // its two displaced pairs with the lanes over the cubature points
-  __shared__ double sgx[N_FIP_ADJ], sgw[N_FIP_ADJ];
+  // the rules in shared memory: the lanes read different nodes at once
+  __shared__ double sgx[N_FIP_ADJ], sgw[N_FIP_ADJ], srule6[18], srule16[2 * NT_SELF];
   if (threadIdx.x < N_FIP_ADJ) { sgx[threadIdx.x] = c_gx8[threadIdx.x]; sgw[threadIdx.x] = c_gw8[threadIdx.x]; }
+  if (threadIdx.x < 18) srule6[threadIdx.x] = c_lo64[threadIdx.x];
+  if (threadIdx.x < NT_SELF) { srule16[threadIdx.x] = c_gx16[threadIdx.x]; srule16[NT_SELF + threadIdx.x] = c_gw16[threadIdx.x]; }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -1852,7 +1860,7 @@ __global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs
       if (t.pvi[3 * d.pa + q] == gv) Va[3 * q + c] += dv;
       if (t.pvi[3 * d.pb + q] == gv) Vb[3 * q + c] += dv;
     }
-    E[s] = near_pair_energy(d, Va, Vb, sgA, sgB, ra, W, lane, sgx, sgw);
+    E[s] = near_pair_energy(d, Va, Vb, sgA, sgB, ra, W, lane, sgx, sgw, srule6, srule16);
   }
   const double dE = (E[0] - E[1]) / (2.0 * h);
   if (lane == 0) {
