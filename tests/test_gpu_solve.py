@@ -171,9 +171,11 @@ def test_gmres_refinement_on_an_ill_conditioned_matrix():
     assert res <= 1e-10
     # the mixed form solves its complex64 matrix: the refinement residual is
     # taken against it (rounding the matrix moves this ill-conditioned
-    # solution by ~1e-3, so it is not compared with the FP64 solution)
+    # solution by ~1e-3, so it is not compared with the FP64 solution); the
+    # sweeps stop at a 2-norm relative residual of 1e-10, so the largest entry
+    # of the residual may exceed 1e-10 of the largest entry of B by ~sqrt(N)
     M32 = G.AssembleBEMMatrix(w, precision="mixed").numpy().astype(np.complex128)
-    assert np.abs(M32 @ X - B).max() / np.abs(B).max() < 1e-9
+    assert np.abs(M32 @ X - B).max() / np.abs(B).max() < 1e-8
     # the refined form keeps the FP64 matrix and reaches the FP64 solution
     Xr, itr, resr = G.solve_refined(w, B, tol=1e-12, max_iter=12)
     print("refined sweeps %d, residual %.2e" % (itr, resr))
