@@ -541,6 +541,18 @@ def main():
             "hbm_gbs": (N * N * 8 + G.np_total * 64 * 8) / (far_ms * 1e-3) / 1e9, "hbm_peak_gbs": hbm_peak,
             "note": "float-float arithmetic issues ~640 FP32 instructions per sample against the 100-flop "
                     "convention"}
+    # solve and refinement: every sweep reads the complex64 factor once (its
+    # forward and backward triangular solves) and the complex64 matrix once
+    # (the FP64-accurate residual), against the HBM copy bandwidth
+    sol_ms = (stage_ms[4] + stage_ms[5]) / args.steps
+    if sol_ms > 0 and iters:
+        sweeps = statistics.median(iters)
+        nbytes = 2 * sweeps * N * N * 8
+        out["roofline_solve"] = {
+            "kernel": "trsv_coop (4 RHS) + residual_partial_df", "bound": "hbm",
+            "bytes_per_step": nbytes, "achieved_gbs": nbytes / (sol_ms * 1e-3) / 1e9, "peak_gbs": hbm_peak,
+            "frac": nbytes / (sol_ms * 1e-3) / 1e9 / hbm_peak, "sweeps": sweeps,
+            "note": "latency-bound: one grid barrier per 64-row block in each triangular solve"}
 
     # plain FP64 path (same geometry): assemble C128, LU, solve -- repeated,
     # with its own stage split
