@@ -1091,8 +1091,11 @@ gbem_status gbem_sp_solve_host(const void* AP, int N, int dtype, const int* ipiv
 
 gbem_status gbem_lu_tuning(int device, char* buf, int cap) {
   if (!buf || cap <= 0) { set_error("gbem_lu_tuning: NULL or empty buffer"); return GBEM_EINVAL; }
+  int prev = 0;
+  CHECK_CUDA(cudaGetDevice(&prev), "cudaGetDevice");
   CHECK_CUDA(cudaSetDevice(device), "cudaSetDevice");
   const std::string j = lu_tuning_json();
+  cudaSetDevice(prev);  // the calling thread's current device is left as it was
   if ((int)j.size() + 1 > cap) { set_error("gbem_lu_tuning: %d bytes needed", (int)j.size() + 1); return GBEM_EINVAL; }
   memcpy(buf, j.c_str(), j.size() + 1);
   return GBEM_OK;
