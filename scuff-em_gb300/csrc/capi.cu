@@ -71,13 +71,15 @@ static void stats_collect() {
 gbem_status rhs_planewave_device(Geometry* g, double wr, double wi, const double* eps, const double* mu, const double* E0,
                                  const double* nh, void* d_rhs, cudaStream_t s);
 
+static thread_local bool tl_pdl = false;
+void pdl_thread_on(bool on) { tl_pdl = on; }
 bool pdl_enabled() {
   static int p = -1;
   if (p < 0) {
     const char* e = getenv("GBEM_PDL");
     p = (e && e[0] == '0') ? 0 : 1;
   }
-  return p == 1;
+  return p == 1 && tl_pdl;
 }
 
 cudaError_t allow_max_smem_raw(const void* kernel) {

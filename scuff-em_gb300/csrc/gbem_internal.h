@@ -225,6 +225,10 @@ gbem_status cuda_status(cudaError_t e, const char* what);
 // hides the launch latency between dependent kernels.  pdl_wait is a no-op in
 // a kernel launched without the attribute.  GBEM_PDL=0 turns the attribute off.
 bool pdl_enabled();
+// per host thread: whether the current factorisation launches with the
+// attribute (set by the LU for its recursive-panel path, where it was
+// measured faster; the grid-panel path at N > 16384 ran 5 % slower with it)
+void pdl_thread_on(bool on);
 #ifdef __CUDACC__
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }

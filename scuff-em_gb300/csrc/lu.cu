@@ -1248,6 +1248,11 @@ static gbem_status factor_impl(cx<T>* A, int N, int ld, int* d_ipiv, int* h_info
   if (leaf_cl)
     w = force_w ? force_w
                 : (sizeof(T) == 4 ? panel_width_c64((cx<float>*)A, N, ld, s, ws, ws_bytes) : 256);
+  // programmatic dependent launch for the recursive-panel path only
+  pdl_thread_on(leaf_cl != 0);
+  struct PdlOff {
+    ~PdlOff() { pdl_thread_on(false); }
+  } pdl_off;
   if (w > N) w = std::max(1, N);
   R = std::max(R, 1);
   size_t smem = std::min((size_t)(R * panel_stride(w) + w) * esz, smem_cap);
