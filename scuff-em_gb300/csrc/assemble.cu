@@ -1653,6 +1653,26 @@ __device__ void vjp_weights(const VjpTables& t, int gpa, int gpb, int bpe_a, int
   }
 }
 
+// the three channels of vjp_weights for one (Qa, Qb) combination m = 3 ja + jb
+// (one lane each in the warp-per-pair adjoint kernel)
+__device__ void vjp_weights_m(const VjpTables& t, int gpa, int gpb, int bpe_a, int bpe_b, bool mirror, int m,
+                              cx<double>* w3) {
+  w3[0] = w3[1] = w3[2] = mk(0.0, 0.0);
+  const int ia = t.sbf[3 * gpa + m / 3], ib = t.sbf[3 * gpb + m % 3];
+  if (ia < 0 || ib < 0) return;
+  for (int r = 0; r < t.nrhs; r++) {
+    const cx<double>* L = t.lam + (long long)r * t.ldl;
+    const cx<double>* X = t.x + (long long)r * t.ldx;
+    for (int al = 0; al < bpe_a; al++)
+      for (int bt = 0; bt < bpe_b; bt++) {
+        const int ch = (al == 0 && bt == 0) ? 0 : (al != bt ? 1 : 2);
+        cx<double> w = conj_mul(L[ia + al], X[ib + bt]);
+        if (mirror) w = w + conj_mul(L[ib + bt], X[ia + al]);
+        w3[ch] = w3[ch] + w;
+      }
+  }
+}
+
 struct VjpFarArgs {
   VjpTables t;
   int offa, offb, npa, npb, bpe_a, bpe_b, sym;
@@ -1726,7 +1746,7 @@ __global__ void __launch_bounds__(128) vjp_far_kernel(VjpFarArgs a, RegionArgs r
 // self and touching Helmholtz integrals dealt to the lanes and reduced), with
 // the edge lengths taken from the positions.  Every lane returns the value.
 __device__ double near_pair_energy(const DevNear& d, const double* Va, const double* Vb, const double* sgA,
-                                   const double* sgB, const RegionArgs& ra, const cx<double> W[3][9], int lane,
+                                   const double* sgB, const RegionArgs& ra, const cx<double> (*W)[9], int lane,
                                    const double* sgx8, const double* sgw8, const double* srule6,
                                    const double* srule16) {
   const bool self = d.pa == d.pb;
@@ -1821,6 +1841,7 @@ __global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs
   // its two displaced pairs with the lanes over the cubature points
   // the rules in shared memory: the lanes read different nodes at once
   __shared__ double sgx[N_FIP_ADJ], sgw[N_FIP_ADJ], srule6[18], srule16[2 * NT_SELF];
+  __shared__ cx<double> sW[4][3][9];  // per warp: the pair's weights (kept out of registers)
   if (threadIdx.x < N_FIP_ADJ) { sgx[threadIdx.x] = c_gx8[threadIdx.x]; sgw[threadIdx.x] = c_gw8[threadIdx.x]; }
   if (threadIdx.x < 18) srule6[threadIdx.x] = c_lo64[threadIdx.x];
   if (threadIdx.x < NT_SELF) { srule16[threadIdx.x] = c_gx16[threadIdx.x]; srule16[NT_SELF + threadIdx.x] = c_gw16[threadIdx.x]; }
@@ -1848,8 +1869,13 @@ __global__ void __launch_bounds__(128) vjp_near_kernel(VjpNearArgs a, RegionArgs
     sgA[q] = t.sbf[3 * d.pa + q] >= 0 ? (t.ssl[3 * d.pa + q] > 0.0 ? 1.0 : -1.0) : 0.0;
     sgB[q] = t.sbf[3 * d.pb + q] >= 0 ? (t.ssl[3 * d.pb + q] > 0.0 ? 1.0 : -1.0) : 0.0;
   }
-  cx<double> W[3][9];
-  vjp_weights(t, d.pa, d.pb, a.bpe_a, a.bpe_b, !self, W);
+  cx<double>(*W)[9] = sW[threadIdx.x >> 5];
+  if (lane < 9) {
+    cx<double> w3[3];
+    vjp_weights_m(t, d.pa, d.pb, a.bpe_a, a.bpe_b, !self, lane, w3);
+    W[0][lane] = w3[0]; W[1][lane] = w3[1]; W[2][lane] = w3[2];
+  }
+  __syncwarp();
   const double h = a.rel_step * d.rmax;
   double E[2];
   for (int s = 0; s < 2; s++) {
