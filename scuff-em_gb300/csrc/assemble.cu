@@ -1750,17 +1750,20 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
                                    const double* sgx8, const double* sgw8, const double* srule6,
                                    const double* srule16) {
   const bool self = d.pa == d.pb;
-  double fac[9];
-  for (int ja = 0; ja < 3; ja++)
-    for (int jb = 0; jb < 3; jb++) {
-      double La = 0.0, Lb = 0.0;
-      for (int c = 0; c < 3; c++) {
-        const double ea = Va[3 * ((ja + 1) % 3) + c] - Va[3 * ((ja + 2) % 3) + c];
-        const double eb = Vb[3 * ((jb + 1) % 3) + c] - Vb[3 * ((jb + 2) % 3) + c];
-        La += ea * ea; Lb += eb * eb;
-      }
-      fac[3 * ja + jb] = sgA[ja] * sgB[jb] * sqrt(La) * sqrt(Lb);
+  // lane m < 9 forms the (Qa, Qb) combination m = 3 ja + jb; the sums over
+  // cubature points before it are spread over all lanes
+  const int m = lane < 9 ? lane : 0;
+  const int ja = m / 3, jb = m % 3;
+  double fac;
+  {
+    double La = 0.0, Lb = 0.0;
+    for (int c = 0; c < 3; c++) {
+      const double ea = Va[3 * ((ja + 1) % 3) + c] - Va[3 * ((ja + 2) % 3) + c];
+      const double eb = Vb[3 * ((jb + 1) % 3) + c] - Vb[3 * ((jb + 2) % 3) + c];
+      La += ea * ea; Lb += eb * eb;
     }
+    fac = sgA[ja] * sgB[jb] * sqrt(La) * sqrt(Lb);
+  }
   PairGeom<double> g;
   for (int c = 0; c < 3; c++) {
     g.D0[c] = Va[c] - Vb[c];
@@ -1774,18 +1777,16 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
     const cx<double> k = ra.k[r];
     if (k.re == 0.0 && k.im == 0.0) continue;
     const cx<double> m4ok2 = cdiv(mk(-4.0, 0.0), k * k);
-    cx<double> H0[9], H1[9];
+    cx<double> H0, H1;
     if (self) {
       cx<double> MG[9], MP[9];
       self_moments(Va, k, srule16, srule16 + NT_SELF, NT_SELF, MG, lane, 32);
       cx_warp_sum(MG, 9);
-      for (int m = 0; m < 9; m++) MP[m] = mk(0.0, 0.0);
-      for (int m = 0; m < 9; m++) {
-        double c[9], dd[9];
-        combo_coeffs(Va, Va, m / 3, m % 3, c, dd);
-        combine(MG, MP, c, dd, m4ok2, &H0[m], &H1[m]);
-        H1[m] = mk(0.0, 0.0);
-      }
+      for (int q = 0; q < 9; q++) MP[q] = mk(0.0, 0.0);
+      double c[9], dd[9];
+      combo_coeffs(Va, Va, ja, jb, c, dd);
+      combine(MG, MP, c, dd, m4ok2, &H0, &H1);
+      H1 = mk(0.0, 0.0);
     } else {
       const bool sw = hypot(k.re * d.rmax, k.im * d.rmax) > M_PI;
       cx<double> MG[9], MP[9];
@@ -1809,23 +1810,21 @@ __device__ double near_pair_energy(const DevNear& d, const double* Va, const dou
         td_touch(d.ncv, Va, Vb, d.perm_a, d.perm_b, k, c_gx12, c_gw12, N_TD, lane, 32, MG, T);
         cx_warp_sum(MG, 9);
         cx_warp_sum(T, 10);
-        for (int m = 0; m < 9; m++) MP[m] = mk(0.0, 0.0);
+        for (int q = 0; q < 9; q++) MP[q] = mk(0.0, 0.0);
         td = true;
       }
       VecMoments<double> vm;
       vec_moments(g, MG, MP, &vm);
-      for (int m = 0; m < 9; m++) {
-        vec_combine(g, vm, m / 3, m % 3, m4ok2, &H0[m], &H1[m]);
-        if (desing) H1[m] = H1[m] + mk(-0.079577471545947667884 * htimes_rm3(F, Va, Vb, m / 3, m % 3), 0.0);
-        if (td) H1[m] = td_h1(Va, Vb, T, m / 3, m % 3);
-      }
+      vec_combine(g, vm, ja, jb, m4ok2, &H0, &H1);
+      if (desing) H1 = H1 + mk(-0.079577471545947667884 * htimes_rm3(F, Va, Vb, ja, jb), 0.0);
+      if (td) H1 = td_h1(Va, Vb, T, ja, jb);
     }
-    for (int m = 0; m < 9; m++) {
-      const cx<double> v = ra.pf1[r] * (W[0][m] * H0[m]) + ra.pfc[r] * (W[1][m] * H1[m]) + ra.pf3[r] * (W[2][m] * H0[m]);
-      E += fac[m] * v.re;
+    if (lane < 9) {
+      const cx<double> v = ra.pf1[r] * (W[0][m] * H0) + ra.pfc[r] * (W[1][m] * H1) + ra.pf3[r] * (W[2][m] * H0);
+      E += fac * v.re;
     }
   }
-  return E;
+  return warp_sum(E);  // every lane returns the value
 }
 
 struct VjpNearArgs {
