@@ -186,3 +186,32 @@ def test_gmres_refinement_on_an_ill_conditioned_matrix():
     assert M.LUFactorize() == 0
     X64 = M.LUSolve(B)
     assert np.abs(Xr - X64).max() / np.abs(X64).max() < 1e-7
+
+
+def _bipyramid(center, r=0.3, h=0.4):
+    """Closed triangular bipyramid (6 outward-oriented panels, 9 edges): an
+    odd number of RWG functions for a PEC body."""
+    c = np.asarray(center, dtype=np.float64)
+    eq = [c + r * np.array([np.cos(a), np.sin(a), 0.0]) for a in (0.0, 2 * np.pi / 3, 4 * np.pi / 3)]
+    V = np.array([c + [0, 0, h], c - [0, 0, h]] + eq)
+    P = np.array([[0, 2, 3], [0, 3, 4], [0, 4, 2], [1, 3, 2], [1, 4, 3], [1, 2, 4]], dtype=np.int32)
+    return V, P
+
+
+def test_mixed_solve_with_odd_n():
+    """An odd number of basis functions (a PEC sphere and a PEC bipyramid,
+    N = 1920 + 9 = 1929): partial leaves, tile edges and the last triangular
+    block of the complex-FP32 path; the refined solution equals the FP64 one."""
+    import scipy.linalg as sl
+    from gbem import RWGGeometry, mesh
+    V, P = mesh.icosphere(3)
+    Vb, Pb = _bipyramid((2.2, 0.0, 0.0))
+    G = RWGGeometry([{"V": V, "P": P, "material": None}, {"V": Vb, "P": Pb, "material": None}])
+    assert G.TotalBFs % 2 == 1
+    w = 1.0
+    B = np.stack([G.AssembleRHSVector(w, e, n) for e, n in [((1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1))]],
+                 axis=1)
+    X, it, res = G.solve_mixed(w, B, tol=1e-10, max_iter=12)
+    assert res <= 1e-10
+    X64 = sl.solve(G.AssembleBEMMatrix(w).numpy(), B)
+    assert np.abs(X - X64).max() / np.abs(X64).max() < 1e-5
